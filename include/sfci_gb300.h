@@ -1,0 +1,154 @@
+/*
+ * sfci_gb300 — C ABI of the GB300 (sm_103a) truncated-Krylov hot path of SFCI.
+ *
+ * The reference (wlj89/SFCI) is a C++/OpenMP program whose hot path is the
+ * on-the-fly Hamiltonian sparse-matrix x sparse-vector product over bitstring
+ * determinants (SpMVMtply_bucket) and the sparse-vector algebra and Krylov
+ * drivers around it.  Its functions are plain C++ on global state; this header
+ * is the drop-in replacement boundary: plain pointers and sizes, status codes,
+ * opaque handles, device-resident vectors, one CUDA stream per context.
+ *
+ * Keys: a determinant is an occupation bitstring over num_orb spin orbitals
+ * (spin orbital b: spatial b >> 1, spin b & 1).  Keys cross the ABI as
+ * key_words() uint64 words per determinant, low word first (1 word for
+ * num_orb <= 64, 2 words for num_orb <= 128).
+ *
+ * Every call returns SFCI_OK (0) or a negative status; sfci_last_error()
+ * returns a message for the calling thread's last failure.  A context is used
+ * from one host thread at a time.
+ */
+#ifndef SFCI_GB300_H
+#define SFCI_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum sfci_status {
+  SFCI_OK = 0,
+  SFCI_ERR_ARG = -1,        /* invalid argument / size */
+  SFCI_ERR_IO = -2,         /* integral file missing or malformed */
+  SFCI_ERR_NOMEM = -3,      /* device memory budget exceeded (never an overflow) */
+  SFCI_ERR_CUDA = -4,       /* CUDA runtime error */
+  SFCI_ERR_CAPACITY = -5,   /* a vector's capacity is smaller than its contents */
+  SFCI_ERR_UNSUPPORTED = -6,/* input the implementation does not handle */
+  SFCI_ERR_NUMERIC = -7     /* non-positive-definite overlap, NaN, ... */
+};
+
+typedef struct sfci_ctx sfci_ctx;
+typedef struct sfci_vec sfci_vec;
+
+/* Options: the sfci.input keys that shape the hot path (src/main.cpp:58-124)
+ * plus the constants src/main.cpp:194-196 hard-codes.  Zero fields take the
+ * reference defaults. */
+typedef struct sfci_opts {
+  uint64_t Nd;             /* Krylov truncation (default 200000, src/main.cpp:23) */
+  uint64_t hpsi_cap;       /* capacity of H*v products (default 6e7, src/main.cpp:194) */
+  double coeff_cut;        /* post-merge magnitude cut (default 1e-5, src/main.cpp:196) */
+  uint64_t bucket_unit;    /* accepted and ignored: sizes come from prefix sums */
+  uint64_t mem_budget;     /* bytes of device scratch the SpMSpV may use (0: 85% of free) */
+  int verbose;             /* 1: print the reference's progress lines */
+  int reserved[7];
+} sfci_opts;
+
+const char* sfci_last_error(void);
+const char* sfci_status_name(int status);
+int sfci_version(void);
+
+/* ---- context ---------------------------------------------------------------
+ * Replaces load_integrals + the global set-up of src/main.cpp:170-223
+ * (src/functions.cpp:398-418, src/all.h:628).  Reads an _IN integral file. */
+int sfci_ctx_create(const char* in_path, int num_orb, int num_e, const sfci_opts* opts,
+                    sfci_ctx** out);
+int sfci_ctx_destroy(sfci_ctx* ctx);
+int sfci_key_words(const sfci_ctx* ctx);
+/* CUDA stream (cudaStream_t) all of the context's work is queued on. */
+int sfci_ctx_stream(const sfci_ctx* ctx, void** stream);
+int sfci_ctx_set_nd(sfci_ctx* ctx, uint64_t Nd);
+/* Kernel launches issued by this context so far (monotone counter). */
+int sfci_ctx_launch_count(const sfci_ctx* ctx, uint64_t* n);
+/* Timing probe: record CUDA event `slot` (0..15) on the context stream, and
+ * read the elapsed milliseconds between two recorded slots (synchronises). */
+int sfci_ctx_event_record(sfci_ctx* ctx, int slot);
+int sfci_ctx_event_elapsed(sfci_ctx* ctx, int slot_a, int slot_b, float* ms);
+/* Per-phase device time of the SpMSpV (ms, accumulated since the last reset);
+ * names: "count", "scatter", "partition", "merge", "select", "sort", "other". */
+int sfci_ctx_profile(sfci_ctx* ctx, int enable);
+int sfci_ctx_profile_read(sfci_ctx* ctx, const char* phase, double* ms, uint64_t* launches);
+int sfci_ctx_profile_reset(sfci_ctx* ctx);
+/* Statistics of the last SpMSpV: [0] input dets used, [1] generated terms,
+ * [2] merged unique dets, [3] survivors of the cut, [4] output length,
+ * [5] passes, [6] leaves, [7] leaves that took the global-memory path. */
+int sfci_ctx_last_stats(const sfci_ctx* ctx, uint64_t stats[8]);
+
+/* ---- sparse vectors (dynVec, src/all.h:150-625) ------------------------------ */
+int sfci_vec_create(sfci_ctx* ctx, uint64_t cap, sfci_vec** out);
+int sfci_vec_destroy(sfci_vec* v);
+int sfci_vec_len(const sfci_vec* v, uint64_t* len);
+int sfci_vec_cap(const sfci_vec* v, uint64_t* cap);
+/* Host -> device: keys (len * key_words words) and amplitudes.  The vector is
+ * sorted by key on the device if it is not already (dynVec keeps key order). */
+int sfci_vec_upload(sfci_vec* v, const uint64_t* keys, const double* amps, uint64_t len);
+/* Device -> host: copies min(len, cap) entries, reports len. */
+int sfci_vec_download(const sfci_vec* v, uint64_t* keys, double* amps, uint64_t cap,
+                      uint64_t* len);
+/* dynVec::naiveCopy (src/all.h:610-623); dst->cap must hold src->len. */
+int sfci_vec_copy(sfci_vec* dst, const sfci_vec* src);
+int sfci_vec_clear(sfci_vec* v);                                   /* setZeroVec :244 */
+
+/* ---- hot path ----------------------------------------------------------------
+ * SpMVMtply_bucket (src/functions.cpp:511-804, declared src/all.h:642):
+ *   out = top_cap( { k : |a_k| > coeff_cut } of merge( coeff * (H - lambda) * top_Nd(in) ) )
+ * sorted by key, with *diag = coeff * <top_Nd(in)| (H - lambda) |top_Nd(in)>
+ * evaluated before the cut.  An empty input leaves *diag untouched and
+ * empties out, as the reference does (:529-533). */
+int sfci_spmspv(sfci_ctx* ctx, const sfci_vec* in, sfci_vec* out, double lambda, double coeff,
+                double* diag);
+/* DiagCal_bit (src/bitstr.cpp:433-476) for `n` host keys. */
+int sfci_diag_elements(sfci_ctx* ctx, const uint64_t* keys, uint64_t n, double* out);
+/* calc_energy (src/functions.cpp:1272-1313): <psi|H|psi> on psi's support. */
+int sfci_energy(sfci_ctx* ctx, const sfci_vec* psi, double* energy);
+
+/* ---- sparse-vector algebra (src/all.h) ---------------------------------------- */
+int sfci_dot(sfci_ctx* ctx, const sfci_vec* x, const sfci_vec* y, double* out);   /* dot :317 */
+int sfci_norm(sfci_ctx* ctx, const sfci_vec* v, double* out);                      /* norm :249 */
+int sfci_scale(sfci_ctx* ctx, sfci_vec* v, double alpha);                          /* scalarMtply :260 */
+int sfci_normalize(sfci_ctx* ctx, sfci_vec* v);                                    /* normalize :267 */
+/* v = v + a*w, merged, top-v.cap by |amp|, key order (addTwo :407-480). */
+int sfci_add_two(sfci_ctx* ctx, sfci_vec* v, const sfci_vec* w, double a);
+/* v = a*x + b*y + c*z, merged, top-Nd by |amp|, drop |amp| <= 1e-14 (addThree :482-608). */
+int sfci_add_three(sfci_ctx* ctx, sfci_vec* v, const sfci_vec* x, const sfci_vec* y,
+                   const sfci_vec* z, double a, double b, double c);
+/* dst = top-dst.cap of src by |amp|, key order (shrinkFrom :281-299; src is left intact). */
+int sfci_shrink_from(sfci_ctx* ctx, sfci_vec* dst, const sfci_vec* src);
+/* dst = merge(sum_i coef[i] * vs[i]) (the restart combination, src/sparse_solver.cpp:492-509). */
+int sfci_combine(sfci_ctx* ctx, sfci_vec* dst, const sfci_vec* const* vs, const double* coef,
+                 int n);
+
+/* ---- Krylov drivers ------------------------------------------------------------
+ * sparse_krylov_solve_eigenval (src/sparse_solver.cpp:246-548): truncated
+ * Lanczos with full projected H and overlap S, generalised eigensolve, nearest
+ * root, restart vector truncated to Nd.  v is the start vector on entry and the
+ * final restart vector on return; energies[0..restarts) receive the per-restart
+ * "gsaes energy" (unused entries NaN); *final_e the closing calc_energy. */
+int sfci_lanczos_ground(sfci_ctx* ctx, sfci_vec* v, int Nl, int restarts, double* energies,
+                        double* final_e);
+/* minres_sp (src/minres.cpp:73-225, declared src/all.h:635-638): MINRES on
+ * (H - lambda) x = rhs with truncated sparse vectors.  *iters_done receives the
+ * iterations run. */
+int sfci_minres(sfci_ctx* ctx, const sfci_vec* rhs, const sfci_vec* guess, sfci_vec* result,
+                int iters, double tol, double lambda, int* iters_done);
+
+/* Generalised symmetric eigensolve K c = E S c (Eigen GSAES as used at
+ * src/sparse_solver.cpp:450), FP64 on the host: eigenvalues ascending,
+ * eigenvectors column-major with c^T S c = 1. */
+int sfci_gsaes(int n, const double* K, const double* S, double* evals, double* evecs);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SFCI_GB300_H */

@@ -1,0 +1,365 @@
+"""sfci_gb300 — GB300-native truncated-Krylov hot path of SFCI.
+
+Python mirror of the reference's operator interface, over the C ABI of
+``libsfci_gb300.so`` (``include/sfci_gb300.h``):
+
+* :class:`Context` — integrals + options; ``SpMVMtply_bucket`` (src/functions.cpp:511),
+  ``calc_energy`` (:1272), ``DiagCal_bit`` (src/bitstr.cpp:433),
+  ``sparse_krylov_solve_eigenval`` (src/sparse_solver.cpp:246), ``minres_sp``
+  (src/minres.cpp:73);
+* :class:`SpVec` — a device-resident ``dynVec`` (src/all.h:150) with the
+  reference's method names (``dot``, ``addTwo``, ``addThree``, ``shrinkFrom``,
+  ``norm``, ``normalize``, ``scalarMtply``, ``naiveCopy``, ``setZeroVec``).
+
+Keys are numpy ``uint64`` arrays: shape ``(n,)`` for up to 64 spin orbitals,
+``(n, 2)`` (low word first) for up to 128.  There is no CPU fallback: if the
+library is missing or its CUDA calls fail, calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+__all__ = ["Context", "SpVec", "SfciError", "load_library", "gsaes", "keys_from_ints", "ints_from_keys"]
+
+
+class SfciError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s: %s" % (status, msg))
+        self.status = status
+
+
+_LIB = None
+
+
+class Opts(C.Structure):
+    _fields_ = [("Nd", C.c_uint64), ("hpsi_cap", C.c_uint64), ("coeff_cut", C.c_double),
+                ("bucket_unit", C.c_uint64), ("mem_budget", C.c_uint64), ("verbose", C.c_int),
+                ("reserved", C.c_int * 7)]
+
+
+_u64p = np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+_vp = C.c_void_p
+
+
+def _sigs(L):
+    L.sfci_last_error.restype = C.c_char_p
+    L.sfci_status_name.restype = C.c_char_p
+    L.sfci_status_name.argtypes = [C.c_int]
+    L.sfci_ctx_create.argtypes = [C.c_char_p, C.c_int, C.c_int, C.POINTER(Opts), C.POINTER(_vp)]
+    L.sfci_ctx_destroy.argtypes = [_vp]
+    L.sfci_key_words.argtypes = [_vp]
+    L.sfci_ctx_stream.argtypes = [_vp, C.POINTER(_vp)]
+    L.sfci_ctx_set_nd.argtypes = [_vp, C.c_uint64]
+    L.sfci_ctx_launch_count.argtypes = [_vp, C.POINTER(C.c_uint64)]
+    L.sfci_ctx_event_record.argtypes = [_vp, C.c_int]
+    L.sfci_ctx_event_elapsed.argtypes = [_vp, C.c_int, C.c_int, C.POINTER(C.c_float)]
+    L.sfci_ctx_profile.argtypes = [_vp, C.c_int]
+    L.sfci_ctx_profile_read.argtypes = [_vp, C.c_char_p, C.POINTER(C.c_double), C.POINTER(C.c_uint64)]
+    L.sfci_ctx_profile_reset.argtypes = [_vp]
+    L.sfci_ctx_last_stats.argtypes = [_vp, C.POINTER(C.c_uint64)]
+    L.sfci_vec_create.argtypes = [_vp, C.c_uint64, C.POINTER(_vp)]
+    L.sfci_vec_destroy.argtypes = [_vp]
+    L.sfci_vec_len.argtypes = [_vp, C.POINTER(C.c_uint64)]
+    L.sfci_vec_cap.argtypes = [_vp, C.POINTER(C.c_uint64)]
+    L.sfci_vec_upload.argtypes = [_vp, _vp, _vp, C.c_uint64]
+    L.sfci_vec_download.argtypes = [_vp, _vp, _vp, C.c_uint64, C.POINTER(C.c_uint64)]
+    L.sfci_vec_copy.argtypes = [_vp, _vp]
+    L.sfci_vec_clear.argtypes = [_vp]
+    L.sfci_spmspv.argtypes = [_vp, _vp, _vp, C.c_double, C.c_double, C.POINTER(C.c_double)]
+    L.sfci_diag_elements.argtypes = [_vp, _vp, C.c_uint64, _vp]
+    L.sfci_energy.argtypes = [_vp, _vp, C.POINTER(C.c_double)]
+    L.sfci_dot.argtypes = [_vp, _vp, _vp, C.POINTER(C.c_double)]
+    L.sfci_norm.argtypes = [_vp, _vp, C.POINTER(C.c_double)]
+    L.sfci_scale.argtypes = [_vp, _vp, C.c_double]
+    L.sfci_normalize.argtypes = [_vp, _vp]
+    L.sfci_add_two.argtypes = [_vp, _vp, _vp, C.c_double]
+    L.sfci_add_three.argtypes = [_vp, _vp, _vp, _vp, _vp, C.c_double, C.c_double, C.c_double]
+    L.sfci_shrink_from.argtypes = [_vp, _vp, _vp]
+    L.sfci_combine.argtypes = [_vp, _vp, C.POINTER(_vp), _vp, C.c_int]
+    L.sfci_lanczos_ground.argtypes = [_vp, _vp, C.c_int, C.c_int, _vp, C.POINTER(C.c_double)]
+    L.sfci_minres.argtypes = [_vp, _vp, _vp, _vp, C.c_int, C.c_double, C.c_double, C.POINTER(C.c_int)]
+    L.sfci_gsaes.argtypes = [C.c_int, _vp, _vp, _vp, _vp]
+    for name in dir(L):
+        pass
+    return L
+
+
+def load_library(path: str | None = None, build: bool = True):
+    """Load libsfci_gb300.so (building it in-tree first when ``build``)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    p = path or os.environ.get("SFCI_GB300_LIB")
+    if p is None:
+        p = _build.build() if build else _build.LIB
+    if not os.path.exists(p):
+        raise ImportError("libsfci_gb300.so not found at %s; run sfci_gb300.build.build()" % p)
+    L = C.CDLL(p)
+    for fn in ("sfci_ctx_create", "sfci_last_error", "sfci_status_name", "sfci_ctx_destroy", "sfci_key_words",
+               "sfci_ctx_stream", "sfci_ctx_set_nd", "sfci_ctx_launch_count", "sfci_ctx_event_record",
+               "sfci_ctx_event_elapsed", "sfci_ctx_profile", "sfci_ctx_profile_read", "sfci_ctx_profile_reset",
+               "sfci_ctx_last_stats", "sfci_vec_create", "sfci_vec_destroy", "sfci_vec_len", "sfci_vec_cap",
+               "sfci_vec_upload", "sfci_vec_download", "sfci_vec_copy", "sfci_vec_clear", "sfci_spmspv",
+               "sfci_diag_elements", "sfci_energy", "sfci_dot", "sfci_norm", "sfci_scale", "sfci_normalize",
+               "sfci_add_two", "sfci_add_three", "sfci_shrink_from", "sfci_combine", "sfci_lanczos_ground",
+               "sfci_minres", "sfci_gsaes"):
+        getattr(L, fn)
+    _LIB = _sigs(L)
+    return _LIB
+
+
+def _check(st):
+    if st != 0:
+        L = _LIB
+        raise SfciError(L.sfci_status_name(st).decode(), L.sfci_last_error().decode())
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None and a.size else None
+
+
+def keys_from_ints(ints, words: int) -> np.ndarray:
+    """Python ints (determinant bitstrings) -> key array for ``words`` words."""
+    ints = [int(x) for x in ints]
+    if words == 1:
+        return np.array(ints, dtype=np.uint64)
+    a = np.zeros((len(ints), 2), dtype=np.uint64)
+    m = (1 << 64) - 1
+    for i, x in enumerate(ints):
+        a[i, 0] = x & m
+        a[i, 1] = x >> 64
+    return a
+
+
+def ints_from_keys(keys: np.ndarray):
+    keys = np.asarray(keys, dtype=np.uint64)
+    if keys.ndim == 1:
+        return [int(x) for x in keys]
+    return [int(lo) | (int(hi) << 64) for lo, hi in keys]
+
+
+def gsaes(K, S):
+    """FP64 generalised symmetric eigensolve K c = E S c (ascending, S-orthonormal)."""
+    L = load_library()
+    K = np.asfortranarray(np.asarray(K, dtype=np.float64))
+    S = np.asfortranarray(np.asarray(S, dtype=np.float64))
+    n = K.shape[0]
+    ev = np.zeros(n)
+    X = np.zeros((n, n), order="F")
+    _check(L.sfci_gsaes(n, K.ctypes.data_as(C.c_void_p), S.ctypes.data_as(C.c_void_p),
+                        ev.ctypes.data_as(C.c_void_p), X.ctypes.data_as(C.c_void_p)))
+    return ev, X
+
+
+class Context:
+    """Integrals + options + one CUDA stream (the reference's global state, made explicit)."""
+
+    def __init__(self, in_path: str, num_orb: int, num_e: int, Nd: int = 200000, hpsi_cap: int = 60000000,
+                 coeff_cut: float = 1e-5, mem_budget: int = 0, verbose: bool = False):
+        self.L = load_library()
+        o = Opts()
+        o.Nd = int(Nd)
+        o.hpsi_cap = int(hpsi_cap)
+        o.coeff_cut = float(coeff_cut)
+        o.mem_budget = int(mem_budget)
+        o.verbose = 1 if verbose else 0
+        h = _vp()
+        _check(self.L.sfci_ctx_create(in_path.encode(), int(num_orb), int(num_e), C.byref(o), C.byref(h)))
+        self.h = h
+        self.num_orb, self.num_e = num_orb, num_e
+        self.words = self.L.sfci_key_words(h)
+        self.Nd = int(Nd)
+        self.hpsi_cap = int(hpsi_cap)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.sfci_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # --- vectors
+    def vec(self, cap: int) -> "SpVec":
+        return SpVec(self, cap)
+
+    def vec_from(self, keys, amps, cap: int | None = None) -> "SpVec":
+        keys = np.ascontiguousarray(keys, dtype=np.uint64)
+        amps = np.ascontiguousarray(amps, dtype=np.float64)
+        v = SpVec(self, cap if cap is not None else max(1, len(amps)))
+        v.upload(keys, amps)
+        return v
+
+    def set_Nd(self, Nd: int):
+        _check(self.L.sfci_ctx_set_nd(self.h, int(Nd)))
+        self.Nd = int(Nd)
+
+    # --- hot path (reference names)
+    def SpMVMtply_bucket(self, vin: "SpVec", vout: "SpVec", lam: float, coeff: float, diag: float = 0.0) -> float:
+        d = C.c_double(diag)
+        _check(self.L.sfci_spmspv(self.h, vin.h, vout.h, float(lam), float(coeff), C.byref(d)))
+        return d.value
+
+    spmspv = SpMVMtply_bucket
+
+    def calc_energy(self, psi: "SpVec") -> float:
+        e = C.c_double()
+        _check(self.L.sfci_energy(self.h, psi.h, C.byref(e)))
+        return e.value
+
+    def DiagCal_bit(self, keys) -> np.ndarray:
+        keys = np.ascontiguousarray(keys, dtype=np.uint64)
+        n = keys.shape[0]
+        out = np.zeros(n)
+        _check(self.L.sfci_diag_elements(self.h, _ptr(keys), n, _ptr(out)))
+        return out
+
+    def sparse_krylov_solve_eigenval(self, v: "SpVec", Nl: int, num_restart: int):
+        en = np.full(num_restart, np.nan)
+        fe = C.c_double()
+        _check(self.L.sfci_lanczos_ground(self.h, v.h, int(Nl), int(num_restart), _ptr(en), C.byref(fe)))
+        return en, fe.value
+
+    def minres_sp(self, rhs: "SpVec", guess: "SpVec", result: "SpVec", iters: int, tol: float, lam: float) -> int:
+        done = C.c_int()
+        _check(self.L.sfci_minres(self.h, rhs.h, guess.h, result.h, int(iters), float(tol), float(lam),
+                                  C.byref(done)))
+        return done.value
+
+    def combine(self, dst: "SpVec", vecs, coef):
+        coef = np.ascontiguousarray(coef, dtype=np.float64)
+        arr = (_vp * len(vecs))(*[v.h for v in vecs])
+        _check(self.L.sfci_combine(self.h, dst.h, arr, _ptr(coef), len(vecs)))
+
+    # --- instrumentation
+    def launches(self) -> int:
+        n = C.c_uint64()
+        _check(self.L.sfci_ctx_launch_count(self.h, C.byref(n)))
+        return n.value
+
+    def stream(self) -> int:
+        s = _vp()
+        _check(self.L.sfci_ctx_stream(self.h, C.byref(s)))
+        return s.value or 0
+
+    def event_record(self, slot: int):
+        _check(self.L.sfci_ctx_event_record(self.h, int(slot)))
+
+    def event_elapsed(self, a: int, b: int) -> float:
+        ms = C.c_float()
+        _check(self.L.sfci_ctx_event_elapsed(self.h, int(a), int(b), C.byref(ms)))
+        return ms.value
+
+    def profile(self, enable: bool = True):
+        _check(self.L.sfci_ctx_profile(self.h, 1 if enable else 0))
+
+    def profile_read(self) -> dict:
+        out = {}
+        for ph in ("count", "scatter", "partition", "merge", "select", "sort", "other"):
+            ms = C.c_double()
+            n = C.c_uint64()
+            _check(self.L.sfci_ctx_profile_read(self.h, ph.encode(), C.byref(ms), C.byref(n)))
+            out[ph] = (ms.value, n.value)
+        return out
+
+    def profile_reset(self):
+        _check(self.L.sfci_ctx_profile_reset(self.h))
+
+    def last_stats(self) -> dict:
+        a = (C.c_uint64 * 8)()
+        _check(self.L.sfci_ctx_last_stats(self.h, a))
+        names = ["input_dets", "terms", "unique", "survivors", "out_len", "passes", "leaves", "big_leaves"]
+        return dict(zip(names, [int(x) for x in a]))
+
+
+class SpVec:
+    """Device-resident sparse vector (dynVec): keys ascending, FP64 amplitudes."""
+
+    def __init__(self, ctx: Context, cap: int):
+        self.ctx = ctx
+        self.L = ctx.L
+        h = _vp()
+        _check(self.L.sfci_vec_create(ctx.h, int(cap), C.byref(h)))
+        self.h = h
+        self.cap = int(cap)
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                self.L.sfci_vec_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+    @property
+    def len(self) -> int:
+        n = C.c_uint64()
+        _check(self.L.sfci_vec_len(self.h, C.byref(n)))
+        return n.value
+
+    def __len__(self):
+        return self.len
+
+    def upload(self, keys, amps):
+        keys = np.ascontiguousarray(keys, dtype=np.uint64)
+        amps = np.ascontiguousarray(amps, dtype=np.float64)
+        if self.ctx.words == 2 and keys.ndim != 2:
+            raise ValueError("128-bit keys need shape (n, 2)")
+        _check(self.L.sfci_vec_upload(self.h, _ptr(keys), _ptr(amps), len(amps)))
+        return self
+
+    def download(self):
+        n = self.len
+        w = self.ctx.words
+        keys = np.zeros((n, 2) if w == 2 else n, dtype=np.uint64)
+        amps = np.zeros(n)
+        got = C.c_uint64()
+        _check(self.L.sfci_vec_download(self.h, _ptr(keys), _ptr(amps), n, C.byref(got)))
+        return keys, amps
+
+    # dynVec method names (src/all.h)
+    def naiveCopy(self, src: "SpVec"):
+        _check(self.L.sfci_vec_copy(self.h, src.h))
+
+    def setZeroVec(self):
+        _check(self.L.sfci_vec_clear(self.h))
+
+    def dot(self, other: "SpVec") -> float:
+        d = C.c_double()
+        _check(self.L.sfci_dot(self.ctx.h, self.h, other.h, C.byref(d)))
+        return d.value
+
+    def norm(self) -> float:
+        d = C.c_double()
+        _check(self.L.sfci_norm(self.ctx.h, self.h, C.byref(d)))
+        return d.value
+
+    def scalarMtply(self, a: float):
+        _check(self.L.sfci_scale(self.ctx.h, self.h, float(a)))
+
+    def normalize(self):
+        _check(self.L.sfci_normalize(self.ctx.h, self.h))
+
+    def addTwo(self, w: "SpVec", a: float):
+        _check(self.L.sfci_add_two(self.ctx.h, self.h, w.h, float(a)))
+
+    def addThree(self, x: "SpVec", y: "SpVec", z: "SpVec", a: float, b: float, c: float):
+        _check(self.L.sfci_add_three(self.ctx.h, self.h, x.h, y.h, z.h, float(a), float(b), float(c)))
+
+    def shrinkFrom(self, src: "SpVec"):
+        _check(self.L.sfci_shrink_from(self.ctx.h, self.h, src.h))

@@ -1,0 +1,141 @@
+// Shared device/host helpers: determinant keys, bit arithmetic, hashing, status.
+//
+// A determinant is an occupation bitstring over N spin orbitals (src/all.h:90-91
+// uses one uint64, so N <= 64).  Here a key is W 64-bit words (W = 1 for N <= 64,
+// W = 2 for N <= 128).  Spin orbital b has spatial index b >> 1 and spin b & 1,
+// the layout the _IN converter writes (util/convert_fcidump.py:100-108).
+#pragma once
+
+#include <cstdint>
+#include <cstddef>
+#include <cuda_runtime.h>
+
+#include "../../include/sfci_gb300.h"
+
+#define SFCI_HD __host__ __device__ __forceinline__
+
+namespace sfci {
+
+typedef unsigned long long u64;
+
+struct K128 {
+  u64 lo, hi;
+};
+
+template <int W> struct KeyOf;
+template <> struct KeyOf<1> { typedef u64 T; };
+template <> struct KeyOf<2> { typedef K128 T; };
+
+// ---- key primitives -------------------------------------------------------
+
+SFCI_HD u64 kword(const u64& k, int) { return k; }
+SFCI_HD u64 kword(const K128& k, int w) { return w ? k.hi : k.lo; }
+
+SFCI_HD bool key_eq(const u64& a, const u64& b) { return a == b; }
+SFCI_HD bool key_eq(const K128& a, const K128& b) { return a.lo == b.lo && a.hi == b.hi; }
+SFCI_HD bool key_lt(const u64& a, const u64& b) { return a < b; }
+SFCI_HD bool key_lt(const K128& a, const K128& b) {
+  return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo);
+}
+SFCI_HD bool key_le(const u64& a, const u64& b) { return a <= b; }
+SFCI_HD bool key_le(const K128& a, const K128& b) { return !key_lt(b, a); }
+
+// An all-ones key would need every spin orbital occupied; contexts reject
+// num_e == num_orb, so it never names a determinant and marks empty slots.
+template <class KT> SFCI_HD KT key_empty();
+template <> SFCI_HD u64 key_empty<u64>() { return ~0ull; }
+template <> SFCI_HD K128 key_empty<K128>() { K128 k; k.lo = ~0ull; k.hi = ~0ull; return k; }
+
+SFCI_HD void key_flip(u64& k, int b) { k ^= (1ull << b); }
+SFCI_HD void key_flip(K128& k, int b) {
+  if (b < 64) k.lo ^= (1ull << b); else k.hi ^= (1ull << (b - 64));
+}
+SFCI_HD bool key_test(const u64& k, int b) { return (k >> b) & 1ull; }
+SFCI_HD bool key_test(const K128& k, int b) {
+  return b < 64 ? ((k.lo >> b) & 1ull) : ((k.hi >> (b - 64)) & 1ull);
+}
+
+// radix digit of the key: bits [shift, shift+8)
+SFCI_HD unsigned key_digit(const u64& k, int shift) { return (unsigned)(k >> shift) & 0xffu; }
+SFCI_HD unsigned key_digit(const K128& k, int shift) {
+  return shift < 64 ? (unsigned)(k.lo >> shift) & 0xffu : (unsigned)(k.hi >> (shift - 64)) & 0xffu;
+}
+
+// ---- bit helpers ----------------------------------------------------------
+
+// bits strictly below b of a 64-bit word, b in [0, 64]
+SFCI_HD u64 mask_below(int b) { return b >= 64 ? ~0ull : ((1ull << b) - 1ull); }
+
+SFCI_HD int popc64(u64 x) {
+#ifdef __CUDA_ARCH__
+  return __popcll(x);
+#else
+  return __builtin_popcountll(x);
+#endif
+}
+
+// Parity of the occupied spin orbitals strictly between p and q (either order):
+// the fermionic phase of moving one electron between p and q, as
+// signCal_bit computes it (src/bitstr.cpp:133-160).
+SFCI_HD int between_parity(const u64& d, int p, int q) {
+  int lo = p < q ? p : q, hi = p < q ? q : p;
+  u64 m = mask_below(hi) & ~mask_below(lo + 1);
+  return popc64(d & m) & 1;
+}
+SFCI_HD void between_mask(int p, int q, u64& m0, u64& m1) {
+  int lo = p < q ? p : q, hi = p < q ? q : p;
+  int a = lo + 1;
+  m0 = mask_below(hi < 64 ? hi : 64) & ~mask_below(a < 64 ? a : 64);
+  int h1 = hi - 64, a1 = a - 64;
+  m1 = mask_below(h1 > 0 ? h1 : 0) & ~mask_below(a1 > 0 ? a1 : 0);
+}
+SFCI_HD int between_parity(const K128& d, int p, int q) {
+  u64 m0, m1;
+  between_mask(p, q, m0, m1);
+  return (popc64(d.lo & m0) + popc64(d.hi & m1)) & 1;
+}
+// parity of popc(d & (btw(p,q) ^ btw(r,s))) in one go
+SFCI_HD int between_parity2(const u64& d, int p, int q, int r, int s) {
+  int lo = p < q ? p : q, hi = p < q ? q : p;
+  int lo2 = r < s ? r : s, hi2 = r < s ? s : r;
+  u64 m = (mask_below(hi) & ~mask_below(lo + 1)) ^ (mask_below(hi2) & ~mask_below(lo2 + 1));
+  return popc64(d & m) & 1;
+}
+SFCI_HD int between_parity2(const K128& d, int p, int q, int r, int s) {
+  u64 a0, a1, b0, b1;
+  between_mask(p, q, a0, a1);
+  between_mask(r, s, b0, b1);
+  return (popc64(d.lo & (a0 ^ b0)) + popc64(d.hi & (a1 ^ b1))) & 1;
+}
+SFCI_HD bool strictly_between(int x, int p, int q) {
+  int lo = p < q ? p : q, hi = p < q ? q : p;
+  return x > lo && x < hi;
+}
+
+// ---- hashing ---------------------------------------------------------------
+
+SFCI_HD u64 mix64(u64 z) {
+  z ^= z >> 30; z *= 0xbf58476d1ce4e5b9ull;
+  z ^= z >> 27; z *= 0x94d049bb133111ebull;
+  z ^= z >> 31;
+  return z;
+}
+SFCI_HD u64 key_hash(const u64& k) { return mix64(k + 0x9e3779b97f4a7c15ull); }
+SFCI_HD u64 key_hash(const K128& k) {
+  return mix64(k.lo + 0x9e3779b97f4a7c15ull) ^ mix64(k.hi ^ 0x632be59bd9b4e019ull) * 0x9e3779b97f4a7c15ull;
+}
+
+// order-preserving integer image of |x| (positive doubles compare as integers)
+SFCI_HD u64 abs_bits(double x) {
+#ifdef __CUDA_ARCH__
+  return (u64)__double_as_longlong(x) & 0x7fffffffffffffffull;
+#else
+  u64 u; __builtin_memcpy(&u, &x, 8); return u & 0x7fffffffffffffffull;
+#endif
+}
+
+SFCI_HD int spatial_pair(int i, int j) {  // packed (i,j) ~ (j,i) index, spatial
+  return i >= j ? i * (i + 1) / 2 + j : j * (j + 1) / 2 + i;
+}
+
+}  // namespace sfci

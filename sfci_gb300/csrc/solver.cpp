@@ -1,0 +1,333 @@
+// Krylov drivers on device-resident sparse vectors, and the FP64 generalised
+// symmetric eigensolver they use.
+//
+// sfci_lanczos_ground follows sparse_krylov_solve_eigenval
+// (src/sparse_solver.cpp:246-548) step for step; sfci_minres follows minres_sp
+// (src/minres.cpp:73-225), including its quirk of comparing the squared
+// residual with the unsquared tolerance (:211).  Every sparse-vector operation
+// runs on the GPU; only the Nl x Nl projected matrices and scalars live on the
+// host.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <limits>
+#include <memory>
+#include <vector>
+
+#include "internal.h"
+#include "spmspv.h"
+
+namespace sfci {
+
+// ---- K c = E S c ----------------------------------------------------------------
+// Cholesky S = L L^T, C = L^-1 K L^-T, cyclic Jacobi on C, x = L^-T y: the
+// eigenvectors come out S-orthonormal, as Eigen's GeneralizedSelfAdjointEigenSolver
+// returns them (Ax_lBx mode).  Column-major n x n arrays.
+static int gsaes_impl(int n, const double* K, const double* S, double* ev, double* X) {
+  std::vector<double> L((size_t)n * n, 0.0), C((size_t)n * n), V((size_t)n * n, 0.0);
+  auto at = [n](std::vector<double>& A, int i, int j) -> double& { return A[(size_t)j * n + i]; };
+  for (int j = 0; j < n; ++j) {
+    double d = S[(size_t)j * n + j];
+    for (int k = 0; k < j; ++k) d -= at(L, j, k) * at(L, j, k);
+    if (!(d > 0.0)) return set_error(SFCI_ERR_NUMERIC, "overlap matrix is not positive definite");
+    double ljj = std::sqrt(d);
+    at(L, j, j) = ljj;
+    for (int i = j + 1; i < n; ++i) {
+      double s = S[(size_t)j * n + i];
+      for (int k = 0; k < j; ++k) s -= at(L, i, k) * at(L, j, k);
+      at(L, i, j) = s / ljj;
+    }
+  }
+  // T = L^-1 K  (forward substitution per column), C = T L^-T = (L^-1 T^T)^T
+  std::vector<double> T((size_t)n * n);
+  for (int c = 0; c < n; ++c)
+    for (int i = 0; i < n; ++i) {
+      double s = K[(size_t)c * n + i];
+      for (int k = 0; k < i; ++k) s -= at(L, i, k) * T[(size_t)c * n + k];
+      T[(size_t)c * n + i] = s / at(L, i, i);
+    }
+  for (int r = 0; r < n; ++r)  // C(r, :) = L^-1 applied to row r of T
+    for (int i = 0; i < n; ++i) {
+      double s = T[(size_t)i * n + r];
+      for (int k = 0; k < i; ++k) s -= at(L, i, k) * at(C, r, k);
+      at(C, r, i) = s / at(L, i, i);
+    }
+  for (int i = 0; i < n; ++i)
+    for (int j = i + 1; j < n; ++j) {
+      double m = 0.5 * (at(C, i, j) + at(C, j, i));
+      at(C, i, j) = at(C, j, i) = m;
+    }
+  for (int i = 0; i < n; ++i) at(V, i, i) = 1.0;
+  for (int sweep = 0; sweep < 100; ++sweep) {
+    double off = 0.0;
+    for (int p = 0; p < n; ++p)
+      for (int q = p + 1; q < n; ++q) off += at(C, p, q) * at(C, p, q);
+    if (off < 1e-30) break;
+    for (int p = 0; p < n; ++p)
+      for (int q = p + 1; q < n; ++q) {
+        double apq = at(C, p, q);
+        if (std::fabs(apq) < 1e-300) continue;
+        double theta = (at(C, q, q) - at(C, p, p)) / (2.0 * apq);
+        double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+        double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+        for (int k = 0; k < n; ++k) {
+          double akp = at(C, k, p), akq = at(C, k, q);
+          at(C, k, p) = c * akp - s * akq;
+          at(C, k, q) = s * akp + c * akq;
+        }
+        for (int k = 0; k < n; ++k) {
+          double apk = at(C, p, k), aqk = at(C, q, k);
+          at(C, p, k) = c * apk - s * aqk;
+          at(C, q, k) = s * apk + c * aqk;
+        }
+        for (int k = 0; k < n; ++k) {
+          double vkp = at(V, k, p), vkq = at(V, k, q);
+          at(V, k, p) = c * vkp - s * vkq;
+          at(V, k, q) = s * vkp + c * vkq;
+        }
+      }
+  }
+  std::vector<int> ord(n);
+  for (int i = 0; i < n; ++i) ord[i] = i;
+  std::sort(ord.begin(), ord.end(), [&](int a, int b) { return at(C, a, a) < at(C, b, b); });
+  for (int k = 0; k < n; ++k) {
+    int src = ord[k];
+    ev[k] = at(C, src, src);
+    // x = L^-T y  (back substitution)
+    for (int i = n - 1; i >= 0; --i) {
+      double s = at(V, i, src);
+      for (int r = i + 1; r < n; ++r) s -= at(L, r, i) * X[(size_t)k * n + r];
+      X[(size_t)k * n + i] = s / at(L, i, i);
+    }
+    // deterministic sign: largest-magnitude component positive
+    int im = 0;
+    for (int i = 1; i < n; ++i)
+      if (std::fabs(X[(size_t)k * n + i]) > std::fabs(X[(size_t)k * n + im])) im = i;
+    if (X[(size_t)k * n + im] < 0)
+      for (int i = 0; i < n; ++i) X[(size_t)k * n + i] = -X[(size_t)k * n + i];
+  }
+  return SFCI_OK;
+}
+
+// ---- RAII device vectors for the drivers -----------------------------------------
+struct DVec {
+  Ctx* c = nullptr;
+  Vec v;
+  int alloc(Ctx& ctx, uint64_t cap) {
+    c = &ctx;
+    v.ctx = &ctx;
+    v.cap = cap;
+    v.len = 0;
+    size_t n = cap ? cap : 1;
+    if (cudaMalloc(&v.keys, n * ctx.W * sizeof(u64)) != cudaSuccess ||
+        cudaMalloc(&v.amps, n * sizeof(double)) != cudaSuccess) {
+      cudaGetLastError();
+      return set_error(SFCI_ERR_NOMEM, "driver vector allocation failed");
+    }
+    return SFCI_OK;
+  }
+  ~DVec() {
+    if (v.keys) cudaFree(v.keys);
+    if (v.amps) cudaFree(v.amps);
+  }
+};
+
+#define TRY(x)              \
+  do {                      \
+    int s_ = (x);           \
+    if (s_) return s_;      \
+  } while (0)
+
+static double now_s() {
+  using namespace std::chrono;
+  return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+static int norm_of(Ctx& c, const Vec& v, double* n) { return norm_impl(c, v, n); }
+
+int lanczos_ground(Ctx& c, Vec& v, int Nl, int restarts, double* energies, double* final_e) {
+  const bool vb = c.opts.verbose != 0;
+  const uint64_t Nd = c.opts.Nd, cap = c.opts.hpsi_cap;
+  std::vector<std::unique_ptr<DVec>> KB(Nl);
+  for (int i = 0; i < Nl; ++i) {
+    KB[i].reset(new DVec);
+    TRY(KB[i]->alloc(c, Nd));
+  }
+  DVec u, temp, temp_u, v_next, vv;
+  TRY(u.alloc(c, cap));
+  TRY(temp.alloc(c, cap));
+  TRY(temp_u.alloc(c, cap));
+  TRY(v_next.alloc(c, Nd));
+  TRY(vv.alloc(c, (uint64_t)Nl * Nd));
+  std::vector<double> KM((size_t)Nl * Nl, 0.0), S((size_t)Nl * Nl, 0.0), ev(Nl), X((size_t)Nl * Nl);
+  auto km = [&](int i, int j) -> double& { return KM[(size_t)j * Nl + i]; };
+  auto sm = [&](int i, int j) -> double& { return S[(size_t)j * Nl + i]; };
+  const double deltaE = 1e-5;
+  double previousE = 0.0, nearestE = -1000000.0;
+  for (int r = 0; r < restarts; ++r) energies[r] = std::numeric_limits<double>::quiet_NaN();
+  for (int res = 0; res < restarts; ++res) {
+    if (vb) printf("\n*****************block %d starts*****************\n", res);
+    TRY(op_copy(c, KB[0]->v, v));
+    double alpha = 0.0;
+    TRY(op_spmspv(c, v, u.v, 0.0, 1.0, &alpha));
+    if (vb) printf("H * phi_0 len:%llu\n", (unsigned long long)u.v.len);
+    km(0, 0) = alpha;
+    double beta = 0.0;
+    for (int i = 1; i < Nl; ++i) {
+      double t_it = now_s();
+      TRY(op_copy(c, temp.v, u.v));
+      TRY(op_add_two(c, temp.v, v, -alpha));
+      TRY(op_shrink(c, v_next.v, temp.v));
+      double gamma = 0.0;
+      TRY(norm_of(c, v_next.v, &gamma));
+      beta = gamma;
+      TRY(scale_impl(c, v_next.v, 1.0 / gamma));
+      double t_sp = now_s();
+      TRY(op_spmspv(c, v_next.v, temp_u.v, 0.0, 1.0, &alpha));
+      cudaStreamSynchronize(c.stream);
+      if (vb) printf("Single spmspvm time:%.6f\n", now_s() - t_sp);
+      km(i, i) = alpha;
+      for (int j = 0; j < i; ++j) {
+        double d = 0.0;
+        TRY(op_dot(c, KB[j]->v, temp_u.v, &d));
+        km(j, i) = d;
+        km(i, j) = d;
+      }
+      TRY(op_add_two(c, temp_u.v, v, -beta));
+      TRY(op_copy(c, u.v, temp_u.v));
+      TRY(op_copy(c, v, v_next.v));
+      TRY(op_copy(c, KB[i]->v, v));
+      temp.v.len = 0;
+      temp_u.v.len = 0;
+      if (vb) printf("time of current iter:%.6f\n", now_s() - t_it);
+    }
+    for (int i = 0; i < Nl; ++i)
+      for (int j = i; j < Nl; ++j) {
+        double d = 0.0;
+        TRY(op_dot(c, KB[i]->v, KB[j]->v, &d));
+        sm(i, j) = d;
+        sm(j, i) = d;
+      }
+    TRY(gsaes_impl(Nl, KM.data(), S.data(), ev.data(), X.data()));
+    int idx = 0;
+    double gap = std::fabs(nearestE - ev[0]);
+    for (int i = 1; i < Nl; ++i)
+      if (std::fabs(nearestE - ev[i]) < gap) {
+        gap = std::fabs(nearestE - ev[i]);
+        idx = i;
+      }
+    nearestE = ev[idx];
+    std::vector<const Vec*> ptr(Nl);
+    for (int i = 0; i < Nl; ++i) ptr[i] = &KB[i]->v;
+    TRY(op_combine(c, vv.v, ptr.data(), X.data() + (size_t)idx * Nl, Nl));
+    TRY(op_shrink(c, v, vv.v));
+    double nv = 0.0;
+    TRY(norm_of(c, v, &nv));
+    TRY(scale_impl(c, v, 1.0 / nv));
+    if (vb) {
+      double et = 0.0;
+      TRY(op_energy(c, v, &et));
+      printf("energy Psi_res after truncation:%.12f\n", et);
+    }
+    std::fill(KM.begin(), KM.end(), 0.0);
+    for (int i = 0; i < Nl; ++i) KB[i]->v.len = 0;
+    energies[res] = ev[idx];
+    if (vb) printf("gsaes energy:%.12f\n*****************block %d ends*****************\n", ev[idx], res);
+    if (previousE - ev[idx] < deltaE) break;
+    previousE = ev[idx];
+  }
+  double fe = 0.0;
+  TRY(op_energy(c, v, &fe));
+  if (vb) printf("final e:%.12f\n", fe);
+  *final_e = fe;
+  return SFCI_OK;
+}
+
+int minres(Ctx& c, const Vec& rhs, const Vec& guess, Vec& result, int iters, double tol, double lambda,
+           int* iters_done) {
+  const uint64_t N = c.opts.Nd;
+  double rhsn = 0.0;
+  TRY(norm_of(c, rhs, &rhsn));
+  DVec x, v_old, v, v_new, w, w_new, p_oold, p_old, p;
+  for (DVec* d : {&x, &v_old, &v, &v_new, &w, &w_new, &p_oold, &p_old, &p}) TRY(d->alloc(c, N));
+  TRY(op_copy(c, x.v, guess));
+  double diag = 0.0;
+  TRY(op_spmspv(c, x.v, v_new.v, lambda, -1.0, &diag));
+  TRY(op_add_two(c, v_new.v, rhs, 1.0));
+  double nr = 0.0;
+  TRY(norm_of(c, v_new.v, &nr));
+  double residualNorm2 = nr * nr;
+  TRY(op_copy(c, w_new.v, v_new.v));
+  double beta_new2 = 0.0;
+  TRY(op_dot(c, v_new.v, w_new.v, &beta_new2));
+  double beta_new = std::sqrt(beta_new2), beta_one = beta_new;
+  TRY(scale_impl(c, v_new.v, 1.0 / beta_new));
+  TRY(scale_impl(c, w_new.v, 1.0 / beta_new));
+  double cs = 1.0, c_old = 1.0, s = 0.0, s_old = 0.0, eta = 1.0;
+  p_old.v.len = 0;
+  p.v.len = 0;
+  int it = 0, done = 0;
+  while (it < iters) {
+    double beta = beta_new;
+    TRY(op_copy(c, v_old.v, v.v));
+    TRY(op_copy(c, v.v, v_new.v));
+    TRY(op_copy(c, w.v, w_new.v));
+    TRY(op_spmspv(c, w.v, v_new.v, lambda, 1.0, &diag));
+    TRY(op_add_two(c, v_new.v, v_old.v, -beta));
+    double alpha = 0.0;
+    TRY(op_dot(c, v_new.v, w.v, &alpha));
+    TRY(op_add_two(c, v_new.v, v.v, -alpha));
+    TRY(op_copy(c, w_new.v, v_new.v));
+    TRY(op_dot(c, v_new.v, w_new.v, &beta_new2));
+    beta_new = std::sqrt(beta_new2);
+    TRY(scale_impl(c, v_new.v, 1.0 / beta_new));
+    TRY(scale_impl(c, w_new.v, 1.0 / beta_new));
+    const double r2 = s * alpha + cs * c_old * beta;
+    const double r3 = s_old * beta;
+    const double r1_hat = cs * alpha - c_old * s * beta;
+    const double r1 = std::sqrt(r1_hat * r1_hat + beta_new * beta_new);
+    c_old = cs;
+    s_old = s;
+    cs = r1_hat / r1;
+    s = beta_new / r1;
+    TRY(op_copy(c, p_oold.v, p_old.v));
+    TRY(op_copy(c, p_old.v, p.v));
+    TRY(op_add_three(c, p.v, w.v, p_old.v, p_oold.v, 1.0 / r1, -r2 / r1, -r3 / r1));
+    TRY(op_add_two(c, x.v, p.v, beta_one * cs * eta));
+    residualNorm2 *= s * s;
+    ++done;
+    if (c.opts.verbose) printf("res norm:%.12g\n%d is done\n", residualNorm2, it);
+    if (residualNorm2 < tol) break;
+    eta = -s * eta;
+    ++it;
+  }
+  if (iters_done) *iters_done = done;
+  return op_copy(c, result, x.v);
+}
+
+}  // namespace sfci
+
+using namespace sfci;
+
+extern "C" {
+
+int sfci_gsaes(int n, const double* K, const double* S, double* evals, double* evecs) {
+  if (n <= 0 || !K || !S || !evals || !evecs) return set_error(SFCI_ERR_ARG, "bad gsaes arguments");
+  return gsaes_impl(n, K, S, evals, evecs);
+}
+
+int sfci_lanczos_ground(sfci_ctx* x, sfci_vec* v, int Nl, int restarts, double* energies, double* final_e) {
+  if (!x || !v || !energies || !final_e || Nl < 1 || restarts < 1)
+    return set_error(SFCI_ERR_ARG, "bad lanczos arguments");
+  if (v->v.len == 0) return set_error(SFCI_ERR_ARG, "lanczos start vector is empty");
+  return lanczos_ground(x->c, v->v, Nl, restarts, energies, final_e);
+}
+
+int sfci_minres(sfci_ctx* x, const sfci_vec* rhs, const sfci_vec* guess, sfci_vec* result, int iters, double tol,
+                double lambda, int* iters_done) {
+  if (!x || !rhs || !guess || !result || iters < 0) return set_error(SFCI_ERR_ARG, "bad minres arguments");
+  return minres(x->c, rhs->v, guess->v, result->v, iters, tol, lambda, iters_done);
+}
+
+}  // extern "C"

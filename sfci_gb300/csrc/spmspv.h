@@ -1,0 +1,33 @@
+// Entry points of the device hot path, one instantiation per key width W.
+#pragma once
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace sfci {
+
+template <int W> int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, double* diag);
+template <int W> int energy_impl(Ctx& c, const Vec& psi, double* E);
+template <int W> int diag_elements_impl(Ctx& c, const typename KeyOf<W>::T* dkeys, u64 n, double* out_host);
+
+template <int W> int dot_impl(Ctx& c, const Vec& x, const Vec& y, double* out);
+template <int W> int add_two_impl(Ctx& c, Vec& v, const Vec& w, double a);
+template <int W> int add_three_impl(Ctx& c, Vec& v, const Vec& x, const Vec& y, const Vec& z, double a, double b,
+                                    double cc);
+template <int W> int shrink_impl(Ctx& c, Vec& dst, const Vec& src);
+template <int W> int combine_impl(Ctx& c, Vec& dst, const Vec* const* vs, const double* coef, int n);
+template <int W> int sort_vec_impl(Ctx& c, Vec& v);
+int scale_impl(Ctx& c, Vec& v, double a);
+int norm_impl(Ctx& c, const Vec& v, double* out);
+
+// width dispatch used by the ABI and the drivers
+int op_spmspv(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, double* diag);
+int op_energy(Ctx& c, const Vec& psi, double* E);
+int op_dot(Ctx& c, const Vec& x, const Vec& y, double* out);
+int op_add_two(Ctx& c, Vec& v, const Vec& w, double a);
+int op_add_three(Ctx& c, Vec& v, const Vec& x, const Vec& y, const Vec& z, double a, double b, double cc);
+int op_shrink(Ctx& c, Vec& dst, const Vec& src);
+int op_combine(Ctx& c, Vec& dst, const Vec* const* vs, const double* coef, int n);
+int op_copy(Ctx& c, Vec& dst, const Vec& src);
+
+}  // namespace sfci

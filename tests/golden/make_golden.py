@@ -1,0 +1,223 @@
+"""Generate the golden fixtures of tests/golden from the reference itself.
+
+Run in a checkout that has the reference tree (the x86 development container):
+
+    python tests/golden/make_golden.py [REF_ROOT]
+
+It (1) runs the reference converter ``util/convert_fcidump.py`` on small
+synthetic FCIDUMPs and stores the resulting ``_IN`` files, and (2) builds the
+reference SpMSpV sources into ``oracle/_ref/libsfci_ref.so`` and records, for a
+few synthetic systems, the outputs of DiagCal_bit, OffDiagGen_bit_e,
+SpMVMtply_bucket, calc_energy, dynVec::dot/addTwo/addThree/shrinkFrom and a
+restated Lanczos driver over those primitives.  The fixtures pin both the
+oracle restatement (oracle/sfci_port.cpp) and the GPU path; neither needs the
+reference tree afterwards.
+"""
+from __future__ import annotations
+
+import hashlib
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from sfci_gb300 import fcidump as fd  # noqa: E402
+from oracle import oracle as orc  # noqa: E402
+
+BUNIT = 1000000
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SFCI_REFERENCE_ROOT", "/root/reference")
+
+# name, kind, M, ne, seeds, Nd for the Lanczos case (0 = no Lanczos)
+SYSTEMS = [
+    ("c1", "rhf", 10, 10, (0,), 20000, 20, 3),        # configs[0] of the benchmark definition
+    ("u8", "uhf", 8, 6, (2, 3), 4000, 12, 3),         # small UHF, FCI dim 3136 < Nd
+    ("r16", "rhf", 16, 8, (1,), 3000, 10, 2),         # wider virtual space
+    ("r28", "rhf", 28, 14, (1,), 0, 0, 0),            # configs[1] shape (SpMSpV level only)
+]
+
+
+def ref_convert(fcidump_path: str, flag: str) -> str:
+    d = tempfile.mkdtemp()
+    try:
+        name = os.path.basename(fcidump_path)
+        shutil.copy(fcidump_path, os.path.join(d, name))
+        subprocess.run([sys.executable, os.path.join(REF, "util", "convert_fcidump.py"), flag, name], cwd=d,
+                       check=True, capture_output=True)
+        return open(os.path.join(d, name.split("_")[0] + "_IN")).read()
+    finally:
+        shutil.rmtree(d)
+
+
+def merged(keys, amps):
+    u, inv = np.unique(keys, return_inverse=True)
+    s = np.zeros(u.size)
+    np.add.at(s, inv, amps)
+    return u, s
+
+
+def sample_dets(hf: int, N: int, ne: int, rng, n: int):
+    """HF plus random Sz-preserving excitations of it (ranks 1..4)."""
+    occ = [b for b in range(N) if hf >> b & 1]
+    vir = [b for b in range(N) if not hf >> b & 1]
+    out = {hf}
+    while len(out) < n:
+        k = int(rng.integers(1, 5))
+        d = hf
+        for _ in range(k):
+            i = int(rng.choice(occ))
+            cand = [a for a in vir if (a & 1) == (i & 1) and not d >> a & 1]
+            if not (d >> i & 1) or not cand:
+                continue
+            a = int(rng.choice(cand))
+            d = d ^ (1 << i) ^ (1 << a)
+        out.add(d)
+    return np.array(sorted(out), dtype=np.uint64)
+
+
+def main():
+    so = orc.build_ref(REF)
+    if not so:
+        raise SystemExit("reference sources not available under %s" % REF)
+    ref = orc.RefLib(so)
+    # (1) converter fixtures: small RHF and UHF files
+    for kind, M in (("rhf", 4), ("uhf", 4), ("rhf", 6)):
+        tmp = tempfile.mkdtemp()
+        try:
+            p = os.path.join(tmp, "sys_fcidump")
+            if kind == "rhf":
+                h, q, v, e = fd.synthetic_rhf(M, 7)
+                fd.write_fcidump_rhf(p, h, q, v, e, 4)
+                txt = ref_convert(p, "-r")
+            else:
+                hs, aa, bb, ab, e = fd.synthetic_uhf(M, 8, 9)
+                fd.write_fcidump_uhf(p, hs, aa, bb, ab, e, 4)
+                txt = ref_convert(p, "-u")
+            with open(os.path.join(HERE, "conv_%s_m%d_IN" % (kind, M)), "w") as f:
+                f.write(txt)
+        finally:
+            shutil.rmtree(tmp)
+    # (2) hot-path fixtures
+    for name, kind, M, ne, seeds, lnd, nl, nres in SYSTEMS:
+        N = 2 * M
+        tmp = tempfile.mkdtemp()
+        try:
+            fpath = os.path.join(tmp, "sys_fcidump")
+            if kind == "rhf":
+                h, q, v, e = fd.synthetic_rhf(M, seeds[0])
+                fd.write_fcidump_rhf(fpath, h, q, v, e, ne)
+                txt = ref_convert(fpath, "-r")
+            else:
+                hs, aa, bb, ab, e = fd.synthetic_uhf(M, seeds[0], seeds[1])
+                fd.write_fcidump_uhf(fpath, hs, aa, bb, ab, e, ne)
+                txt = ref_convert(fpath, "-u")
+            inp = os.path.join(tmp, "sys_IN")
+            open(inp, "w").write(txt)
+            Nd_big = 200000
+            ref.setup(inp, N, ne, Nd_big, bucket_unit=BUNIT, nthread=os.cpu_count(), num_connected=2000000)
+            rng = np.random.default_rng(100 + M)
+            hf = (1 << ne) - 1
+            out = {"M": M, "ne": ne, "kind": kind, "seeds": np.array(seeds), "hf": np.uint64(hf),
+                   "in_sha256": hashlib.sha256(txt.encode()).hexdigest()}
+            dets = sample_dets(hf, N, ne, rng, 40)
+            out["diag_dets"] = dets
+            out["diag_vals"] = ref.diag(dets)
+            for t, d in enumerate(dets[:3]):
+                k, a = ref.offdiag(d)
+                u, s = merged(k, a)
+                out["off%d_det" % t] = np.uint64(d)
+                out["off%d_keys" % t] = u
+                out["off%d_amps" % t] = s
+            # SpMSpV cases
+            cap_big = 2000000
+            k0 = np.array([hf], np.uint64)
+            a0 = np.array([1.0])
+            if N <= 40:
+                kA, aA, dA = ref.spmspv(k0, a0, cap_big, 0.0, 1.0)
+            else:
+                # a 1-det input on this size overflows the reference's len*5000 buffer
+                # (src/functions.cpp:566); start from a 2000-det vector instead
+                kA, aA = None, None
+            if kA is not None:
+                out.update(A_in_keys=k0, A_in_amps=a0, A_keys=kA, A_amps=aA, A_diag=dA)
+                order = np.argsort(-np.abs(aA), kind="stable")[: min(400, aA.size)]
+                v1k = kA[np.sort(order)]
+                v1a = aA[np.sort(order)]
+            else:
+                v1k = sample_dets(hf, N, ne, rng, 2000)
+                v1a = rng.normal(size=v1k.size) * np.exp(-rng.uniform(0, 8, size=v1k.size))
+            v1a = v1a / np.linalg.norm(v1a)
+            out_cap_B = cap_big if N <= 40 else 20000
+            kB, aB, dB = ref.spmspv(v1k, v1a, out_cap_B, 0.0, 1.0)
+            out.update(B_in_keys=v1k, B_in_amps=v1a, B_keys=kB, B_amps=aB, B_diag=dB, B_cap=out_cap_B)
+            # Nd smaller than the input + shift + negative coefficient + small output cap
+            nd_c = max(2, v1k.size // 3)
+            ref.setup(inp, N, ne, nd_c, bucket_unit=BUNIT, nthread=os.cpu_count(), num_connected=2000000)
+            eh = float(ref.diag(np.array([hf], np.uint64))[0])
+            cap_c = 5000
+            kC, aC, dC = ref.spmspv(v1k, v1a, cap_c, eh, -1.0)
+            out.update(C_Nd=nd_c, C_cap=cap_c, C_lambda=eh, C_coeff=-1.0, C_keys=kC, C_amps=aC, C_diag=dC)
+            ref.setup(inp, N, ne, Nd_big, bucket_unit=BUNIT, nthread=os.cpu_count(), num_connected=2000000)
+            # energies and vector algebra (vectors sorted by key, as dynVec keeps them)
+            out["E_v1"] = ref.energy(v1k, v1a)
+            bsel = np.argsort(-np.abs(aB), kind="stable")[: min(3000, aB.size)]
+            wk, wa = kB[np.sort(bsel)], aB[np.sort(bsel)]
+            wa = wa / np.linalg.norm(wa)
+            out.update(w_keys=wk, w_amps=wa)
+            out["E_w"] = ref.energy(wk, wa)
+            out["dot_v1_B"] = ref.dot(v1k, v1a, kB, aB)
+            out["dot_w_B"] = ref.dot(wk, wa, kB, aB)
+            out["norm_B"] = ref.norm(kB, aB)
+            for cap in (10 ** 7, 1000):
+                k2, a2 = ref.add_two(kB, aB, cap, v1k, v1a, -0.37)
+                out["add2_%d_keys" % cap] = k2
+                out["add2_%d_amps" % cap] = a2
+            ref.setup(inp, N, ne, 2000, bucket_unit=BUNIT, nthread=os.cpu_count(), num_connected=2000000)
+            k3, a3 = ref.add_three(wk, wa, v1k, v1a, kB, aB, 0.5, -1.25, 0.75)
+            out.update(add3_keys=k3, add3_amps=a3, add3_Nd=2000)
+            ref.setup(inp, N, ne, Nd_big, bucket_unit=BUNIT, nthread=os.cpu_count(), num_connected=2000000)
+            ks, as_ = ref.shrink_from(kB, aB, 777)
+            out.update(shrink_keys=ks, shrink_amps=as_, shrink_cap=777)
+            # Lanczos through the reference primitives
+            if lnd:
+                ref.setup(inp, N, ne, lnd, bucket_unit=BUNIT, nthread=os.cpu_count(), num_connected=2000000)
+                en, fe, (vk, va) = orc.lanczos(ref, k0, a0, nl, nres, lnd, hpsi_cap=2000000)
+                out.update(L_hpsi_cap=2000000)
+                out.update(L_Nd=lnd, L_Nl=nl, L_restarts=nres, L_energies=en, L_final_e=fe)
+                if kind == "uhf" or M <= 8:
+                    out["fci_energy"] = exact_fci(ref, N, ne, hf)
+            np.savez_compressed(os.path.join(HERE, "%s.npz" % name), **out)
+            print(name, {k: (v.shape if hasattr(v, "shape") else v) for k, v in out.items() if "keys" not in k})
+        finally:
+            shutil.rmtree(tmp)
+
+
+def exact_fci(ref, N, ne, hf):
+    """Dense FCI over the Sz-sector of hf, from the reference's own elements."""
+    import itertools
+    import scipy.linalg as sl
+    M = N // 2
+    na = bin(hf & 0x5555555555555555).count("1")
+    nb = bin(hf & 0xAAAAAAAAAAAAAAAA).count("1")
+    alphas = [sum(1 << (2 * o) for o in c) for c in itertools.combinations(range(M), na)]
+    betas = [sum(1 << (2 * o + 1) for o in c) for c in itertools.combinations(range(M), nb)]
+    dets = np.array(sorted(a | b for a in alphas for b in betas), dtype=np.uint64)
+    index = {int(d): i for i, d in enumerate(dets)}
+    H = np.zeros((dets.size, dets.size))
+    diag = ref.diag(dets)
+    for j, d in enumerate(dets):
+        H[j, j] += diag[j]
+        k, a = ref.offdiag(d)
+        for kk, aa in zip(k, a):
+            H[index[int(kk)], j] += aa
+    return float(sl.eigh(H, eigvals_only=True)[0])
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,104 @@
+// Test-only harness: the device excitation decoder (sfci_gb300/csrc/gen.cuh),
+// compiled for the host so that its enumeration, phases and matrix elements can
+// be checked on a CPU-only machine against the reference's emitted terms.
+// Built by tests/test_gen_host.py; not part of the library.
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "gen.cuh"
+#include "internal.h"
+
+using namespace sfci;
+
+static HamHost g_h;
+
+template <class KT>
+static void setup_host(DetInfo<KT>& d, const KT& key, int M, double cc, double D) {
+  d.key = key;
+  d.cc = cc;
+  d.dterm = D * cc;
+  for (int s = 0; s < 2; ++s) {
+    unsigned no = 0, nv = 0;
+    for (int o = 0; o < M; ++o) {
+      int b = 2 * o + s;
+      if (key_test(key, b)) d.occ[s][no++] = (unsigned char)b;
+      else d.vir[s][nv++] = (unsigned char)b;
+    }
+    d.na[s] = no;
+    d.nv[s] = nv;
+    d.nvp[s] = c2(nv);
+    d.inv_nv[s] = nv ? 1.0f / (float)nv : 0.f;
+    d.inv_nvp[s] = d.nvp[s] ? 1.0f / (float)d.nvp[s] : 0.f;
+  }
+  d.nsb = d.na[1] * d.nv[1];
+  d.inv_nsb = d.nsb ? 1.0f / (float)d.nsb : 0.f;
+  d.c[0] = 1;
+  d.c[1] = d.c[0] + d.na[0] * d.nv[0];
+  d.c[2] = d.c[1] + d.na[1] * d.nv[1];
+  d.c[3] = d.c[2] + c2(d.na[0]) * d.nvp[0];
+  d.c[4] = d.c[3] + c2(d.na[1]) * d.nvp[1];
+  d.c[5] = d.c[4] + d.na[0] * d.nv[0] * d.nsb;
+}
+
+static void pair_table(unsigned short* pt) {
+  for (int y = 1; y < 64; ++y)
+    for (int x = 0; x < y; ++x) pt[y * (y - 1) / 2 + x] = (unsigned short)(x | (y << 8));
+}
+
+template <class KT>
+static double diag_host(const KT& key, const HamView& h) {
+  std::vector<int> occ;
+  for (int b = 0; b < h.N; ++b)
+    if (key_test(key, b)) occ.push_back(b);
+  double s = 0;
+  for (size_t x = 0; x < occ.size(); ++x)
+    for (size_t y = x + 1; y < occ.size(); ++y) {
+      int i = occ[x], j = occ[y], si = i & 1, sj = j & 1;
+      double J = 0.5 * (vget(h, 2 * si + sj, i, i, j, j) + vget(h, 2 * sj + si, j, j, i, i));
+      double K = si == sj ? vget(h, 3 * si, i, j, j, i) : 0.0;
+      s += J - K;
+    }
+  for (int i : occ) s += h.h1[((size_t)(i & 1) * h.M + (i >> 1)) * h.M + (i >> 1)];
+  return s + h.ecore;
+}
+
+extern "C" int gh_load(const char* path, int N) {
+  std::string err;
+  return load_in_file(path, N, g_h, err);
+}
+
+// All terms of one determinant with unit amplitude: returns the count, writes
+// up to cap (key words, element) pairs; term 0 is the diagonal.
+extern "C" long gh_terms(const uint64_t* kw, uint64_t* out_k, double* out_a, long cap) {
+  HamView h{g_h.N, g_h.M, g_h.P, g_h.h1.data(), g_h.V.data(), g_h.ecore};
+  static unsigned short pt[2016];
+  pair_table(pt);
+  long n = 0;
+  if (g_h.N <= 64) {
+    DetInfo<u64> d;
+    u64 key = kw[0];
+    setup_host(d, key, g_h.M, 1.0, diag_host(key, h));
+    for (unsigned l = 0; l < d.c[5]; ++l, ++n) {
+      Exc e = decode(d, pt, l);
+      if (n < cap) {
+        out_k[n] = target_key(d, e);
+        out_a[n] = term_amp(d, e, h);
+      }
+    }
+  } else {
+    DetInfo<K128> d;
+    K128 key{kw[0], kw[1]};
+    setup_host(d, key, g_h.M, 1.0, diag_host(key, h));
+    for (unsigned l = 0; l < d.c[5]; ++l, ++n) {
+      Exc e = decode(d, pt, l);
+      if (n < cap) {
+        K128 t = target_key(d, e);
+        out_k[2 * n] = t.lo;
+        out_k[2 * n + 1] = t.hi;
+        out_a[n] = term_amp(d, e, h);
+      }
+    }
+  }
+  return n;
+}

@@ -1,0 +1,93 @@
+"""The C-ABI library: builds, loads, exports every declared entry point, and
+rejects bad input before touching the GPU.  No device compute here."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+import sfci_gb300 as sg
+
+
+def declared_symbols():
+    names = []
+    inc = os.path.join(ROOT, "include")
+    for f in sorted(os.listdir(inc)):
+        if f.endswith(".h"):
+            txt = open(os.path.join(inc, f)).read()
+            names += re.findall(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b(sfci_\w+)\s*\(", txt, flags=re.M)
+    return sorted(set(names))
+
+
+def test_library_exports_every_declared_symbol():
+    L = sg.load_library()
+    names = declared_symbols()
+    assert len(names) >= 30
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_gsaes_matches_scipy():
+    import scipy.linalg as sl
+    rng = np.random.default_rng(3)
+    for n in (1, 3, 20, 40):
+        A = rng.normal(size=(n, n))
+        K = A + A.T
+        B = rng.normal(size=(n, n))
+        S = B @ B.T + n * np.eye(n)
+        ev, X = sg.gsaes(K, S)
+        ref = sl.eigh(K, S, eigvals_only=True)
+        assert np.max(np.abs(ev - ref)) < 1e-11 * max(1.0, np.max(np.abs(ref)))
+        assert np.max(np.abs(X.T @ S @ X - np.eye(n))) < 1e-10
+        assert np.max(np.abs(K @ X - (S @ X) * ev)) < 1e-9
+
+
+def test_gsaes_rejects_indefinite_overlap():
+    with pytest.raises(sg.SfciError) as e:
+        sg.gsaes(np.eye(2), np.array([[1.0, 2.0], [2.0, 1.0]]))
+    assert e.value.status == "SFCI_ERR_NUMERIC"
+
+
+def _create(path, norb, ne):
+    L = sg.load_library()
+    h = C.c_void_p()
+    st = L.sfci_ctx_create(path.encode(), norb, ne, None, C.byref(h))
+    return st, L
+
+
+def test_missing_file_is_io_error(tmp_path):
+    st, L = _create(str(tmp_path / "nope_IN"), 20, 10)
+    assert L.sfci_status_name(st).decode() == "SFCI_ERR_IO"
+
+
+def test_bad_sizes_rejected(tmp_path):
+    p = tmp_path / "x_IN"
+    p.write_text("0\n0\n0\n0\n0\n0\n0\n")
+    for norb, ne in ((130, 4), (7, 2), (8, 8), (8, -1)):
+        st, L = _create(str(p), norb, ne)
+        assert L.sfci_status_name(st).decode() == "SFCI_ERR_ARG", (norb, ne)
+
+
+def test_asymmetric_integrals_rejected(tmp_path):
+    # (mn|pq) and (nm|pq) share a table slot; different values must be refused
+    p = tmp_path / "asym_IN"
+    p.write_text("2\n1.0 2 4 2 4\n2.0 4 2 2 4\n0\n0\n0\n0\n0\n0\n")
+    st, L = _create(str(p), 4, 2)
+    assert L.sfci_status_name(st).decode() == "SFCI_ERR_UNSUPPORTED"
+    assert b"contradicts" in L.sfci_last_error()
+
+
+def test_repeated_entry_rejected(tmp_path):
+    p = tmp_path / "rep_IN"
+    p.write_text("2\n1.0 2 4 3 5\n1.0 2 4 3 5\n0\n0\n0\n0\n0\n0\n")
+    st, L = _create(str(p), 4, 2)
+    assert L.sfci_status_name(st).decode() == "SFCI_ERR_UNSUPPORTED"
+
+
+def test_keys_roundtrip_helpers():
+    ints = [0, 1, (1 << 64) + 5, (1 << 127) | 3]
+    k = sg.keys_from_ints(ints, 2)
+    assert sg.ints_from_keys(k) == ints

@@ -254,12 +254,15 @@ constexpr int CP_THREADS = 256;
 constexpr int CP_CHUNKS = 16;
 constexpr int CP_TILE = CP_THREADS * CP_CHUNKS;
 
-// mode 0: keep |a| > cut  (cut passed as bits via tau, need_eq unused)
-// mode 1: keep |a| > tau or (|a| == tau and eq-rank < need_eq), then |a| > tiny if tiny >= 0
+// mode 0: keep |a| > cut
+// mode 1: keep |a| > tau or (|a| == tau and eq-rank >= eq_skip), then |a| > tiny if tiny >= 0.
+// Ties at the threshold are kept from the end of the index order (the largest keys
+// of a key-sorted vector), as a stable ascending sort by |a| followed by "keep the
+// last k" does.
 struct KeepRule {
   int mode;
   u64 tau;
-  u64 need_eq;
+  u64 eq_skip;
   double cut;
   double tiny;
 };
@@ -271,7 +274,7 @@ __device__ __forceinline__ bool keep_of(const KeepRule& r, double a, u64 eq_rank
     return fabs(a) > r.cut;
   }
   is_eq = (b == r.tau);
-  bool k = b > r.tau || (is_eq && eq_rank < r.need_eq);
+  bool k = b > r.tau || (is_eq && eq_rank >= r.eq_skip);
   if (k && r.tiny >= 0.0) k = fabs(a) > r.tiny;
   return k;
 }
@@ -386,6 +389,10 @@ static int compact_rule(Ctx& c, const typename KeyOf<W>::T* ik, const double* ia
   if (rule.mode == 1) {
     SFCI_LAUNCH(c, k_cp_eqcount, (unsigned)nt, CP_THREADS, 0, ia, n, rule.tau, eqo);
     if ((st = scan_excl(c, eqo, eqo, nt))) return st;
+    // eq_skip arrives as the number of ties to keep; turn it into ties to skip
+    u64 tot_eq = 0;
+    if ((st = read_words(c, eqo + nt, sizeof(u64), &tot_eq))) return st;
+    rule.eq_skip = rule.eq_skip >= tot_eq ? 0 : tot_eq - rule.eq_skip;
   }
   SFCI_LAUNCH(c, (k_cp_pass<KT, false>), (unsigned)nt, CP_THREADS, 0, ik, ia, n, rule, (const u64*)eqo, kpo,
               (const u64*)nullptr, (KT*)nullptr, (double*)nullptr);
@@ -419,9 +426,8 @@ int top_k_stable(Ctx& c, typename KeyOf<W>::T* ik, double* ia, size_t n, size_t 
   if (n <= k) {
     if (tiny >= 0.0) {
       // filter only: keep |a| > tiny (all of them pass the selection)
-      KeepRule r{1, 0ull, 0ull, 0.0, tiny};
-      // tau = 0 with need_eq = n keeps everything before the tiny filter
-      r.need_eq = n;
+      // tau = 0 keeping all n ties keeps everything before the tiny filter
+      KeepRule r{1, 0ull, (u64)n, 0.0, tiny};
       return compact_rule<W>(c, ik, ia, n, r, ok, oa, m);
     }
     if (ok != ik) {

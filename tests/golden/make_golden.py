@@ -157,7 +157,12 @@ def main():
             kB, aB, dB = ref.spmspv(v1k, v1a, out_cap_B, 0.0, 1.0)
             out.update(B_in_keys=v1k, B_in_amps=v1a, B_keys=kB, B_amps=aB, B_diag=dB, B_cap=out_cap_B)
             # Nd smaller than the input + shift + negative coefficient + small output cap
+            # an Nd whose boundary is not a magnitude tie (RHF spin-mirror determinants
+            # have equal |amp|, and the reference breaks ties arbitrarily)
+            mags = np.sort(np.abs(v1a))[::-1]
             nd_c = max(2, v1k.size // 3)
+            while nd_c < v1k.size - 1 and not mags[nd_c - 1] > mags[nd_c] * (1 + 1e-9):
+                nd_c += 1
             ref.setup(inp, N, ne, nd_c, bucket_unit=BUNIT, nthread=os.cpu_count(), num_connected=2000000)
             eh = float(ref.diag(np.array([hf], np.uint64))[0])
             cap_c = 5000

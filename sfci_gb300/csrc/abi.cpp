@@ -241,6 +241,15 @@ int sfci_ctx_destroy(sfci_ctx* x) {
   if (!x) return SFCI_OK;
   Ctx& c = x->c;
   if (c.stream) cudaStreamSynchronize(c.stream);
+  for (Vec* v : c.live) {  // orphan vectors that outlive their context
+    if (v->keys) cudaFree(v->keys);
+    if (v->amps) cudaFree(v->amps);
+    v->keys = nullptr;
+    v->amps = nullptr;
+    v->ctx = nullptr;
+    v->cap = v->len = 0;
+  }
+  c.live.clear();
   scratch_free_all(c);
   if (c.d_h1) cudaFree(c.d_h1);
   if (c.d_V) cudaFree(c.d_V);
@@ -334,6 +343,7 @@ int sfci_vec_create(sfci_ctx* x, uint64_t cap, sfci_vec** out) {
   sfci_vec* v = new sfci_vec();
   v->v.ctx = &x->c;
   v->v.cap = cap;
+  x->c.live.insert(&v->v);
   size_t n = cap ? cap : 1;
   cudaError_t e = cudaMalloc(&v->v.keys, n * x->c.W * sizeof(u64));
   if (e == cudaSuccess) e = cudaMalloc(&v->v.amps, n * sizeof(double));
@@ -348,7 +358,10 @@ int sfci_vec_create(sfci_ctx* x, uint64_t cap, sfci_vec** out) {
 
 int sfci_vec_destroy(sfci_vec* v) {
   if (!v) return SFCI_OK;
-  if (v->v.ctx && v->v.ctx->stream) cudaStreamSynchronize(v->v.ctx->stream);
+  if (v->v.ctx) {
+    if (v->v.ctx->stream) cudaStreamSynchronize(v->v.ctx->stream);
+    v->v.ctx->live.erase(&v->v);
+  }
   if (v->v.keys) cudaFree(v->v.keys);
   if (v->v.amps) cudaFree(v->v.amps);
   delete v;

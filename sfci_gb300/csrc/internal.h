@@ -4,6 +4,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <map>
+#include <set>
 #include <string>
 #include <vector>
 
@@ -55,6 +56,8 @@ struct Ctx {
   std::vector<cudaEvent_t> ev_pool;
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ph_pending;
   uint64_t stats[8] = {};
+  // vectors created on this context (freed with it; their handles become orphans)
+  std::set<struct Vec*> live;
   // pinned host staging for small readbacks
   u64* h_pin = nullptr;
   size_t h_pin_words = 0;

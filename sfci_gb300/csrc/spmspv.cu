@@ -401,6 +401,7 @@ struct LeafArgs {
   double* dpart;       // per-CTA <v|Hv> partials (accumulated across launches)
   unsigned* ovf;       // [0] = count, then leaf ids (global)
   unsigned ovf_cap;
+  u64* uniq;           // merged distinct determinants (statistics)
 };
 
 template <class KT>
@@ -417,7 +418,12 @@ __global__ void __launch_bounds__(LEAF_THREADS) k_leaf(LeafArgs<KT> a) {
   double dacc = 0.0;
   for (u64 leaf = blockIdx.x; leaf < a.nleaves; leaf += gridDim.x) {
     const u64 beg = a.loff[leaf * a.lstride] - a.lbase, end = a.loff[(leaf + 1) * a.lstride] - a.lbase;
-    for (int s = tid; s < TBL; s += LEAF_THREADS) {
+    // table sized to the leaf: >= 2x its terms (so it cannot fill), 512..TBL slots
+    const u64 n = end - beg;
+    unsigned tb = 512;
+    while (tb < TBL && (u64)tb < 2 * n) tb <<= 1;
+    const unsigned limit = tb == TBL ? LEAF_LIMIT : tb;
+    for (unsigned s = tid; s < tb; s += LEAF_THREADS) {
       tk[s] = empty;
       ta[s] = 0.0;
     }
@@ -428,7 +434,7 @@ __global__ void __launch_bounds__(LEAF_THREADS) k_leaf(LeafArgs<KT> a) {
     __syncthreads();
     for (u64 e = beg + tid; e < end; e += LEAF_THREADS) {
       if (*(volatile unsigned*)&s_ovf) break;
-      if (!table_add(tk, ta, TBL - 1, a.keys[e], a.amps[e], &s_nuniq, LEAF_LIMIT)) s_ovf = 1;
+      if (!table_add(tk, ta, tb - 1, a.keys[e], a.amps[e], &s_nuniq, limit)) s_ovf = 1;
     }
     __syncthreads();
     if (s_ovf) {
@@ -442,25 +448,26 @@ __global__ void __launch_bounds__(LEAF_THREADS) k_leaf(LeafArgs<KT> a) {
     // <v| (H - lambda) |v> share of this leaf
     const u64 gl = a.gleaf0 + leaf;
     for (u64 e = a.in_off[gl] + tid; e < a.in_off[gl + 1]; e += LEAF_THREADS) {
-      int s = table_find(tk, TBL - 1, a.in_keys[e]);
+      int s = table_find(tk, tb - 1, a.in_keys[e]);
       if (s >= 0) dacc += ta[s] * a.in_amps[e];
     }
-    // survivors |a| > cut: each thread owns TBL/THREADS consecutive slots
-    constexpr int PER = TBL / LEAF_THREADS;
+    // survivors |a| > cut: each thread owns tb/THREADS consecutive slots
+    const unsigned per = tb / LEAF_THREADS;
     unsigned c = 0;
-#pragma unroll
-    for (int q = 0; q < PER; ++q) {
-      int s = tid * PER + q;
+    for (unsigned q = 0; q < per; ++q) {
+      unsigned s = tid * per + q;
       if (!key_eq(tk[s], empty) && fabs(ta[s]) > a.cut) ++c;
     }
     u64 tot;
     u64 ex = block_excl_scan<u64, LEAF_THREADS>((u64)c, &tot, s_sum);
-    if (tid == 0) s_base = tot ? atomicAdd(a.scount, tot) : 0;
+    if (tid == 0) {
+      s_base = tot ? atomicAdd(a.scount, tot) : 0;
+      atomicAdd(a.uniq, (u64)s_nuniq);
+    }
     __syncthreads();
     u64 pos = s_base + ex;
-#pragma unroll
-    for (int q = 0; q < PER; ++q) {
-      int s = tid * PER + q;
+    for (unsigned q = 0; q < per; ++q) {
+      unsigned s = tid * per + q;
       if (!key_eq(tk[s], empty) && fabs(ta[s]) > a.cut) {
         a.skeys[pos] = tk[s];
         a.samps[pos] = ta[s];
@@ -489,7 +496,8 @@ __global__ void k_big_insert(const KT* __restrict__ keys, const double* __restri
 
 template <class KT>
 __global__ void k_big_finish(const KT* tk, const double* ta, unsigned mask, const KT* in_keys, const double* in_amps,
-                             u64 ib, u64 ie, double cut, KT* skeys, double* samps, u64* scount, double* dsum) {
+                             u64 ib, u64 ie, double cut, KT* skeys, double* samps, u64* scount, double* dsum,
+                             u64* uniq) {
   const KT empty = key_empty<KT>();
   u64 gt = (u64)blockIdx.x * blockDim.x + threadIdx.x, gs = (u64)gridDim.x * blockDim.x;
   double acc = 0.0;
@@ -499,6 +507,7 @@ __global__ void k_big_finish(const KT* tk, const double* ta, unsigned mask, cons
   }
   if (acc != 0.0) atomicAdd(dsum, acc);
   for (u64 s = gt; s <= mask; s += gs) {
+    if (!key_eq(tk[s], empty)) atomicAdd(uniq, 1ull);
     if (!key_eq(tk[s], empty) && fabs(ta[s]) > cut) {
       u64 p = atomicAdd(scount, 1ull);
       skeys[p] = tk[s];
@@ -728,7 +737,7 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
   KT* sk = (KT*)scratch_get(c, "sp_sk", SC * sizeof(KT));
   double* sa = (double*)scratch_get(c, "sp_sa", SC * sizeof(double));
   if (!l1k || !l1a || !sk || !sa || (b2 && (!l2k || !l2a))) return SFCI_ERR_NOMEM;
-  u64* scount = (u64*)scratch_get(c, "sp_scount", 4 * sizeof(u64));
+  u64* scount = (u64*)scratch_get(c, "sp_scount", 4 * sizeof(u64));  // [0] survivors, [1] distinct
   unsigned leafgrid = (unsigned)c.sm_count * 6;
   double* dpart = (double*)scratch_get(c, "sp_dpart", (leafgrid + 1) * sizeof(double));
   const unsigned OVF_CAP = 1u << 16;
@@ -820,6 +829,7 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
       la.dpart = dpart;
       la.ovf = ovf;
       la.ovf_cap = OVF_CAP;
+      la.uniq = scount + 1;
       const KT* lkeys;
       const double* lamps;
       if (b2 > 0) {
@@ -916,7 +926,8 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
           if ((st = read_words(c, inoff + id, 2 * sizeof(u64), ib_ie))) return st;
           gr = (unsigned)std::min<u64>((tsz + 255) / 256, (u64)c.sm_count * 8);
           SFCI_LAUNCH(c, k_big_finish<KT>, gr, 256, 0, (const KT*)bk, (const double*)ba, (unsigned)(tsz - 1),
-                      (const KT*)ink, (const double*)ina, ib_ie[0], ib_ie[1], cut, sk, sa, scount, dbig);
+                      (const KT*)ink, (const double*)ina, ib_ie[0], ib_ie[1], cut, sk, sa, scount, dbig,
+                      scount + 1);
         }
       }
       if ((st = read_words(c, scount, sizeof(u64), &scount_h))) return st;
@@ -949,7 +960,11 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
   out.len = nout;
   phase_end(c, tok);
   c.stats[4] = nout;
-  c.stats[2] = 0;  // unique count is not materialised separately
+  {
+    u64 uq = 0;
+    if ((st = read_words(c, scount + 1, sizeof(u64), &uq))) return st;
+    c.stats[2] = uq;
+  }
   (void)merged;
   *diag = dl + dbig_h;
   return SFCI_OK;

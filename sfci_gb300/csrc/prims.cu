@@ -18,7 +18,7 @@ __global__ void k_scan_reduce(const T* __restrict__ in, size_t n, T* __restrict_
 #pragma unroll
   for (int i = 0; i < SCAN_ITEMS; ++i) {
     size_t idx = base + (size_t)i * SCAN_THREADS + threadIdx.x;
-    if (idx < n) s += in[idx];
+    if (idx < n) s += __ldcg(in + idx);  // counts may come from atomics of the previous kernel
   }
   T tot;
   block_excl_scan<T, SCAN_THREADS>(s, &tot, sh);
@@ -33,7 +33,7 @@ __global__ void k_scan_down(const T* in, T* out, size_t n, const T* __restrict__
   T s = 0;
 #pragma unroll
   for (int i = 0; i < SCAN_ITEMS; ++i) {
-    v[i] = (base + i < n) ? in[base + i] : T(0);
+    v[i] = (base + i < n) ? __ldcg(in + base + i) : T(0);
     s += v[i];
   }
   T off = block_excl_scan<T, SCAN_THREADS>(s, nullptr, sh) + (boff ? boff[blockIdx.x] : T(0));
@@ -481,7 +481,7 @@ __global__ void k_sumsq_part(const double* __restrict__ a, size_t n, double* __r
 __global__ void k_sum_final(const double* __restrict__ part, int np, double* __restrict__ out) {
   if (threadIdx.x == 0 && blockIdx.x == 0) {
     double s = 0.0;
-    for (int i = 0; i < np; ++i) s += part[i];
+    for (int i = 0; i < np; ++i) s += __ldcg(part + i);
     *out = s;
   }
 }

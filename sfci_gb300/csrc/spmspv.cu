@@ -123,6 +123,30 @@ __device__ __forceinline__ int table_find(const KT* tk, unsigned mask, const KT&
   return -1;
 }
 
+// Global-memory variant for tables built with atomics by an earlier kernel: the
+// reads go to L2 (ld.global.cg).  Letting the compiler route them through the
+// non-coherent read-only path returned stale slots in practice.
+__device__ __forceinline__ u64 ldcg_key(const u64* p) { return __ldcg((const unsigned long long*)p); }
+__device__ __forceinline__ K128 ldcg_key(const K128* p) {
+  K128 k;
+  k.lo = __ldcg((const unsigned long long*)p);
+  k.hi = __ldcg((const unsigned long long*)p + 1);
+  return k;
+}
+
+template <class KT>
+__device__ __forceinline__ int table_find_global(const KT* tk, unsigned mask, const KT& key) {
+  unsigned slot = (unsigned)key_hash(key) & mask;
+  const KT empty = key_empty<KT>();
+  for (unsigned probe = 0; probe <= mask; ++probe) {
+    KT cur = ldcg_key(tk + slot);
+    if (key_eq(cur, key)) return (int)slot;
+    if (key_eq(cur, empty)) return -1;
+    slot = (slot + 1) & mask;
+  }
+  return -1;
+}
+
 // ---------------------------------------------------------------------------
 // per-determinant preparation: term counts and diagonal elements
 // ---------------------------------------------------------------------------
@@ -266,8 +290,8 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
             if (MODE == M_COUNT) {
               atomicAdd(&hist[(unsigned)(key_hash(key) >> shift1)], 1u);
             } else {
-              int s = table_find(g.tkeys, g.tmask, key);
-              if (s >= 0) eacc += term_amp(d, e, g.h) * g.tvals[s];
+              int s = table_find_global(g.tkeys, g.tmask, key);
+              if (s >= 0) eacc += term_amp(d, e, g.h) * __ldcg(g.tvals + s);
             }
           }
         }
@@ -482,7 +506,7 @@ __global__ void __launch_bounds__(LEAF_THREADS) k_leaf(LeafArgs<KT> a) {
   if (tid == 0) {
     double s = 0.0;
     for (int w = 0; w < LEAF_THREADS / 32; ++w) s += s_red[w];
-    a.dpart[blockIdx.x] += s;
+    atomicAdd(a.dpart + blockIdx.x, s);  // one adder per slot and launch: order stays fixed
   }
 }
 
@@ -502,16 +526,19 @@ __global__ void k_big_finish(const KT* tk, const double* ta, unsigned mask, cons
   u64 gt = (u64)blockIdx.x * blockDim.x + threadIdx.x, gs = (u64)gridDim.x * blockDim.x;
   double acc = 0.0;
   for (u64 e = ib + gt; e < ie; e += gs) {
-    int s = table_find(tk, mask, in_keys[e]);
-    if (s >= 0) acc += ta[s] * in_amps[e];
+    int s = table_find_global(tk, mask, in_keys[e]);
+    if (s >= 0) acc += __ldcg(ta + s) * in_amps[e];
   }
   if (acc != 0.0) atomicAdd(dsum, acc);
   for (u64 s = gt; s <= mask; s += gs) {
-    if (!key_eq(tk[s], empty)) atomicAdd(uniq, 1ull);
-    if (!key_eq(tk[s], empty) && fabs(ta[s]) > cut) {
+    KT k = ldcg_key(tk + s);
+    if (key_eq(k, empty)) continue;
+    atomicAdd(uniq, 1ull);
+    double v = __ldcg(ta + s);
+    if (fabs(v) > cut) {
       u64 p = atomicAdd(scount, 1ull);
-      skeys[p] = tk[s];
-      samps[p] = ta[s];
+      skeys[p] = k;
+      samps[p] = v;
     }
   }
 }
@@ -564,7 +591,7 @@ __global__ void k_table_build(const KT* __restrict__ keys, const double* __restr
 __global__ void k_sum_parts(const double* __restrict__ p, int n, double* __restrict__ out) {
   if (threadIdx.x == 0 && blockIdx.x == 0) {
     double s = 0.0;
-    for (int i = 0; i < n; ++i) s += p[i];
+    for (int i = 0; i < n; ++i) s += __ldcg(p + i);
     *out = s;
   }
 }
@@ -981,6 +1008,9 @@ int energy_impl(Ctx& c, const Vec& psi, double* E) {
   u64 *doff = nullptr, T = 0;
   double* diagE = nullptr;
   if ((st = prep_dets<W>(c, (const KT*)psi.keys, psi.len, &doff, &diagE, &T))) return st;
+  for (auto& s : c.stats) s = 0;
+  c.stats[0] = psi.len;
+  c.stats[1] = T;
   u64 tsz = 1;
   while (tsz < 2 * psi.len) tsz <<= 1;
   if (tsz > (1ull << 31)) return set_error(SFCI_ERR_UNSUPPORTED, "energy support table too large");

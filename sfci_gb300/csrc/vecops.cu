@@ -83,7 +83,7 @@ __global__ void k_dot(const KT* __restrict__ A, const double* __restrict__ Aa, u
 __global__ void k_sum_serial(const double* __restrict__ p, u64 n, double* __restrict__ out) {
   if (threadIdx.x == 0 && blockIdx.x == 0) {
     double s = 0.0;
-    for (u64 i = 0; i < n; ++i) s += p[i];
+    for (u64 i = 0; i < n; ++i) s += __ldcg(p + i);
     *out = s;
   }
 }

@@ -142,6 +142,24 @@ int sfci_lanczos_ground(sfci_ctx* ctx, sfci_vec* v, int Nl, int restarts, double
 int sfci_minres(sfci_ctx* ctx, const sfci_vec* rhs, const sfci_vec* guess, sfci_vec* result,
                 int iters, double tol, double lambda, int* iters_done);
 
+/* ---- allocation-free variant (no counterpart in the reference) -----------------
+ * Sparse dot product of two key-sorted vectors held in caller-owned DEVICE arrays
+ * (keys: n * key_words uint64 words; amplitudes: n doubles).  The result goes to
+ * the device double *d_out, queued on `stream` (a cudaStream_t; NULL = the
+ * default stream); the call does not synchronise.  It allocates no device memory:
+ * its per-block partial sums live in a fixed 64 KiB device array that every GPU
+ * loading the library holds until the process exits.  It is meant for callers
+ * that cannot allocate: code running inside another framework's device-memory
+ * pool that has reserved the GPU up front (a new cudaMalloc fails or fragments
+ * the pool), or hosts whose hot loop must not allocate.  Limit: nx + ny <=
+ * 16,777,216 entries, otherwise SFCI_ERR_ARG before any launch.  All calls share
+ * the array, so calls whose kernels overlap on the GPU race; order them on one
+ * stream.  The first call on a device looks up the array's address with that
+ * device current (cudaGetSymbolAddress); make that first call before any stream
+ * capture begins. */
+int sfci_dot_noalloc(const uint64_t* x_keys, const double* x_amps, uint64_t nx, const uint64_t* y_keys,
+                     const double* y_amps, uint64_t ny, int key_words, double* d_out, void* stream);
+
 /* Generalised symmetric eigensolve K c = E S c (Eigen GSAES as used at
  * src/sparse_solver.cpp:450), FP64 on the host: eigenvalues ascending,
  * eigenvectors column-major with c^T S c = 1. */

@@ -343,7 +343,8 @@ def run_gpu(args, rank, ws, local, dist):
                                "synthetic RHF seed 1",
                    "num_orb": 2 * M_SPATIAL, "num_e": NUM_E, "Nd": nd, "input_dets": n_in,
                    "connected_per_det": C, "emitted_per_det_reference": emitted_per_det(M_SPATIAL, 7, 7),
-                   "generated_terms_per_step": T, "survivors_per_step": surv, "output_dets": out_len,
+                   "generated_terms_per_step": T, "merged_unique_per_step": stats["unique"],
+                   "survivors_per_step": surv, "output_dets": out_len,
                    "passes": stats["passes"], "leaves": stats["leaves"],
                    "l2": "inputs larger than L2: %.0f GB of terms per step vs 129 MB" % (16.0 * T / 1e9),
                    "parallelism": "replicas" if ws > 1 else "1 GPU"},

@@ -1,25 +1,27 @@
 // SpMSpV over bitstring determinants: the GB300 replacement of SpMVMtply_bucket
 // (src/functions.cpp:511-804) and calc_energy (src/functions.cpp:1272-1313).
 //
-// Pipeline (all on one stream; sizes come from prefix sums, so nothing can
-// overflow — the reference's bucket_unit / len*5000 / numConnected buffers are
-// gone):
+// Pipeline (one stream; every buffer is sized by an exclusive scan of counts, so
+// nothing can overflow — the reference's bucket_unit / len*5000 / numConnected
+// buffers are gone):
 //   1. top-Nd of the input by |amp| (radix select, stable) — :535-550
 //   2. per-determinant term counts -> exclusive scan -> term offsets; diagonal
 //      elements D_j (DiagCal_bit, src/bitstr.cpp:433)
 //   3. COUNT sweep: every CTA generates the target keys of a fixed contiguous
-//      slice of the term space and histograms hash(key) into 2^b1 level-1 bins
+//      slice of the term space and histograms the top 8 bits of hash(key)
 //      (one row of a [bin x CTA] count matrix, no global atomics)
-//   4. the scanned matrix gives every CTA its own write cursor per bin; bins are
-//      grouped into passes that fit the device-memory budget
-//   5. per pass, SCATTER sweep: regenerate, keep terms of the pass's bins, write
-//      (key, c*H_kj) to the level-1 buffer through shared-memory cursors
-//   6. per group of bins, level-2 partition into 2^b2 leaves per bin (count
-//      matrix + cursors again), then one CTA per leaf merges duplicates in a
-//      shared-memory hash table (segmented FP64 sums, :646-731), adds the
-//      leaf's share of <v|H|v> (:674-677) and emits survivors |a| > cut (:750)
+//   4. the scanned matrix gives every CTA a private write cursor per bin; bins
+//      are grouped into passes that fit the device-memory budget
+//   5. per pass, SCATTER sweep: regenerate, keep the pass's bins, stage a round
+//      of terms in shared memory sorted by bin, and write coalesced runs
+//   6. per group of bins, MSD radix partition on further hash digits (<= 9 bits,
+//      segment-aligned units, count matrix + staged coalesced writes) down to
+//      leaves of ~512 terms; then one warp per leaf merges duplicates in a
+//      private shared-memory hash table (FP64 sums, :646-731), adds the leaf's
+//      share of <v|H|v> (:674-677) and emits survivors |a| > cut (:750)
 //   7. top-cap of the survivors (radix select) and LSD radix sort by key (:777-793)
-// The oversized-leaf fallback merges in a global-memory table instead.
+// A leaf with more distinct keys than a warp table holds is merged in a
+// global-memory table instead.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -33,19 +35,21 @@ namespace sfci {
 
 constexpr int GEN_THREADS = 512;
 constexpr int GEN_IPT = 4;
-constexpr int GEN_ROUND = GEN_THREADS * GEN_IPT;
-constexpr int P2_THREADS = 512;
-constexpr int P2_IPT = 4;
-constexpr int P2_ROUND = P2_THREADS * P2_IPT;
-constexpr int LEAF_THREADS = 256;
-constexpr int TBL_BITS = 12;
-constexpr int TBL = 1 << TBL_BITS;
-constexpr int LEAF_LIMIT = (TBL * 3) / 4;
-constexpr double LEAF_AVG = 1024.0;
-constexpr int B2_MAX = 12;
-constexpr int B1_MAX = 14;
+constexpr int GEN_ROUND = GEN_THREADS * GEN_IPT;  // terms staged per round
+constexpr int L1_BITS = 8;                        // level-1 bins of the generation sweep
+constexpr int PT_THREADS = 512;
+constexpr int DIGIT_MAX = 9;                      // bits per partition level
+constexpr unsigned long long UNIT_ITEMS = 1ull << 16;  // partition work unit
+constexpr int LW_WARPS = 4;                       // warps per leaf-merge CTA
+constexpr int TW_MAX = 1024;                      // hash slots per warp
+constexpr double LEAF_AVG = 512.0;                // target terms per leaf
+constexpr int B_MAX = 30;
 
 enum { M_COUNT = 0, M_SCATTER = 1, M_ENERGY = 2 };
+
+template <int W> struct PartIPT;
+template <> struct PartIPT<1> { static constexpr int v = 8; };
+template <> struct PartIPT<2> { static constexpr int v = 4; };
 
 SFCI_HD size_t al16(size_t x) { return (x + 15) & ~(size_t)15; }
 
@@ -172,6 +176,8 @@ __global__ void k_det_prep(const KT* __restrict__ keys, u64 n, HamView h, u64* _
 // ---------------------------------------------------------------------------
 // generation sweep
 // ---------------------------------------------------------------------------
+// generation sweep
+// ---------------------------------------------------------------------------
 template <class KT>
 struct GenArgs {
   const KT* keys;
@@ -195,6 +201,16 @@ struct GenArgs {
   double* epart;            // ENERGY: per-CTA partial
 };
 
+template <class KT>
+__host__ __device__ inline size_t gen_smem_bytes(int mode, unsigned nbp) {
+  size_t s = al16(sizeof(DetInfo<KT>)) + al16(2016 * sizeof(unsigned short));
+  if (mode != M_ENERGY) s += al16(sizeof(uint32_t) * nbp);
+  if (mode == M_SCATTER)
+    s += al16(sizeof(uint32_t) * nbp) + al16(sizeof(u64) * nbp) + al16(sizeof(KT) * GEN_ROUND) +
+         al16(sizeof(double) * GEN_ROUND) + al16(sizeof(unsigned short) * GEN_ROUND);
+  return s;
+}
+
 template <class KT, int MODE>
 __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -205,9 +221,24 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
   const unsigned nbp = (MODE == M_COUNT) ? (1u << g.b1) : (g.bin_hi - g.bin_lo);
   uint32_t* hist = reinterpret_cast<uint32_t*>(smem + off);
   off += al16(sizeof(uint32_t) * (MODE == M_ENERGY ? 0 : nbp));
-  u64* cur = reinterpret_cast<u64*>(smem + off);
+  uint32_t* bst = reinterpret_cast<uint32_t*>(smem + off);
+  u64* cur = nullptr;
+  KT* sk = nullptr;
+  double* sa = nullptr;
+  unsigned short* sb = nullptr;
+  if (MODE == M_SCATTER) {
+    off += al16(sizeof(uint32_t) * nbp);
+    cur = reinterpret_cast<u64*>(smem + off);
+    off += al16(sizeof(u64) * nbp);
+    sk = reinterpret_cast<KT*>(smem + off);
+    off += al16(sizeof(KT) * GEN_ROUND);
+    sa = reinterpret_cast<double*>(smem + off);
+    off += al16(sizeof(double) * GEN_ROUND);
+    sb = reinterpret_cast<unsigned short*>(smem + off);
+  }
   __shared__ u64 s_det;
   __shared__ double s_red[GEN_THREADS / 32];
+  __shared__ uint32_t s_scan[GEN_THREADS / 32 + 1];
 
   const int tid = threadIdx.x, lane = tid & 31;
   const unsigned G = gridDim.x;
@@ -241,7 +272,7 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
       if (MODE == M_SCATTER) {
         KT kk[GEN_IPT];
         double aa[GEN_IPT];
-        unsigned br[GEN_IPT];  // (rank << 16) | bin, or ~0u
+        unsigned br[GEN_IPT];  // (rank << 16) | local bin, or ~0u
 #pragma unroll
         for (int it = 0; it < GEN_IPT; ++it) {
           unsigned l = rb + it * GEN_THREADS + tid;
@@ -260,24 +291,31 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
           }
         }
         __syncthreads();
+        // stage the round sorted by bin, then write each bin's run contiguously
+        uint32_t tot;
+        uint32_t ex = block_excl_scan<uint32_t, GEN_THREADS>(tid < (int)nbp ? hist[tid] : 0u, &tot, s_scan);
+        if (tid < (int)nbp) bst[tid] = ex;
+        __syncthreads();
 #pragma unroll
         for (int it = 0; it < GEN_IPT; ++it) {
           if (br[it] != ~0u) {
-            unsigned lb = br[it] & 0xffffu, r = br[it] >> 16;
-            u64 pos = cur[lb] + r;
-            g.okeys[pos] = kk[it];
-            g.oamps[pos] = aa[it];
+            unsigned lb = br[it] & 0xffffu, p = bst[lb] + (br[it] >> 16);
+            sk[p] = kk[it];
+            sa[p] = aa[it];
+            sb[p] = (unsigned short)lb;
           }
         }
         __syncthreads();
-        // the holder of rank 0 advances its bin's cursor
-#pragma unroll
-        for (int it = 0; it < GEN_IPT; ++it) {
-          if (br[it] != ~0u && (br[it] >> 16) == 0) {
-            unsigned lb = br[it] & 0xffffu;
-            cur[lb] += hist[lb];
-            hist[lb] = 0;
-          }
+        for (unsigned i = tid; i < tot; i += GEN_THREADS) {
+          unsigned lb = sb[i];
+          u64 pos = cur[lb] + (i - bst[lb]);
+          g.okeys[pos] = sk[i];
+          g.oamps[pos] = sa[i];
+        }
+        __syncthreads();
+        if (tid < (int)nbp) {
+          cur[tid] += hist[tid];
+          hist[tid] = 0;
         }
         __syncthreads();
       } else {
@@ -318,106 +356,163 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
 }
 
 // ---------------------------------------------------------------------------
-// level-2 partition of level-1 bins into leaves
+// MSD radix partition of segments on a further hash digit
 // ---------------------------------------------------------------------------
+// A unit is a contiguous piece (<= UNIT_ITEMS) of one segment.  Its count for
+// digit dg lives at cbase + dg * stride of the level's count matrix, laid out
+// so that one exclusive scan orders positions by (segment, digit, unit).
+struct Unit {
+  u64 start, end, cbase;
+  unsigned stride, pad;
+};
+
 template <class KT>
-struct P2Args {
+struct PartArgs {
   const KT* ikeys;
   const double* iamps;
-  const u64* bin_off;  // nbg+1 item offsets of the group's bins in the level-1 buffer
-  unsigned nbg;        // bins in group
-  unsigned S;          // CTAs per bin
-  int b, b2;
-  u64* cntm;           // COUNT: [(lb << b2 | l2) * S + sub]
-  const u64* basem;    // SCATTER: scanned cntm (positions in the level-2 buffer)
+  const Unit* units;
+  unsigned nunits;
+  int shift;      // digit = (hash >> shift) & (nd - 1)
+  unsigned nd;
+  u64* cm;        // COUNT: counts out; SCATTER: scanned counts in
+  u64 dst_base;   // added to scanned positions
   KT* okeys;
   double* oamps;
 };
 
-template <class KT, int MODE>
-__global__ void __launch_bounds__(P2_THREADS, 2) k_part2(P2Args<KT> a) {
+template <class KT, int IPT>
+__host__ __device__ inline size_t part_smem_bytes(int mode, unsigned nd) {
+  size_t s = al16(sizeof(uint32_t) * nd);
+  if (mode == M_SCATTER) {
+    const int R = PT_THREADS * IPT;
+    s += al16(sizeof(uint32_t) * nd) + al16(sizeof(u64) * nd) + al16(sizeof(KT) * R) + al16(sizeof(double) * R) +
+         al16(sizeof(unsigned short) * R);
+  }
+  return s;
+}
+
+template <class KT, int MODE, int IPT>
+__global__ void __launch_bounds__(PT_THREADS, 2) k_part(PartArgs<KT> a) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const unsigned nl = 1u << a.b2;
-  uint32_t* hist = reinterpret_cast<uint32_t*>(smem);
-  u64* cur = reinterpret_cast<u64*>(smem + al16(sizeof(uint32_t) * nl));
+  constexpr int R = PT_THREADS * IPT;
+  const unsigned nd = a.nd;
+  size_t off = 0;
+  uint32_t* hist = reinterpret_cast<uint32_t*>(smem + off);
+  off += al16(sizeof(uint32_t) * nd);
+  uint32_t* bst = reinterpret_cast<uint32_t*>(smem + off);
+  u64* cur = nullptr;
+  KT* sk = nullptr;
+  double* sa = nullptr;
+  unsigned short* sb = nullptr;
+  if (MODE == M_SCATTER) {
+    off += al16(sizeof(uint32_t) * nd);
+    cur = reinterpret_cast<u64*>(smem + off);
+    off += al16(sizeof(u64) * nd);
+    sk = reinterpret_cast<KT*>(smem + off);
+    off += al16(sizeof(KT) * R);
+    sa = reinterpret_cast<double*>(smem + off);
+    off += al16(sizeof(double) * R);
+    sb = reinterpret_cast<unsigned short*>(smem + off);
+  }
+  __shared__ uint32_t s_scan[PT_THREADS / 32 + 1];
   const int tid = threadIdx.x;
-  const unsigned lmask = nl - 1;
-  const int shift = 64 - a.b;
-  for (unsigned unit = blockIdx.x; unit < a.nbg * a.S; unit += gridDim.x) {
-    const unsigned lb = unit / a.S, sub = unit - lb * a.S;
-    const u64 bb = a.bin_off[lb], be = a.bin_off[lb + 1], n = be - bb;
-    const u64 s0 = bb + n * sub / a.S, s1 = bb + n * (sub + 1) / a.S;
-    for (unsigned l = tid; l < nl; l += P2_THREADS) {
-      hist[l] = 0;
-      if (MODE == M_SCATTER) cur[l] = a.basem[((u64)lb * nl + l) * a.S + sub];
+  const unsigned dmask = nd - 1;
+  for (unsigned u = blockIdx.x; u < a.nunits; u += gridDim.x) {
+    const Unit un = a.units[u];
+    for (unsigned dg = tid; dg < nd; dg += PT_THREADS) {
+      hist[dg] = 0;
+      if (MODE == M_SCATTER) cur[dg] = __ldcg(a.cm + un.cbase + (u64)dg * un.stride) + a.dst_base;
     }
     __syncthreads();
-    for (u64 rb = s0; rb < s1; rb += P2_ROUND) {
+    for (u64 rb = un.start; rb < un.end; rb += R) {
       if (MODE == M_COUNT) {
 #pragma unroll
-        for (int it = 0; it < P2_IPT; ++it) {
-          u64 i = rb + (u64)it * P2_THREADS + tid;
-          if (i < s1) atomicAdd(&hist[(unsigned)(key_hash(a.ikeys[i]) >> shift) & lmask], 1u);
+        for (int it = 0; it < IPT; ++it) {
+          u64 i = rb + (u64)it * PT_THREADS + tid;
+          if (i < un.end) atomicAdd(&hist[(unsigned)(key_hash(a.ikeys[i]) >> a.shift) & dmask], 1u);
         }
       } else {
-        KT kk[P2_IPT];
-        double aa[P2_IPT];
-        unsigned br[P2_IPT];
+        KT kk[IPT];
+        double aa[IPT];
+        unsigned br[IPT];
 #pragma unroll
-        for (int it = 0; it < P2_IPT; ++it) {
-          u64 i = rb + (u64)it * P2_THREADS + tid;
+        for (int it = 0; it < IPT; ++it) {
+          u64 i = rb + (u64)it * PT_THREADS + tid;
           br[it] = ~0u;
-          if (i < s1) {
+          if (i < un.end) {
             kk[it] = a.ikeys[i];
             aa[it] = a.iamps[i];
-            unsigned l2 = (unsigned)(key_hash(kk[it]) >> shift) & lmask;
-            unsigned r = atomicAdd(&hist[l2], 1u);
-            br[it] = (r << 16) | l2;
+            unsigned dg = (unsigned)(key_hash(kk[it]) >> a.shift) & dmask;
+            unsigned r = atomicAdd(&hist[dg], 1u);
+            br[it] = (r << 16) | dg;
           }
         }
         __syncthreads();
+        // exclusive scan of the digit histogram (nd <= 512 = PT_THREADS)
+        uint32_t tot;
+        uint32_t ex = block_excl_scan<uint32_t, PT_THREADS>(tid < (int)nd ? hist[tid] : 0u, &tot, s_scan);
+        if (tid < (int)nd) bst[tid] = ex;
+        __syncthreads();
 #pragma unroll
-        for (int it = 0; it < P2_IPT; ++it) {
+        for (int it = 0; it < IPT; ++it) {
           if (br[it] != ~0u) {
-            u64 pos = cur[br[it] & 0xffffu] + (br[it] >> 16);
-            a.okeys[pos] = kk[it];
-            a.oamps[pos] = aa[it];
+            unsigned dg = br[it] & 0xffffu, p = bst[dg] + (br[it] >> 16);
+            sk[p] = kk[it];
+            sa[p] = aa[it];
+            sb[p] = (unsigned short)dg;
           }
         }
         __syncthreads();
-#pragma unroll
-        for (int it = 0; it < P2_IPT; ++it) {
-          if (br[it] != ~0u && (br[it] >> 16) == 0) {
-            unsigned l2 = br[it] & 0xffffu;
-            cur[l2] += hist[l2];
-            hist[l2] = 0;
-          }
+        for (unsigned i = tid; i < tot; i += PT_THREADS) {
+          unsigned dg = sb[i];
+          u64 pos = cur[dg] + (i - bst[dg]);
+          a.okeys[pos] = sk[i];
+          a.oamps[pos] = sa[i];
+        }
+        __syncthreads();
+        if (tid < (int)nd) {
+          cur[tid] += hist[tid];
+          hist[tid] = 0;
         }
         __syncthreads();
       }
     }
     __syncthreads();
     if (MODE == M_COUNT)
-      for (unsigned l = tid; l < nl; l += P2_THREADS) a.cntm[((u64)lb * nl + l) * a.S + sub] = hist[l];
+      for (unsigned dg = tid; dg < nd; dg += PT_THREADS) a.cm[un.cbase + (u64)dg * un.stride] = hist[dg];
     __syncthreads();
   }
 }
 
+// next level's segment boundaries: out[s*nd + dg] = scanned[segbase[s] + dg*segnu[s]] + base
+__global__ void k_seg_gather(const u64* __restrict__ cm, const u64* __restrict__ segbase,
+                             const unsigned* __restrict__ segnu, u64 nseg, unsigned nd, u64 total_idx, u64 base,
+                             u64* __restrict__ out) {
+  const u64 n = nseg * nd;
+  for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i <= n; i += (u64)gridDim.x * blockDim.x) {
+    if (i == n) {
+      out[n] = __ldcg(cm + total_idx) + base;
+    } else {
+      u64 s = i / nd;
+      unsigned dg = (unsigned)(i - s * nd);
+      out[i] = __ldcg(cm + segbase[s] + (u64)dg * segnu[s]) + base;
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
-// leaf merge
+// leaf merge: one warp per leaf, private shared-memory hash table
 // ---------------------------------------------------------------------------
 template <class KT>
 struct LeafArgs {
   const KT* keys;
   const double* amps;
-  const u64* loff;     // leaf l spans [loff[l*lstride] - lbase, loff[(l+1)*lstride] - lbase)
-  unsigned lstride;
-  u64 lbase;
+  const u64* loff;     // nleaves + 1 boundaries in keys/amps
   u64 nleaves;
   u64 gleaf0;          // global leaf id of local leaf 0
   const KT* in_keys;   // input dets sorted by global leaf
   const double* in_amps;
-  const u64* in_off;   // [2^b + 1]
+  const uint32_t* in_off;  // [2^b + 1]
   double cut;
   KT* skeys;
   double* samps;
@@ -429,84 +524,86 @@ struct LeafArgs {
 };
 
 template <class KT>
-__global__ void __launch_bounds__(LEAF_THREADS) k_leaf(LeafArgs<KT> a) {
+__global__ void __launch_bounds__(LW_WARPS * 32) k_leafw(LeafArgs<KT> a) {
   extern __shared__ __align__(16) unsigned char smem[];
-  KT* tk = reinterpret_cast<KT*>(smem);
-  double* ta = reinterpret_cast<double*>(smem + sizeof(KT) * TBL);
-  __shared__ unsigned s_nuniq, s_ovf;
-  __shared__ u64 s_sum[LEAF_THREADS / 32 + 1];
-  __shared__ double s_red[LEAF_THREADS / 32];
-  __shared__ u64 s_base;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  KT* tk = reinterpret_cast<KT*>(smem) + (size_t)warp * TW_MAX;
+  double* ta = reinterpret_cast<double*>(smem + sizeof(KT) * TW_MAX * LW_WARPS) + (size_t)warp * TW_MAX;
+  __shared__ unsigned s_nu[LW_WARPS];
+  __shared__ double s_red[LW_WARPS];
+  __shared__ u64 s_uq[LW_WARPS];
   const KT empty = key_empty<KT>();
+  const unsigned lt = (1u << lane) - 1u;
   double dacc = 0.0;
-  for (u64 leaf = blockIdx.x; leaf < a.nleaves; leaf += gridDim.x) {
-    const u64 beg = a.loff[leaf * a.lstride] - a.lbase, end = a.loff[(leaf + 1) * a.lstride] - a.lbase;
-    // table sized to the leaf: >= 2x its terms (so it cannot fill), 512..TBL slots
-    const u64 n = end - beg;
-    unsigned tb = 512;
-    while (tb < TBL && (u64)tb < 2 * n) tb <<= 1;
-    const unsigned limit = tb == TBL ? LEAF_LIMIT : tb;
-    for (unsigned s = tid; s < tb; s += LEAF_THREADS) {
+  u64 uq = 0;
+  for (u64 leaf = (u64)blockIdx.x * LW_WARPS + warp; leaf < a.nleaves; leaf += (u64)gridDim.x * LW_WARPS) {
+    const u64 beg = a.loff[leaf], end = a.loff[leaf + 1], n = end - beg;
+    unsigned tb = 64;
+    while (tb < (unsigned)TW_MAX && (u64)tb < 2 * n) tb <<= 1;
+    const unsigned limit = (tb * 3) / 4;
+    for (unsigned s = lane; s < tb; s += 32) {
       tk[s] = empty;
       ta[s] = 0.0;
     }
-    if (tid == 0) {
-      s_nuniq = 0;
-      s_ovf = 0;
+    if (lane == 0) s_nu[warp] = 0;
+    __syncwarp();
+    bool ovf = false;
+    for (u64 e = beg + lane; e < end; e += 32) {
+      if (!table_add(tk, ta, tb - 1, a.keys[e], a.amps[e], &s_nu[warp], limit)) {
+        ovf = true;
+        break;
+      }
     }
-    __syncthreads();
-    for (u64 e = beg + tid; e < end; e += LEAF_THREADS) {
-      if (*(volatile unsigned*)&s_ovf) break;
-      if (!table_add(tk, ta, tb - 1, a.keys[e], a.amps[e], &s_nuniq, limit)) s_ovf = 1;
-    }
-    __syncthreads();
-    if (s_ovf) {
-      if (tid == 0) {
+    ovf = __any_sync(0xffffffffu, ovf);
+    __syncwarp();
+    if (ovf) {
+      if (lane == 0) {
         unsigned k = atomicAdd(&a.ovf[0], 1u);
         if (k < a.ovf_cap) a.ovf[1 + k] = (unsigned)(a.gleaf0 + leaf);
       }
-      __syncthreads();
+      __syncwarp();
       continue;
     }
-    // <v| (H - lambda) |v> share of this leaf
     const u64 gl = a.gleaf0 + leaf;
-    for (u64 e = a.in_off[gl] + tid; e < a.in_off[gl + 1]; e += LEAF_THREADS) {
+    for (u64 e = a.in_off[gl] + lane; e < a.in_off[gl + 1]; e += 32) {
       int s = table_find(tk, tb - 1, a.in_keys[e]);
       if (s >= 0) dacc += ta[s] * a.in_amps[e];
     }
-    // survivors |a| > cut: each thread owns tb/THREADS consecutive slots
-    const unsigned per = tb / LEAF_THREADS;
-    unsigned c = 0;
-    for (unsigned q = 0; q < per; ++q) {
-      unsigned s = tid * per + q;
-      if (!key_eq(tk[s], empty) && fabs(ta[s]) > a.cut) ++c;
-    }
-    u64 tot;
-    u64 ex = block_excl_scan<u64, LEAF_THREADS>((u64)c, &tot, s_sum);
-    if (tid == 0) {
-      s_base = tot ? atomicAdd(a.scount, tot) : 0;
-      atomicAdd(a.uniq, (u64)s_nuniq);
-    }
-    __syncthreads();
-    u64 pos = s_base + ex;
-    for (unsigned q = 0; q < per; ++q) {
-      unsigned s = tid * per + q;
-      if (!key_eq(tk[s], empty) && fabs(ta[s]) > a.cut) {
-        a.skeys[pos] = tk[s];
-        a.samps[pos] = ta[s];
-        ++pos;
+    for (unsigned base = 0; base < tb; base += 32) {
+      const unsigned s = base + lane;
+      const KT k = tk[s];
+      const double v = ta[s];
+      const bool keep = !key_eq(k, empty) && fabs(v) > a.cut;
+      const unsigned m = __ballot_sync(0xffffffffu, keep);
+      if (m) {
+        u64 b0 = 0;
+        if (lane == 0) b0 = atomicAdd(a.scount, (u64)__popc(m));
+        b0 = __shfl_sync(0xffffffffu, b0, 0);
+        if (keep) {
+          const u64 p = b0 + __popc(m & lt);
+          a.skeys[p] = k;
+          a.samps[p] = v;
+        }
       }
     }
-    __syncthreads();
+    if (lane == 0) uq += s_nu[warp];
+    __syncwarp();
   }
   double v = warp_sum(dacc);
-  if (lane == 0) s_red[warp] = v;
+  if (lane == 0) {
+    s_red[warp] = v;
+    s_uq[warp] = uq;
+  }
   __syncthreads();
   if (tid == 0) {
     double s = 0.0;
-    for (int w = 0; w < LEAF_THREADS / 32; ++w) s += s_red[w];
-    atomicAdd(a.dpart + blockIdx.x, s);  // one adder per slot and launch: order stays fixed
+    u64 q = 0;
+    for (int w = 0; w < LW_WARPS; ++w) {
+      s += s_red[w];
+      q += s_uq[w];
+    }
+    atomicAdd(a.dpart + blockIdx.x, s);  // one adder per slot and launch: the order stays fixed
+    if (q) atomicAdd(a.uniq, q);
   }
 }
 
@@ -556,15 +653,15 @@ __global__ void k_fill_empty(KT* tk, double* ta, u64 n) {
 // input determinants grouped by global leaf (for the <v|Hv> lookups)
 // ---------------------------------------------------------------------------
 template <class KT>
-__global__ void k_in_count(const KT* __restrict__ keys, u64 n, int b, u64* __restrict__ cnt) {
+__global__ void k_in_count(const KT* __restrict__ keys, u64 n, int b, uint32_t* __restrict__ cnt) {
   for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (u64)gridDim.x * blockDim.x)
-    atomicAdd(&cnt[key_hash(keys[i]) >> (64 - b)], 1ull);
+    atomicAdd(&cnt[key_hash(keys[i]) >> (64 - b)], 1u);
 }
 template <class KT>
 __global__ void k_in_scatter(const KT* __restrict__ keys, const double* __restrict__ amps, u64 n, int b,
-                             u64* __restrict__ cur, KT* __restrict__ ok, double* __restrict__ oa) {
+                             uint32_t* __restrict__ cur, KT* __restrict__ ok, double* __restrict__ oa) {
   for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (u64)gridDim.x * blockDim.x) {
-    u64 p = atomicAdd(&cur[key_hash(keys[i]) >> (64 - b)], 1ull);
+    u64 p = atomicAdd(&cur[key_hash(keys[i]) >> (64 - b)], 1u);
     ok[p] = keys[i];
     oa[p] = amps[i];
   }
@@ -600,6 +697,7 @@ __global__ void k_sum_parts(const double* __restrict__ p, int n, double* __restr
 // host orchestration
 // ---------------------------------------------------------------------------
 
+
 static HamView ham_view(Ctx& c) {
   HamView h;
   h.N = c.N;
@@ -611,19 +709,10 @@ static HamView ham_view(Ctx& c) {
   return h;
 }
 
-template <int W>
-static size_t gen_smem(int mode, unsigned nbp) {
-  typedef typename KeyOf<W>::T KT;
-  size_t s = al16(sizeof(DetInfo<KT>)) + al16(2016 * sizeof(unsigned short));
-  if (mode != M_ENERGY) s += al16(sizeof(uint32_t) * nbp);
-  if (mode == M_SCATTER) s += al16(sizeof(u64) * nbp);
-  return s;
-}
-
 template <int W, int MODE>
 static int launch_gen(Ctx& c, const GenArgs<typename KeyOf<W>::T>& g, unsigned grid, unsigned nbp) {
   typedef typename KeyOf<W>::T KT;
-  size_t sm = gen_smem<W>(MODE, nbp);
+  size_t sm = gen_smem_bytes<KT>(MODE, nbp);
   static size_t configured = 0;
   if (sm > 48 * 1024 && sm > configured) {
     SFCI_CUDA(cudaFuncSetAttribute(k_gen<KT, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
@@ -657,8 +746,24 @@ static unsigned gen_grid(Ctx& c, u64 T) {
 }
 
 template <int W>
+static int leaf_smem_config() {
+  typedef typename KeyOf<W>::T KT;
+  static bool done = false;
+  if (!done) {
+    const int sm = (int)((sizeof(KT) + sizeof(double)) * TW_MAX * LW_WARPS);
+    SFCI_CUDA(cudaFuncSetAttribute(k_leafw<KT>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    constexpr int IPT = PartIPT<W>::v;
+    const int ps = (int)part_smem_bytes<KT, IPT>(M_SCATTER, 1u << DIGIT_MAX);
+    SFCI_CUDA(cudaFuncSetAttribute(k_part<KT, M_SCATTER, IPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, ps));
+    done = true;
+  }
+  return SFCI_OK;
+}
+
+template <int W>
 int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, double* diag) {
   typedef typename KeyOf<W>::T KT;
+  constexpr int IPT = PartIPT<W>::v;
   for (auto& s : c.stats) s = 0;
   if (in.len == 0) {
     out.len = 0;
@@ -667,6 +772,7 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
   const double cut = c.opts.coeff_cut;
   const u64 Nd = c.opts.Nd;
   int st;
+  if ((st = leaf_smem_config<W>())) return st;
   int tok = phase_begin(c, PH_OTHER);
   // 1. top-Nd of the input by |amp|
   const KT* src_k = (const KT*)in.keys;
@@ -688,13 +794,15 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
   double* diagE = nullptr;
   if ((st = prep_dets<W>(c, src_k, ns, &doff, &diagE, &T))) return st;
   c.stats[1] = T;
-  // hash-partition geometry
+  // hash digits: level 1 (generation) d0 bits, then nlev partition levels
   int b = (int)std::ceil(std::log2(std::max(2.0, (double)T / LEAF_AVG)));
-  if (b < 1) b = 1;
-  int b2 = std::min(std::max(b - 11, 0), B2_MAX);
-  int b1 = b - b2;
-  if (b1 > B1_MAX) return set_error(SFCI_ERR_UNSUPPORTED, "SpMSpV term count beyond 2^26 leaves");
-  const unsigned NB1 = 1u << b1;
+  b = std::max(1, std::min(b, B_MAX));
+  const int d0 = std::min(b, L1_BITS);
+  const int rem = b - d0;
+  const int nlev = rem ? (rem + DIGIT_MAX - 1) / DIGIT_MAX : 0;
+  std::vector<int> dig(nlev);
+  for (int k = 0; k < nlev; ++k) dig[k] = rem / nlev + (k < rem % nlev ? 1 : 0);
+  const unsigned NB1 = 1u << d0;
   const unsigned G = gen_grid(c, T);
   phase_end(c, tok);
 
@@ -712,13 +820,12 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
   g.lambda = lambda;
   g.h = ham_view(c);
   g.T = T;
-  g.b1 = b1;
+  g.b1 = d0;
   g.cntm = cntm;
   if ((st = launch_gen<W, M_COUNT>(c, g, G, NB1))) return st;
   if ((st = scan_excl(c, cntm, cntm, (u64)NB1 * G))) return st;
   std::vector<u64> binoff(NB1 + 1);
   {
-    // bin start offsets: cntm[bin * G] for every bin, plus the total
     u64* bo = (u64*)scratch_get(c, "sp_binoff", (NB1 + 1) * sizeof(u64));
     if (!bo) return SFCI_ERR_NOMEM;
     SFCI_CUDA(cudaMemcpy2DAsync(bo, sizeof(u64), cntm, G * sizeof(u64), sizeof(u64), NB1, cudaMemcpyDeviceToDevice,
@@ -736,9 +843,8 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
   for (unsigned i = 0; i < NB1; ++i) maxbin = std::max(maxbin, binoff[i + 1] - binoff[i]);
   size_t freeb = 0, totb = 0;
   SFCI_CUDA(cudaMemGetInfo(&freeb, &totb));
-  // buffers this call may grow into: what it already holds plus what is free
   size_t held = 0;
-  for (const char* nm : {"sp_l1k", "sp_l1a", "sp_l2k", "sp_l2a", "sp_sk", "sp_sa"}) {
+  for (const char* nm : {"sp_l1k", "sp_l1a", "sp_l2k", "sp_l2a", "sp_sk", "sp_sa", "topk_k", "topk_a"}) {
     auto it = c.scratch.find(nm);
     if (it != c.scratch.end()) held += it->second.bytes;
   }
@@ -748,10 +854,10 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
   // level-2 group capacity, survivor capacity (x2: a reduction of the survivors
   // stages through a second buffer of the same size), level-1 capacity
   u64 C2 = std::max<u64>(maxbin, std::min<u64>(T, std::max<u64>(avail / 16, 1u << 20)));
-  if (b2 == 0) C2 = std::max<u64>(maxbin, std::min<u64>(T, avail / 6));
+  if (nlev == 0) C2 = std::max<u64>(maxbin, std::min<u64>(T, avail / 6));
   u64 SC = std::min<u64>(cap, T) + std::min<u64>(C2, T);
   u64 C1 = T;
-  u64 l2need = (b2 > 0) ? C2 : 0;
+  u64 l2need = (nlev > 0) ? C2 : 0;
   if (C1 + l2need + 2 * SC > avail) {
     if (avail < l2need + 2 * SC + maxbin) return set_error(SFCI_ERR_NOMEM, "SpMSpV device-memory budget too small");
     C1 = avail - l2need - 2 * SC;
@@ -759,13 +865,13 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
   if (C1 < maxbin || C2 < maxbin) return set_error(SFCI_ERR_NOMEM, "SpMSpV level-1 bin exceeds its buffer");
   KT* l1k = (KT*)scratch_get(c, "sp_l1k", C1 * sizeof(KT));
   double* l1a = (double*)scratch_get(c, "sp_l1a", C1 * sizeof(double));
-  KT* l2k = b2 ? (KT*)scratch_get(c, "sp_l2k", C2 * sizeof(KT)) : nullptr;
-  double* l2a = b2 ? (double*)scratch_get(c, "sp_l2a", C2 * sizeof(double)) : nullptr;
+  KT* l2k = nlev ? (KT*)scratch_get(c, "sp_l2k", C2 * sizeof(KT)) : nullptr;
+  double* l2a = nlev ? (double*)scratch_get(c, "sp_l2a", C2 * sizeof(double)) : nullptr;
   KT* sk = (KT*)scratch_get(c, "sp_sk", SC * sizeof(KT));
   double* sa = (double*)scratch_get(c, "sp_sa", SC * sizeof(double));
-  if (!l1k || !l1a || !sk || !sa || (b2 && (!l2k || !l2a))) return SFCI_ERR_NOMEM;
+  if (!l1k || !l1a || !sk || !sa || (nlev && (!l2k || !l2a))) return SFCI_ERR_NOMEM;
   u64* scount = (u64*)scratch_get(c, "sp_scount", 4 * sizeof(u64));  // [0] survivors, [1] distinct
-  unsigned leafgrid = (unsigned)c.sm_count * 6;
+  const unsigned leafgrid = (unsigned)c.sm_count * 8;
   double* dpart = (double*)scratch_get(c, "sp_dpart", (leafgrid + 1) * sizeof(double));
   const unsigned OVF_CAP = 1u << 16;
   unsigned* ovf = (unsigned*)scratch_get(c, "sp_ovf", (OVF_CAP + 1) * sizeof(unsigned));
@@ -773,19 +879,19 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
   SFCI_CUDA(cudaMemsetAsync(scount, 0, 4 * sizeof(u64), c.stream));
   SFCI_CUDA(cudaMemsetAsync(dpart, 0, (leafgrid + 1) * sizeof(double), c.stream));
 
-  // input dets grouped by global leaf
+  // input dets grouped by global leaf (top b bits of the hash)
   const u64 NL = 1ull << b;
-  u64* inoff = (u64*)scratch_get(c, "sp_inoff", (NL + 1) * sizeof(u64));
-  u64* incur = (u64*)scratch_get(c, "sp_incur", (NL + 1) * sizeof(u64));
+  uint32_t* inoff = (uint32_t*)scratch_get(c, "sp_inoff", (NL + 1) * sizeof(uint32_t));
+  uint32_t* incur = (uint32_t*)scratch_get(c, "sp_incur", (NL + 1) * sizeof(uint32_t));
   KT* ink = (KT*)scratch_get(c, "sp_ink", ns * sizeof(KT));
   double* ina = (double*)scratch_get(c, "sp_ina", ns * sizeof(double));
   if (!inoff || !incur || !ink || !ina) return SFCI_ERR_NOMEM;
-  SFCI_CUDA(cudaMemsetAsync(inoff, 0, (NL + 1) * sizeof(u64), c.stream));
+  SFCI_CUDA(cudaMemsetAsync(inoff, 0, (NL + 1) * sizeof(uint32_t), c.stream));
   {
     unsigned gr = (unsigned)std::min<u64>((ns + 255) / 256, (u64)c.sm_count * 8);
     SFCI_LAUNCH(c, k_in_count<KT>, gr, 256, 0, src_k, ns, b, inoff);
-    if ((st = scan_excl(c, inoff, inoff, NL))) return st;
-    SFCI_CUDA(cudaMemcpyAsync(incur, inoff, NL * sizeof(u64), cudaMemcpyDeviceToDevice, c.stream));
+    if ((st = scan_excl_u32(c, inoff, inoff, NL))) return st;
+    SFCI_CUDA(cudaMemcpyAsync(incur, inoff, NL * sizeof(uint32_t), cudaMemcpyDeviceToDevice, c.stream));
     SFCI_LAUNCH(c, k_in_scatter<KT>, gr, 256, 0, src_k, src_a, ns, b, incur, ink, ina);
   }
   phase_end(c, tok);
@@ -803,23 +909,19 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
   }
   c.stats[5] = passes.size();
   c.stats[6] = NL;
-  const size_t lsm = (sizeof(KT) + sizeof(double)) * TBL;
-  {
-    static size_t cfg = 0;
-    if (lsm > cfg) {
-      SFCI_CUDA(cudaFuncSetAttribute(k_leaf<KT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lsm));
-      cfg = lsm;
-    }
-  }
-  u64 scount_h = 0, merged = 0, big_leaves = 0;
+  u64 scount_h = 0, big_leaves = 0;
   double dbig_h = 0.0;
   double* dbig = (double*)scratch_get(c, "sp_dbig", sizeof(double));
   if (!dbig) return SFCI_ERR_NOMEM;
   SFCI_CUDA(cudaMemsetAsync(dbig, 0, sizeof(double), c.stream));
-  std::vector<u64> gbo;
+  const size_t lsm = (sizeof(KT) + sizeof(double)) * TW_MAX * LW_WARPS;
+  std::vector<u64> segs, nsegs_h;
+  std::vector<Unit> units;
+  std::vector<u64> segbase;
+  std::vector<unsigned> segnu;
   for (auto& ps : passes) {
     const unsigned lo = ps.first, hi = ps.second;
-    // 5. SCATTER sweep for this pass
+    // 5. SCATTER sweep for this pass (level-1 buffer holds bins [lo, hi))
     tok = phase_begin(c, PH_SCATTER);
     g.bin_lo = lo;
     g.bin_hi = hi;
@@ -829,13 +931,11 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
     g.oamps = l1a;
     if ((st = launch_gen<W, M_SCATTER>(c, g, G, hi - lo))) return st;
     phase_end(c, tok);
-    // groups of bins
     unsigned glo = lo;
     while (glo < hi) {
       unsigned ghi = glo + 1;
       while (ghi < hi && binoff[ghi + 1] - binoff[glo] <= C2) ++ghi;
       const u64 gterms = binoff[ghi] - binoff[glo];
-      // survivors buffer headroom
       if (scount_h + gterms > SC && scount_h > cap) {
         int t2 = phase_begin(c, PH_SELECT);
         size_t m = 0;
@@ -845,7 +945,105 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
         phase_end(c, t2);
       }
       const unsigned nbg = ghi - glo;
+      // segments of this group: its level-1 bins, positions in the level-1 buffer
+      segs.assign(nbg + 1, 0);
+      for (unsigned i = 0; i <= nbg; ++i) segs[i] = binoff[glo + i] - binoff[lo];
+      const u64 gbase = segs[0];
+      KT* srck = l1k;
+      double* srca = l1a;
+      KT* dstk = l2k;
+      double* dsta = l2a;
+      bool dst_is_l1 = false;
+      u64* loff_dev = nullptr;
+      // 6a. partition levels
+      tok = phase_begin(c, PH_PARTITION);
+      int consumed = d0;
+      for (int k = 0; k < nlev; ++k) {
+        const unsigned nd = 1u << dig[k];
+        const u64 nseg = segs.size() - 1;
+        units.clear();
+        segbase.assign(nseg, 0);
+        segnu.assign(nseg, 0);
+        u64 cbase = 0;
+        for (u64 s = 0; s < nseg; ++s) {
+          const u64 a0 = segs[s], a1 = segs[s + 1], n = a1 - a0;
+          const unsigned nu = (unsigned)std::max<u64>(1, (n + UNIT_ITEMS - 1) / UNIT_ITEMS);
+          segbase[s] = cbase;
+          segnu[s] = nu;
+          for (unsigned j = 0; j < nu; ++j) {
+            Unit un;
+            un.start = a0 + (u64)j * UNIT_ITEMS;
+            un.end = std::min<u64>(a1, un.start + UNIT_ITEMS);
+            if (un.start > un.end) un.start = un.end;
+            un.cbase = cbase + j;
+            un.stride = nu;
+            un.pad = 0;
+            units.push_back(un);
+          }
+          cbase += (u64)nu * nd;
+        }
+        const u64 mlen = cbase;
+        Unit* du = (Unit*)scratch_get(c, "sp_units", units.size() * sizeof(Unit));
+        u64* cm = (u64*)scratch_get(c, "sp_cm", (mlen + 1) * sizeof(u64));
+        u64* dsb = (u64*)scratch_get(c, "sp_segbase", nseg * sizeof(u64));
+        unsigned* dsn = (unsigned*)scratch_get(c, "sp_segnu", nseg * sizeof(unsigned));
+        u64* nextoff = (u64*)scratch_get(c, k == nlev - 1 ? "sp_loff" : "sp_segoff", (nseg * nd + 1) * sizeof(u64));
+        if (!du || !cm || !dsb || !dsn || !nextoff) return SFCI_ERR_NOMEM;
+        SFCI_CUDA(cudaMemcpyAsync(du, units.data(), units.size() * sizeof(Unit), cudaMemcpyHostToDevice, c.stream));
+        SFCI_CUDA(cudaMemcpyAsync(dsb, segbase.data(), nseg * sizeof(u64), cudaMemcpyHostToDevice, c.stream));
+        SFCI_CUDA(cudaMemcpyAsync(dsn, segnu.data(), nseg * sizeof(unsigned), cudaMemcpyHostToDevice, c.stream));
+        PartArgs<KT> pa{};
+        pa.ikeys = srck;
+        pa.iamps = srca;
+        pa.units = du;
+        pa.nunits = (unsigned)units.size();
+        pa.shift = 64 - consumed - dig[k];
+        pa.nd = nd;
+        pa.cm = cm;
+        pa.dst_base = dst_is_l1 ? gbase : 0;
+        pa.okeys = dstk;
+        pa.oamps = dsta;
+        const unsigned pgrid = (unsigned)std::min<u64>(units.size(), (u64)c.sm_count * 4);
+        const size_t smc = part_smem_bytes<KT, IPT>(M_COUNT, nd);
+        const size_t sms = part_smem_bytes<KT, IPT>(M_SCATTER, nd);
+        SFCI_LAUNCH(c, (k_part<KT, M_COUNT, IPT>), pgrid, PT_THREADS, smc, pa);
+        if ((st = scan_excl(c, cm, cm, mlen))) return st;
+        SFCI_LAUNCH(c, (k_part<KT, M_SCATTER, IPT>), pgrid, PT_THREADS, sms, pa);
+        {
+          const u64 nn = nseg * nd + 1;
+          unsigned gr = (unsigned)std::min<u64>((nn + 255) / 256, (u64)c.sm_count * 8);
+          SFCI_LAUNCH(c, k_seg_gather, gr, 256, 0, (const u64*)cm, (const u64*)dsb, (const unsigned*)dsn, nseg, nd,
+                      mlen, pa.dst_base, nextoff);
+        }
+        consumed += dig[k];
+        if (k == nlev - 1) {
+          loff_dev = nextoff;
+          segs.resize(nseg * nd + 1);  // sizes only needed for the leaf count below
+        } else {
+          nsegs_h.resize(nseg * nd + 1);
+          if ((st = read_words(c, nextoff, (nseg * nd + 1) * sizeof(u64), nsegs_h.data()))) return st;
+          segs.swap(nsegs_h);
+        }
+        std::swap(srck, dstk);
+        std::swap(srca, dsta);
+        dst_is_l1 = !dst_is_l1;
+      }
+      phase_end(c, tok);
+      const u64 nleaves = segs.size() - 1;
+      if (nlev == 0) {
+        loff_dev = (u64*)scratch_get(c, "sp_loff", (nleaves + 1) * sizeof(u64));
+        if (!loff_dev) return SFCI_ERR_NOMEM;
+        SFCI_CUDA(cudaMemcpyAsync(loff_dev, segs.data(), (nleaves + 1) * sizeof(u64), cudaMemcpyHostToDevice,
+                                  c.stream));
+      }
+      // 6b. leaf merge (one warp per leaf)
+      tok = phase_begin(c, PH_MERGE);
       LeafArgs<KT> la{};
+      la.keys = srck;
+      la.amps = srca;
+      la.loff = loff_dev;
+      la.nleaves = nleaves;
+      la.gleaf0 = (u64)glo << (b - d0);
       la.in_keys = ink;
       la.in_amps = ina;
       la.in_off = inoff;
@@ -857,73 +1055,9 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
       la.ovf = ovf;
       la.ovf_cap = OVF_CAP;
       la.uniq = scount + 1;
-      const KT* lkeys;
-      const double* lamps;
-      if (b2 > 0) {
-        // 6a. level-2 partition of the group's bins
-        tok = phase_begin(c, PH_PARTITION);
-        gbo.assign(nbg + 1, 0);
-        for (unsigned i = 0; i <= nbg; ++i) gbo[i] = binoff[glo + i] - binoff[lo];
-        u64* dgbo = (u64*)scratch_get(c, "sp_gbo", (nbg + 1) * sizeof(u64));
-        if (!dgbo) return SFCI_ERR_NOMEM;
-        SFCI_CUDA(cudaMemcpyAsync(dgbo, gbo.data(), (nbg + 1) * sizeof(u64), cudaMemcpyHostToDevice, c.stream));
-        const unsigned nl = 1u << b2;
-        unsigned S = (unsigned)std::min<u64>(16, std::max<u64>(1, ((u64)c.sm_count * 4 + nbg - 1) / nbg));
-        u64 mlen = (u64)nbg * nl * S;
-        u64* cm2 = (u64*)scratch_get(c, "sp_cm2", (mlen + 1) * sizeof(u64));
-        if (!cm2) return SFCI_ERR_NOMEM;
-        P2Args<KT> pa{};
-        pa.ikeys = l1k;
-        pa.iamps = l1a;
-        pa.bin_off = dgbo;
-        pa.nbg = nbg;
-        pa.S = S;
-        pa.b = b;
-        pa.b2 = b2;
-        pa.cntm = cm2;
-        pa.basem = cm2;
-        pa.okeys = l2k;
-        pa.oamps = l2a;
-        size_t psm = al16(sizeof(uint32_t) * nl) + al16(sizeof(u64) * nl);
-        unsigned pgrid = (unsigned)std::min<u64>((u64)nbg * S, (u64)c.sm_count * 4);
-        {
-          static size_t cfg2 = 0;
-          if (psm > 48 * 1024 && psm > cfg2) {
-            SFCI_CUDA(cudaFuncSetAttribute(k_part2<KT, M_COUNT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psm));
-            SFCI_CUDA(cudaFuncSetAttribute(k_part2<KT, M_SCATTER>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psm));
-            cfg2 = psm;
-          }
-        }
-        SFCI_LAUNCH(c, (k_part2<KT, M_COUNT>), pgrid, P2_THREADS, psm, pa);
-        if ((st = scan_excl(c, cm2, cm2, mlen))) return st;
-        SFCI_LAUNCH(c, (k_part2<KT, M_SCATTER>), pgrid, P2_THREADS, psm, pa);
-        phase_end(c, tok);
-        lkeys = l2k;
-        lamps = l2a;
-        la.loff = cm2;
-        la.lstride = S;
-        la.lbase = 0;
-        la.nleaves = (u64)nbg * nl;
-        la.gleaf0 = (u64)glo << b2;
-      } else {
-        lkeys = l1k;
-        lamps = l1a;
-        la.loff = cntm + (u64)glo * G;
-        la.lstride = G;
-        la.lbase = binoff[lo];
-        la.nleaves = nbg;
-        la.gleaf0 = glo;
-        if (ghi == NB1) {
-          // loff[(nleaves) * G] must be the total: cntm has NB1*G+1 entries with the total last
-        }
-      }
-      // 6b. leaf merge
-      tok = phase_begin(c, PH_MERGE);
-      la.keys = lkeys;
-      la.amps = lamps;
       SFCI_CUDA(cudaMemsetAsync(ovf, 0, sizeof(unsigned), c.stream));
-      unsigned lg = (unsigned)std::min<u64>(la.nleaves, leafgrid);
-      SFCI_LAUNCH(c, k_leaf<KT>, lg, LEAF_THREADS, lsm, la);
+      const unsigned lg = (unsigned)std::min<u64>((nleaves + LW_WARPS - 1) / LW_WARPS, leafgrid);
+      SFCI_LAUNCH(c, k_leafw<KT>, lg, LW_WARPS * 32, lsm, la);
       unsigned novf = 0;
       if ((st = read_words(c, ovf, sizeof(unsigned), &novf))) return st;
       if (novf > OVF_CAP) return set_error(SFCI_ERR_NOMEM, "too many oversized SpMSpV leaves");
@@ -932,11 +1066,10 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
         if ((st = read_words(c, ovf + 1, novf * sizeof(unsigned), ids.data()))) return st;
         big_leaves += novf;
         for (unsigned id : ids) {
-          u64 lid = id - la.gleaf0;
+          const u64 lid = id - la.gleaf0;
           u64 lb2[2];
-          if ((st = read_words(c, la.loff + lid * la.lstride, sizeof(u64), &lb2[0]))) return st;
-          if ((st = read_words(c, la.loff + (lid + 1) * la.lstride, sizeof(u64), &lb2[1]))) return st;
-          u64 beg = lb2[0] - la.lbase, end = lb2[1] - la.lbase, n = end - beg;
+          if ((st = read_words(c, loff_dev + lid, 2 * sizeof(u64), lb2))) return st;
+          const u64 beg = lb2[0], end = lb2[1], n = end - beg;
           u64 tsz = 1;
           while (tsz < 2 * n) tsz <<= 1;
           KT* bk = (KT*)scratch_get(c, "sp_bigk", tsz * sizeof(KT));
@@ -948,18 +1081,18 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
           SFCI_CUDA(cudaMemsetAsync(bu, 0, sizeof(unsigned), c.stream));
           gr = (unsigned)std::min<u64>((n + 255) / 256, (u64)c.sm_count * 8);
           if (gr == 0) gr = 1;
-          SFCI_LAUNCH(c, k_big_insert<KT>, gr, 256, 0, lkeys, lamps, beg, end, bk, ba, (unsigned)(tsz - 1), bu);
-          u64 ib_ie[2];
-          if ((st = read_words(c, inoff + id, 2 * sizeof(u64), ib_ie))) return st;
+          SFCI_LAUNCH(c, k_big_insert<KT>, gr, 256, 0, (const KT*)srck, (const double*)srca, beg, end, bk, ba,
+                      (unsigned)(tsz - 1), bu);
+          uint32_t ib_ie[2];
+          if ((st = read_words(c, inoff + id, 2 * sizeof(uint32_t), ib_ie))) return st;
           gr = (unsigned)std::min<u64>((tsz + 255) / 256, (u64)c.sm_count * 8);
           SFCI_LAUNCH(c, k_big_finish<KT>, gr, 256, 0, (const KT*)bk, (const double*)ba, (unsigned)(tsz - 1),
-                      (const KT*)ink, (const double*)ina, ib_ie[0], ib_ie[1], cut, sk, sa, scount, dbig,
+                      (const KT*)ink, (const double*)ina, (u64)ib_ie[0], (u64)ib_ie[1], cut, sk, sa, scount, dbig,
                       scount + 1);
         }
       }
       if ((st = read_words(c, scount, sizeof(u64), &scount_h))) return st;
       phase_end(c, tok);
-      merged += gterms;
       glo = ghi;
     }
   }
@@ -992,7 +1125,6 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
     if ((st = read_words(c, scount + 1, sizeof(u64), &uq))) return st;
     c.stats[2] = uq;
   }
-  (void)merged;
   *diag = dl + dbig_h;
   return SFCI_OK;
 }

@@ -56,6 +56,7 @@ struct Ctx {
   std::vector<cudaEvent_t> ev_pool;
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ph_pending;
   uint64_t stats[8] = {};
+  double dup_est = 0.0;  // terms per distinct key of the last SpMSpV (sizes its leaves)
   // vectors created on this context (freed with it; their handles become orphans)
   std::set<struct Vec*> live;
   // pinned host staging for small readbacks

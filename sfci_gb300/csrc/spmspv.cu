@@ -40,9 +40,11 @@ constexpr int L1_BITS = 8;                        // level-1 bins of the generat
 constexpr int PT_THREADS = 512;
 constexpr int DIGIT_MAX = 9;                      // bits per partition level
 constexpr unsigned long long UNIT_ITEMS = 1ull << 16;  // partition work unit
-constexpr int LW_WARPS = 4;                       // warps per leaf-merge CTA
-constexpr int TW_MAX = 1024;                      // hash slots per warp
-constexpr double LEAF_AVG = 512.0;                // target terms per leaf
+constexpr int LW_WARPS = 8;                       // warps per leaf-merge CTA
+constexpr int TW_MAX = 256;                       // hash slots per warp (fast tier)
+constexpr int TW_UNIQ = 48;                       // distinct keys a leaf is sized for
+constexpr int LC_THREADS = 256;                   // second tier: one CTA per leaf
+constexpr int LC_SLOTS = 4096;
 constexpr int B_MAX = 30;
 
 enum { M_COUNT = 0, M_SCATTER = 1, M_ENERGY = 2 };
@@ -538,7 +540,7 @@ __global__ void __launch_bounds__(LW_WARPS * 32) k_leafw(LeafArgs<KT> a) {
   u64 uq = 0;
   for (u64 leaf = (u64)blockIdx.x * LW_WARPS + warp; leaf < a.nleaves; leaf += (u64)gridDim.x * LW_WARPS) {
     const u64 beg = a.loff[leaf], end = a.loff[leaf + 1], n = end - beg;
-    unsigned tb = 64;
+    unsigned tb = 32;
     while (tb < (unsigned)TW_MAX && (u64)tb < 2 * n) tb <<= 1;
     const unsigned limit = (tb * 3) / 4;
     for (unsigned s = lane; s < tb; s += 32) {
@@ -604,6 +606,90 @@ __global__ void __launch_bounds__(LW_WARPS * 32) k_leafw(LeafArgs<KT> a) {
     }
     atomicAdd(a.dpart + blockIdx.x, s);  // one adder per slot and launch: the order stays fixed
     if (q) atomicAdd(a.uniq, q);
+  }
+}
+
+// Second tier: leaves whose distinct keys overflowed a warp table, one CTA per
+// leaf with a 4096-slot shared-memory table; leaves that overflow this too go
+// to the global-memory table below.
+template <class KT>
+__global__ void __launch_bounds__(LC_THREADS) k_leafc(LeafArgs<KT> a, const unsigned* __restrict__ ids, unsigned nids,
+                                                      unsigned* __restrict__ ovf2) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  KT* tk = reinterpret_cast<KT*>(smem);
+  double* ta = reinterpret_cast<double*>(smem + sizeof(KT) * LC_SLOTS);
+  __shared__ unsigned s_nuniq, s_ovf;
+  __shared__ u64 s_sum[LC_THREADS / 32 + 1];
+  __shared__ double s_red[LC_THREADS / 32];
+  __shared__ u64 s_base;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const KT empty = key_empty<KT>();
+  double dacc = 0.0;
+  u64 uq = 0;
+  for (unsigned q = blockIdx.x; q < nids; q += gridDim.x) {
+    const u64 leaf = ids[q] - a.gleaf0;
+    const u64 beg = a.loff[leaf], end = a.loff[leaf + 1];
+    for (int s = tid; s < LC_SLOTS; s += LC_THREADS) {
+      tk[s] = empty;
+      ta[s] = 0.0;
+    }
+    if (tid == 0) {
+      s_nuniq = 0;
+      s_ovf = 0;
+    }
+    __syncthreads();
+    for (u64 e = beg + tid; e < end; e += LC_THREADS) {
+      if (*(volatile unsigned*)&s_ovf) break;
+      if (!table_add(tk, ta, LC_SLOTS - 1, a.keys[e], a.amps[e], &s_nuniq, (LC_SLOTS * 3) / 4)) s_ovf = 1;
+    }
+    __syncthreads();
+    if (s_ovf) {
+      if (tid == 0) {
+        unsigned k = atomicAdd(&ovf2[0], 1u);
+        if (k < a.ovf_cap) ovf2[1 + k] = ids[q];
+      }
+      __syncthreads();
+      continue;
+    }
+    const u64 gl = ids[q];
+    for (u64 e = a.in_off[gl] + tid; e < a.in_off[gl + 1]; e += LC_THREADS) {
+      int s = table_find(tk, LC_SLOTS - 1, a.in_keys[e]);
+      if (s >= 0) dacc += ta[s] * a.in_amps[e];
+    }
+    constexpr int PER = LC_SLOTS / LC_THREADS;
+    unsigned c = 0;
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+      int s = tid * PER + k;
+      if (!key_eq(tk[s], empty) && fabs(ta[s]) > a.cut) ++c;
+    }
+    u64 tot;
+    u64 ex = block_excl_scan<u64, LC_THREADS>((u64)c, &tot, s_sum);
+    if (tid == 0) {
+      s_base = tot ? atomicAdd(a.scount, tot) : 0;
+      uq += s_nuniq;
+    }
+    __syncthreads();
+    u64 pos = s_base + ex;
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+      int s = tid * PER + k;
+      if (!key_eq(tk[s], empty) && fabs(ta[s]) > a.cut) {
+        a.skeys[pos] = tk[s];
+        a.samps[pos] = ta[s];
+        ++pos;
+      }
+    }
+    __syncthreads();
+  }
+  double v = warp_sum(dacc);
+  if (lane == 0) s_red[warp] = v;
+  __syncthreads();
+  if (tid == 0) {
+    double s = 0.0;
+    for (int w = 0; w < LC_THREADS / 32; ++w) s += s_red[w];
+    atomicAdd(a.dpart + blockIdx.x, s);
+    if (uq) atomicAdd(a.uniq, uq);
   }
 }
 
@@ -752,6 +838,8 @@ static int leaf_smem_config() {
   if (!done) {
     const int sm = (int)((sizeof(KT) + sizeof(double)) * TW_MAX * LW_WARPS);
     SFCI_CUDA(cudaFuncSetAttribute(k_leafw<KT>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    SFCI_CUDA(cudaFuncSetAttribute(k_leafc<KT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)((sizeof(KT) + sizeof(double)) * LC_SLOTS)));
     constexpr int IPT = PartIPT<W>::v;
     const int ps = (int)part_smem_bytes<KT, IPT>(M_SCATTER, 1u << DIGIT_MAX);
     SFCI_CUDA(cudaFuncSetAttribute(k_part<KT, M_SCATTER, IPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, ps));
@@ -795,7 +883,11 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
   if ((st = prep_dets<W>(c, src_k, ns, &doff, &diagE, &T))) return st;
   c.stats[1] = T;
   // hash digits: level 1 (generation) d0 bits, then nlev partition levels
-  int b = (int)std::ceil(std::log2(std::max(2.0, (double)T / LEAF_AVG)));
+  // leaves sized so a warp table holds their distinct keys: the duplication
+  // (terms per distinct key) of the previous product on this context, default 8
+  const double dup = c.dup_est > 0.0 ? c.dup_est : 8.0;
+  const double leaf_avg = std::min(4096.0, std::max(64.0, TW_UNIQ * dup));
+  int b = (int)std::ceil(std::log2(std::max(2.0, (double)T / leaf_avg)));
   b = std::max(1, std::min(b, B_MAX));
   const int d0 = std::min(b, L1_BITS);
   const int rem = b - d0;
@@ -873,9 +965,10 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
   u64* scount = (u64*)scratch_get(c, "sp_scount", 4 * sizeof(u64));  // [0] survivors, [1] distinct
   const unsigned leafgrid = (unsigned)c.sm_count * 8;
   double* dpart = (double*)scratch_get(c, "sp_dpart", (leafgrid + 1) * sizeof(double));
-  const unsigned OVF_CAP = 1u << 16;
+  const unsigned OVF_CAP = 1u << 20;
   unsigned* ovf = (unsigned*)scratch_get(c, "sp_ovf", (OVF_CAP + 1) * sizeof(unsigned));
-  if (!scount || !dpart || !ovf) return SFCI_ERR_NOMEM;
+  unsigned* ovf2 = (unsigned*)scratch_get(c, "sp_ovf2", (OVF_CAP + 1) * sizeof(unsigned));
+  if (!scount || !dpart || !ovf || !ovf2) return SFCI_ERR_NOMEM;
   SFCI_CUDA(cudaMemsetAsync(scount, 0, 4 * sizeof(u64), c.stream));
   SFCI_CUDA(cudaMemsetAsync(dpart, 0, (leafgrid + 1) * sizeof(double), c.stream));
 
@@ -1062,8 +1155,17 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
       if ((st = read_words(c, ovf, sizeof(unsigned), &novf))) return st;
       if (novf > OVF_CAP) return set_error(SFCI_ERR_NOMEM, "too many oversized SpMSpV leaves");
       if (novf) {
+        // second tier: one CTA per overflowed leaf, all in one launch
+        SFCI_CUDA(cudaMemsetAsync(ovf2, 0, sizeof(unsigned), c.stream));
+        const unsigned cg = std::min<unsigned>(novf, leafgrid);
+        SFCI_LAUNCH(c, k_leafc<KT>, cg, LC_THREADS, (sizeof(KT) + sizeof(double)) * LC_SLOTS, la,
+                    (const unsigned*)(ovf + 1), novf, ovf2);
+        if ((st = read_words(c, ovf2, sizeof(unsigned), &novf))) return st;
+        if (novf > OVF_CAP) return set_error(SFCI_ERR_NOMEM, "too many oversized SpMSpV leaves");
+      }
+      if (novf) {
         std::vector<unsigned> ids(novf);
-        if ((st = read_words(c, ovf + 1, novf * sizeof(unsigned), ids.data()))) return st;
+        if ((st = read_words(c, ovf2 + 1, novf * sizeof(unsigned), ids.data()))) return st;
         big_leaves += novf;
         for (unsigned id : ids) {
           const u64 lid = id - la.gleaf0;
@@ -1124,6 +1226,7 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
     u64 uq = 0;
     if ((st = read_words(c, scount + 1, sizeof(u64), &uq))) return st;
     c.stats[2] = uq;
+    if (uq) c.dup_est = (double)T / (double)uq;
   }
   *diag = dl + dbig_h;
   return SFCI_OK;

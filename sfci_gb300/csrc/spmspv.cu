@@ -43,6 +43,7 @@ constexpr unsigned long long UNIT_ITEMS = 1ull << 16;  // partition work unit
 constexpr int LW_WARPS = 8;                       // warps per leaf-merge CTA
 constexpr int TW_MAX = 256;                       // hash slots per warp (fast tier)
 constexpr int TW_UNIQ = 48;                       // distinct keys a leaf is sized for
+constexpr int LW_BATCH = 4;                       // leaf items per lane loaded ahead
 constexpr int LC_THREADS = 256;                   // second tier: one CTA per leaf
 constexpr int LC_SLOTS = 4096;
 constexpr int B_MAX = 30;
@@ -428,10 +429,16 @@ __global__ void __launch_bounds__(PT_THREADS, 2) k_part(PartArgs<KT> a) {
     __syncthreads();
     for (u64 rb = un.start; rb < un.end; rb += R) {
       if (MODE == M_COUNT) {
+        KT kk[IPT];
+#pragma unroll
+        for (int it = 0; it < IPT; ++it) {  // all loads first, then the atomics
+          u64 i = rb + (u64)it * PT_THREADS + tid;
+          if (i < un.end) kk[it] = a.ikeys[i];
+        }
 #pragma unroll
         for (int it = 0; it < IPT; ++it) {
           u64 i = rb + (u64)it * PT_THREADS + tid;
-          if (i < un.end) atomicAdd(&hist[(unsigned)(key_hash(a.ikeys[i]) >> a.shift) & dmask], 1u);
+          if (i < un.end) atomicAdd(&hist[(unsigned)(key_hash(kk[it]) >> a.shift) & dmask], 1u);
         }
       } else {
         KT kk[IPT];
@@ -440,10 +447,16 @@ __global__ void __launch_bounds__(PT_THREADS, 2) k_part(PartArgs<KT> a) {
 #pragma unroll
         for (int it = 0; it < IPT; ++it) {
           u64 i = rb + (u64)it * PT_THREADS + tid;
-          br[it] = ~0u;
           if (i < un.end) {
             kk[it] = a.ikeys[i];
             aa[it] = a.iamps[i];
+          }
+        }
+#pragma unroll
+        for (int it = 0; it < IPT; ++it) {
+          u64 i = rb + (u64)it * PT_THREADS + tid;
+          br[it] = ~0u;
+          if (i < un.end) {
             unsigned dg = (unsigned)(key_hash(kk[it]) >> a.shift) & dmask;
             unsigned r = atomicAdd(&hist[dg], 1u);
             br[it] = (r << 16) | dg;
@@ -526,7 +539,7 @@ struct LeafArgs {
 };
 
 template <class KT>
-__global__ void __launch_bounds__(LW_WARPS * 32) k_leafw(LeafArgs<KT> a) {
+__global__ void __launch_bounds__(LW_WARPS * 32, 4) k_leafw(LeafArgs<KT> a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   KT* tk = reinterpret_cast<KT*>(smem) + (size_t)warp * TW_MAX;
@@ -550,10 +563,23 @@ __global__ void __launch_bounds__(LW_WARPS * 32) k_leafw(LeafArgs<KT> a) {
     if (lane == 0) s_nu[warp] = 0;
     __syncwarp();
     bool ovf = false;
-    for (u64 e = beg + lane; e < end; e += 32) {
-      if (!table_add(tk, ta, tb - 1, a.keys[e], a.amps[e], &s_nu[warp], limit)) {
-        ovf = true;
-        break;
+    // batches of LW_BATCH items per lane: the loads of a batch are issued before
+    // any shared-memory atomic, so their latencies overlap
+    for (u64 e0 = beg; e0 < end && !ovf; e0 += 32 * LW_BATCH) {
+      KT kb[LW_BATCH];
+      double ab[LW_BATCH];
+#pragma unroll
+      for (int q = 0; q < LW_BATCH; ++q) {
+        const u64 e = e0 + (u64)q * 32 + lane;
+        if (e < end) {
+          kb[q] = a.keys[e];
+          ab[q] = a.amps[e];
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < LW_BATCH; ++q) {
+        const u64 e = e0 + (u64)q * 32 + lane;
+        if (e < end && !ovf && !table_add(tk, ta, tb - 1, kb[q], ab[q], &s_nu[warp], limit)) ovf = true;
       }
     }
     ovf = __any_sync(0xffffffffu, ovf);
@@ -964,6 +990,16 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
   if (!l1k || !l1a || !sk || !sa || (nlev && (!l2k || !l2a))) return SFCI_ERR_NOMEM;
   u64* scount = (u64*)scratch_get(c, "sp_scount", 4 * sizeof(u64));  // [0] survivors, [1] distinct
   const unsigned leafgrid = (unsigned)c.sm_count * 8;
+  unsigned leaf_resident = leafgrid;
+  {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_leafw<KT>, LW_WARPS * 32,
+                                                      (sizeof(KT) + sizeof(double)) * TW_MAX * LW_WARPS) ==
+            cudaSuccess &&
+        per_sm > 0)
+      leaf_resident = std::min<unsigned>(leafgrid, (unsigned)per_sm * c.sm_count);
+    cudaGetLastError();
+  }
   double* dpart = (double*)scratch_get(c, "sp_dpart", (leafgrid + 1) * sizeof(double));
   const unsigned OVF_CAP = 1u << 20;
   unsigned* ovf = (unsigned*)scratch_get(c, "sp_ovf", (OVF_CAP + 1) * sizeof(unsigned));
@@ -1149,7 +1185,7 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
       la.ovf_cap = OVF_CAP;
       la.uniq = scount + 1;
       SFCI_CUDA(cudaMemsetAsync(ovf, 0, sizeof(unsigned), c.stream));
-      const unsigned lg = (unsigned)std::min<u64>((nleaves + LW_WARPS - 1) / LW_WARPS, leafgrid);
+      const unsigned lg = (unsigned)std::min<u64>((nleaves + LW_WARPS - 1) / LW_WARPS, leaf_resident);
       SFCI_LAUNCH(c, k_leafw<KT>, lg, LW_WARPS * 32, lsm, la);
       unsigned novf = 0;
       if ((st = read_words(c, ovf, sizeof(unsigned), &novf))) return st;

@@ -134,6 +134,112 @@ SFCI_HD u64 abs_bits(double x) {
 #endif
 }
 
+// ---- exact amplitude accumulation -------------------------------------------
+// GB300 issues FP64 arithmetic at a small fraction of its integer rate, and a
+// double atomicAdd to shared memory is a compare-and-swap loop around an FP64
+// add.  The merge therefore accumulates amplitudes as 128-bit two's-complement
+// integers in units of 2^-FX_FRAC, with integer atomics only: the conversion
+// in and the sums are exact integer operations, so a merged amplitude does not
+// depend on the order in which its terms arrive, and the only rounding is the
+// final conversion back to double (round to nearest, ties to even).
+// A term's magnitude is truncated below 2^-FX_FRAC (2.1e-22) and must stay
+// below 2^FX_MAX_EXP (1.1e12); 2^15 terms of that size still fit the 2^55
+// range of a sum.
+constexpr int FX_FRAC = 72;
+constexpr int FX_MAX_EXP = 40;
+
+SFCI_HD u64 dbl_bits(double x) {
+#ifdef __CUDA_ARCH__
+  return (u64)__double_as_longlong(x);
+#else
+  u64 u; __builtin_memcpy(&u, &x, 8); return u;
+#endif
+}
+SFCI_HD double bits_dbl(u64 u) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)u);
+#else
+  double x; __builtin_memcpy(&x, &u, 8); return x;
+#endif
+}
+SFCI_HD int clz64(u64 x) {  // x != 0
+#ifdef __CUDA_ARCH__
+  return __clzll((long long)x);
+#else
+  return __builtin_clzll(x);
+#endif
+}
+
+// x * 2^FX_FRAC as a 128-bit integer (hi:lo), truncated toward zero; sets
+// *bad for |x| >= 2^FX_MAX_EXP, infinities and NaNs (and returns zero).
+SFCI_HD void fx_from_double(double x, u64& lo, u64& hi, unsigned& bad) {
+  const u64 b = dbl_bits(x);
+  const int e = (int)((b >> 52) & 0x7ff);
+  const u64 m = (b & 0xfffffffffffffull) | (1ull << 52);
+  const int s = e - (1075 - FX_FRAC);  // x * 2^FX_FRAC = m * 2^s
+  lo = 0;
+  hi = 0;
+  if (e >= 1023 + FX_MAX_EXP) {
+    bad = 1u;
+    return;
+  }
+  if (e == 0 || s <= -53) return;  // zero, subnormal or below the resolution
+  if (s < 0) {
+    lo = m >> -s;
+  } else {  // s < 64 - 11 here
+    lo = m << s;
+    hi = s ? (m >> (64 - s)) : 0ull;
+  }
+  if (b >> 63) {  // negate
+    hi = ~hi + (lo == 0 ? 1ull : 0ull);
+    lo = 0ull - lo;
+  }
+}
+
+// (hi:lo) * 2^-FX_FRAC rounded to the nearest double, ties to even
+SFCI_HD double fx_to_double(u64 lo, u64 hi) {
+  const u64 neg = hi >> 63;
+  if (neg) {
+    hi = ~hi + (lo == 0 ? 1ull : 0ull);
+    lo = 0ull - lo;
+  }
+  if ((hi | lo) == 0) return 0.0;
+  int top = hi ? 127 - clz64(hi) : 63 - clz64(lo);  // leading bit
+  u64 mant;
+  if (top <= 52) {
+    mant = lo << (52 - top);
+  } else {
+    const int sh = top - 52;  // bits dropped, 1..75
+    u64 rb, st;               // round bit, sticky bits
+    if (sh < 64) {
+      mant = (lo >> sh) | (hi << (64 - sh));
+      rb = (lo >> (sh - 1)) & 1ull;
+      st = lo & ((1ull << (sh - 1)) - 1ull);
+    } else {
+      mant = hi >> (sh - 64);
+      if (sh == 64) {
+        rb = lo >> 63;
+        st = lo & 0x7fffffffffffffffull;
+      } else {
+        rb = (hi >> (sh - 65)) & 1ull;
+        st = lo | (hi & ((1ull << (sh - 65)) - 1ull));
+      }
+    }
+    if (rb && (st || (mant & 1ull))) {
+      ++mant;
+      if (mant >> 53) {
+        mant >>= 1;
+        ++top;
+      }
+    }
+  }
+  return bits_dbl((neg << 63) | ((u64)(top - FX_FRAC + 1023) << 52) | (mant & 0xfffffffffffffull));
+}
+
+// |x| > cut for a cut given as cut_key(cut): an integer compare of the bits
+SFCI_HD long long cut_key(double cut) { return cut < 0.0 ? -1ll : (long long)abs_bits(cut); }
+SFCI_HD bool above_cut(double x, long long ck) { return (long long)abs_bits(x) > ck; }
+
 SFCI_HD int spatial_pair(int i, int j) {  // packed (i,j) ~ (j,i) index, spatial
   return i >= j ? i * (i + 1) / 2 + j : j * (j + 1) / 2 + i;
 }

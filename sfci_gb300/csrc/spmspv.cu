@@ -82,39 +82,40 @@ __device__ __forceinline__ K128 vload(const volatile K128* p) {
   return k;
 }
 
-// Insert-or-accumulate into an open-addressing table; returns false when the
-// table claimed more than `limit` distinct keys (caller falls back).
-// 64-bit keys are read with one plain load (single-copy atomic); a 128-bit key
-// is read through the CAS itself so that a concurrent claim is never seen torn.
+// Find or claim the slot of `key` in an open-addressing table; returns -1
+// once the table has claimed more than `limit` distinct keys (the caller then
+// falls back to a larger tier).  64-bit keys are read with one plain load
+// (single-copy atomic); a 128-bit key is read through the CAS itself so that a
+// concurrent claim is never seen torn.
 template <class KT>
-__device__ __forceinline__ bool table_add(KT* tk, double* ta, unsigned mask, const KT& key, double amp,
-                                          unsigned* nuniq, unsigned limit) {
+__device__ __forceinline__ int table_slot(KT* tk, unsigned mask, const KT& key, unsigned* nuniq, unsigned limit) {
   unsigned slot = (unsigned)key_hash(key) & mask;
   const KT empty = key_empty<KT>();
   for (unsigned probe = 0; probe <= mask; ++probe) {
     KT prev;
     if (sizeof(KT) == 8) {
       KT cur = vload((volatile KT*)&tk[slot]);
-      if (key_eq(cur, key)) {
-        atomicAdd(&ta[slot], amp);
-        return true;
-      }
+      if (key_eq(cur, key)) return (int)slot;
       prev = key_eq(cur, empty) ? cas_key(&tk[slot], empty, key) : cur;
     } else {
       prev = cas_key(&tk[slot], empty, key);
     }
-    if (key_eq(prev, empty)) {
-      atomicAdd(&ta[slot], amp);
-      unsigned u = atomicAdd(nuniq, 1u);
-      return u < limit;
-    }
-    if (key_eq(prev, key)) {
-      atomicAdd(&ta[slot], amp);
-      return true;
-    }
+    if (key_eq(prev, empty)) return atomicAdd(nuniq, 1u) < limit ? (int)slot : -1;
+    if (key_eq(prev, key)) return (int)slot;
     slot = (slot + 1) & mask;
   }
-  return false;
+  return -1;
+}
+
+// add a 128-bit fixed-point amplitude (hi:lo) to a slot's accumulator: the low
+// words add atomically, the carry out of them is recovered from the old value,
+// and the high word is touched only when it changes
+__device__ __forceinline__ void fx_add(u64* lo_p, u64* hi_p, u64 lo, u64 hi) {
+  if (lo) {
+    const u64 old = atomicAdd((unsigned long long*)lo_p, (unsigned long long)lo);
+    hi += (old + lo < lo) ? 1ull : 0ull;
+  }
+  if (hi) atomicAdd((unsigned long long*)hi_p, (unsigned long long)hi);
 }
 
 template <class KT>
@@ -528,7 +529,7 @@ struct LeafArgs {
   const KT* in_keys;   // input dets sorted by global leaf
   const double* in_amps;
   const uint32_t* in_off;  // [2^b + 1]
-  double cut;
+  long long cutk;      // cut_key(coeff_cut)
   KT* skeys;
   double* samps;
   u64* scount;
@@ -536,14 +537,29 @@ struct LeafArgs {
   unsigned* ovf;       // [0] = count, then leaf ids (global)
   unsigned ovf_cap;
   u64* uniq;           // merged distinct determinants (statistics)
+  unsigned* bad;       // set when a term is outside the fixed-point range
 };
 
+// Shared-memory layout of a merge table with `n` slots: keys, then the low and
+// high words of the fixed-point accumulators.
 template <class KT>
-__global__ void __launch_bounds__(LW_WARPS * 32, 4) k_leafw(LeafArgs<KT> a) {
+struct STable {
+  KT* k;
+  u64* lo;
+  u64* hi;
+  __device__ __forceinline__ STable(unsigned char* base, unsigned n)
+      : k(reinterpret_cast<KT*>(base)),
+        lo(reinterpret_cast<u64*>(base + sizeof(KT) * n)),
+        hi(reinterpret_cast<u64*>(base + (sizeof(KT) + sizeof(u64)) * n)) {}
+  __device__ __forceinline__ double amp(unsigned s) const { return fx_to_double(lo[s], hi[s]); }
+};
+constexpr size_t SLOT_BYTES_EXTRA = 2 * sizeof(u64);
+
+template <class KT>
+__global__ void __launch_bounds__(LW_WARPS * 32, sizeof(KT) == 8 ? 4 : 3) k_leafw(LeafArgs<KT> a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  KT* tk = reinterpret_cast<KT*>(smem) + (size_t)warp * TW_MAX;
-  double* ta = reinterpret_cast<double*>(smem + sizeof(KT) * TW_MAX * LW_WARPS) + (size_t)warp * TW_MAX;
+  STable<KT> t(smem + (sizeof(KT) + SLOT_BYTES_EXTRA) * TW_MAX * warp, TW_MAX);
   __shared__ unsigned s_nu[LW_WARPS];
   __shared__ double s_red[LW_WARPS];
   __shared__ u64 s_uq[LW_WARPS];
@@ -551,14 +567,16 @@ __global__ void __launch_bounds__(LW_WARPS * 32, 4) k_leafw(LeafArgs<KT> a) {
   const unsigned lt = (1u << lane) - 1u;
   double dacc = 0.0;
   u64 uq = 0;
+  unsigned bad = 0;
   for (u64 leaf = (u64)blockIdx.x * LW_WARPS + warp; leaf < a.nleaves; leaf += (u64)gridDim.x * LW_WARPS) {
     const u64 beg = a.loff[leaf], end = a.loff[leaf + 1], n = end - beg;
     unsigned tb = 32;
     while (tb < (unsigned)TW_MAX && (u64)tb < 2 * n) tb <<= 1;
     const unsigned limit = (tb * 3) / 4;
     for (unsigned s = lane; s < tb; s += 32) {
-      tk[s] = empty;
-      ta[s] = 0.0;
+      t.k[s] = empty;
+      t.lo[s] = 0;
+      t.hi[s] = 0;
     }
     if (lane == 0) s_nu[warp] = 0;
     __syncwarp();
@@ -579,7 +597,13 @@ __global__ void __launch_bounds__(LW_WARPS * 32, 4) k_leafw(LeafArgs<KT> a) {
 #pragma unroll
       for (int q = 0; q < LW_BATCH; ++q) {
         const u64 e = e0 + (u64)q * 32 + lane;
-        if (e < end && !ovf && !table_add(tk, ta, tb - 1, kb[q], ab[q], &s_nu[warp], limit)) ovf = true;
+        if (e < end && !ovf) {
+          u64 xl, xh;
+          fx_from_double(ab[q], xl, xh, bad);
+          const int s = table_slot(t.k, tb - 1, kb[q], &s_nu[warp], limit);
+          if (s < 0) ovf = true;
+          else fx_add(t.lo + s, t.hi + s, xl, xh);
+        }
       }
     }
     ovf = __any_sync(0xffffffffu, ovf);
@@ -594,14 +618,14 @@ __global__ void __launch_bounds__(LW_WARPS * 32, 4) k_leafw(LeafArgs<KT> a) {
     }
     const u64 gl = a.gleaf0 + leaf;
     for (u64 e = a.in_off[gl] + lane; e < a.in_off[gl + 1]; e += 32) {
-      int s = table_find(tk, tb - 1, a.in_keys[e]);
-      if (s >= 0) dacc += ta[s] * a.in_amps[e];
+      int s = table_find(t.k, tb - 1, a.in_keys[e]);
+      if (s >= 0) dacc += t.amp(s) * a.in_amps[e];
     }
     for (unsigned base = 0; base < tb; base += 32) {
       const unsigned s = base + lane;
-      const KT k = tk[s];
-      const double v = ta[s];
-      const bool keep = !key_eq(k, empty) && fabs(v) > a.cut;
+      const KT k = t.k[s];
+      const double v = t.amp(s);
+      const bool keep = !key_eq(k, empty) && above_cut(v, a.cutk);
       const unsigned m = __ballot_sync(0xffffffffu, keep);
       if (m) {
         u64 b0 = 0;
@@ -617,6 +641,7 @@ __global__ void __launch_bounds__(LW_WARPS * 32, 4) k_leafw(LeafArgs<KT> a) {
     if (lane == 0) uq += s_nu[warp];
     __syncwarp();
   }
+  if (bad) atomicOr(a.bad, 1u);
   double v = warp_sum(dacc);
   if (lane == 0) {
     s_red[warp] = v;
@@ -642,8 +667,7 @@ template <class KT>
 __global__ void __launch_bounds__(LC_THREADS) k_leafc(LeafArgs<KT> a, const unsigned* __restrict__ ids, unsigned nids,
                                                       unsigned* __restrict__ ovf2) {
   extern __shared__ __align__(16) unsigned char smem[];
-  KT* tk = reinterpret_cast<KT*>(smem);
-  double* ta = reinterpret_cast<double*>(smem + sizeof(KT) * LC_SLOTS);
+  STable<KT> t(smem, LC_SLOTS);
   __shared__ unsigned s_nuniq, s_ovf;
   __shared__ u64 s_sum[LC_THREADS / 32 + 1];
   __shared__ double s_red[LC_THREADS / 32];
@@ -652,12 +676,14 @@ __global__ void __launch_bounds__(LC_THREADS) k_leafc(LeafArgs<KT> a, const unsi
   const KT empty = key_empty<KT>();
   double dacc = 0.0;
   u64 uq = 0;
+  unsigned bad = 0;
   for (unsigned q = blockIdx.x; q < nids; q += gridDim.x) {
     const u64 leaf = ids[q] - a.gleaf0;
     const u64 beg = a.loff[leaf], end = a.loff[leaf + 1];
     for (int s = tid; s < LC_SLOTS; s += LC_THREADS) {
-      tk[s] = empty;
-      ta[s] = 0.0;
+      t.k[s] = empty;
+      t.lo[s] = 0;
+      t.hi[s] = 0;
     }
     if (tid == 0) {
       s_nuniq = 0;
@@ -666,7 +692,11 @@ __global__ void __launch_bounds__(LC_THREADS) k_leafc(LeafArgs<KT> a, const unsi
     __syncthreads();
     for (u64 e = beg + tid; e < end; e += LC_THREADS) {
       if (*(volatile unsigned*)&s_ovf) break;
-      if (!table_add(tk, ta, LC_SLOTS - 1, a.keys[e], a.amps[e], &s_nuniq, (LC_SLOTS * 3) / 4)) s_ovf = 1;
+      u64 xl, xh;
+      fx_from_double(a.amps[e], xl, xh, bad);
+      const int s = table_slot(t.k, LC_SLOTS - 1, a.keys[e], &s_nuniq, (LC_SLOTS * 3) / 4);
+      if (s < 0) s_ovf = 1;
+      else fx_add(t.lo + s, t.hi + s, xl, xh);
     }
     __syncthreads();
     if (s_ovf) {
@@ -679,15 +709,15 @@ __global__ void __launch_bounds__(LC_THREADS) k_leafc(LeafArgs<KT> a, const unsi
     }
     const u64 gl = ids[q];
     for (u64 e = a.in_off[gl] + tid; e < a.in_off[gl + 1]; e += LC_THREADS) {
-      int s = table_find(tk, LC_SLOTS - 1, a.in_keys[e]);
-      if (s >= 0) dacc += ta[s] * a.in_amps[e];
+      int s = table_find(t.k, LC_SLOTS - 1, a.in_keys[e]);
+      if (s >= 0) dacc += t.amp(s) * a.in_amps[e];
     }
     constexpr int PER = LC_SLOTS / LC_THREADS;
     unsigned c = 0;
 #pragma unroll
     for (int k = 0; k < PER; ++k) {
       int s = tid * PER + k;
-      if (!key_eq(tk[s], empty) && fabs(ta[s]) > a.cut) ++c;
+      if (!key_eq(t.k[s], empty) && above_cut(t.amp(s), a.cutk)) ++c;
     }
     u64 tot;
     u64 ex = block_excl_scan<u64, LC_THREADS>((u64)c, &tot, s_sum);
@@ -700,14 +730,16 @@ __global__ void __launch_bounds__(LC_THREADS) k_leafc(LeafArgs<KT> a, const unsi
 #pragma unroll
     for (int k = 0; k < PER; ++k) {
       int s = tid * PER + k;
-      if (!key_eq(tk[s], empty) && fabs(ta[s]) > a.cut) {
-        a.skeys[pos] = tk[s];
-        a.samps[pos] = ta[s];
+      const double v = t.amp(s);
+      if (!key_eq(t.k[s], empty) && above_cut(v, a.cutk)) {
+        a.skeys[pos] = t.k[s];
+        a.samps[pos] = v;
         ++pos;
       }
     }
     __syncthreads();
   }
+  if (bad) atomicOr(a.bad, 1u);
   double v = warp_sum(dacc);
   if (lane == 0) s_red[warp] = v;
   __syncthreads();
@@ -719,32 +751,38 @@ __global__ void __launch_bounds__(LC_THREADS) k_leafc(LeafArgs<KT> a, const unsi
   }
 }
 
-// oversized leaf: global-memory table
+// oversized leaf: global-memory table (keys tk, accumulators tl/th zeroed)
 template <class KT>
 __global__ void k_big_insert(const KT* __restrict__ keys, const double* __restrict__ amps, u64 beg, u64 end, KT* tk,
-                             double* ta, unsigned mask, unsigned* nuniq) {
-  for (u64 e = beg + (u64)blockIdx.x * blockDim.x + threadIdx.x; e < end; e += (u64)gridDim.x * blockDim.x)
-    table_add(tk, ta, mask, keys[e], amps[e], nuniq, 0xffffffffu);
+                             u64* tl, u64* th, unsigned mask, unsigned* nuniq, unsigned* bad) {
+  unsigned b = 0;
+  for (u64 e = beg + (u64)blockIdx.x * blockDim.x + threadIdx.x; e < end; e += (u64)gridDim.x * blockDim.x) {
+    u64 xl, xh;
+    fx_from_double(amps[e], xl, xh, b);
+    const int s = table_slot(tk, mask, keys[e], nuniq, 0xffffffffu);
+    if (s >= 0) fx_add(tl + s, th + s, xl, xh);
+  }
+  if (b) atomicOr(bad, 1u);
 }
 
 template <class KT>
-__global__ void k_big_finish(const KT* tk, const double* ta, unsigned mask, const KT* in_keys, const double* in_amps,
-                             u64 ib, u64 ie, double cut, KT* skeys, double* samps, u64* scount, double* dsum,
-                             u64* uniq) {
+__global__ void k_big_finish(const KT* tk, const u64* tl, const u64* th, unsigned mask, const KT* in_keys,
+                             const double* in_amps, u64 ib, u64 ie, long long cutk, KT* skeys, double* samps,
+                             u64* scount, double* dsum, u64* uniq) {
   const KT empty = key_empty<KT>();
   u64 gt = (u64)blockIdx.x * blockDim.x + threadIdx.x, gs = (u64)gridDim.x * blockDim.x;
   double acc = 0.0;
   for (u64 e = ib + gt; e < ie; e += gs) {
     int s = table_find_global(tk, mask, in_keys[e]);
-    if (s >= 0) acc += __ldcg(ta + s) * in_amps[e];
+    if (s >= 0) acc += fx_to_double(__ldcg(tl + s), __ldcg(th + s)) * in_amps[e];
   }
   if (acc != 0.0) atomicAdd(dsum, acc);
   for (u64 s = gt; s <= mask; s += gs) {
     KT k = ldcg_key(tk + s);
     if (key_eq(k, empty)) continue;
     atomicAdd(uniq, 1ull);
-    double v = __ldcg(ta + s);
-    if (fabs(v) > cut) {
+    const double v = fx_to_double(__ldcg(tl + s), __ldcg(th + s));
+    if (above_cut(v, cutk)) {
       u64 p = atomicAdd(scount, 1ull);
       skeys[p] = k;
       samps[p] = v;
@@ -862,10 +900,10 @@ static int leaf_smem_config() {
   typedef typename KeyOf<W>::T KT;
   static bool done = false;
   if (!done) {
-    const int sm = (int)((sizeof(KT) + sizeof(double)) * TW_MAX * LW_WARPS);
+    const int sm = (int)((sizeof(KT) + SLOT_BYTES_EXTRA) * TW_MAX * LW_WARPS);
     SFCI_CUDA(cudaFuncSetAttribute(k_leafw<KT>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     SFCI_CUDA(cudaFuncSetAttribute(k_leafc<KT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)((sizeof(KT) + sizeof(double)) * LC_SLOTS)));
+                                   (int)((sizeof(KT) + SLOT_BYTES_EXTRA) * LC_SLOTS)));
     constexpr int IPT = PartIPT<W>::v;
     const int ps = (int)part_smem_bytes<KT, IPT>(M_SCATTER, 1u << DIGIT_MAX);
     SFCI_CUDA(cudaFuncSetAttribute(k_part<KT, M_SCATTER, IPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, ps));
@@ -988,13 +1026,14 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
   KT* sk = (KT*)scratch_get(c, "sp_sk", SC * sizeof(KT));
   double* sa = (double*)scratch_get(c, "sp_sa", SC * sizeof(double));
   if (!l1k || !l1a || !sk || !sa || (nlev && (!l2k || !l2a))) return SFCI_ERR_NOMEM;
-  u64* scount = (u64*)scratch_get(c, "sp_scount", 4 * sizeof(u64));  // [0] survivors, [1] distinct
+  // [0] survivors, [1] distinct, [2] fixed-point range flag
+  u64* scount = (u64*)scratch_get(c, "sp_scount", 4 * sizeof(u64));
   const unsigned leafgrid = (unsigned)c.sm_count * 8;
   unsigned leaf_resident = leafgrid;
   {
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_leafw<KT>, LW_WARPS * 32,
-                                                      (sizeof(KT) + sizeof(double)) * TW_MAX * LW_WARPS) ==
+                                                      (sizeof(KT) + SLOT_BYTES_EXTRA) * TW_MAX * LW_WARPS) ==
             cudaSuccess &&
         per_sm > 0)
       leaf_resident = std::min<unsigned>(leafgrid, (unsigned)per_sm * c.sm_count);
@@ -1043,7 +1082,7 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
   double* dbig = (double*)scratch_get(c, "sp_dbig", sizeof(double));
   if (!dbig) return SFCI_ERR_NOMEM;
   SFCI_CUDA(cudaMemsetAsync(dbig, 0, sizeof(double), c.stream));
-  const size_t lsm = (sizeof(KT) + sizeof(double)) * TW_MAX * LW_WARPS;
+  const size_t lsm = (sizeof(KT) + SLOT_BYTES_EXTRA) * TW_MAX * LW_WARPS;
   std::vector<u64> segs, nsegs_h;
   std::vector<Unit> units;
   std::vector<u64> segbase;
@@ -1176,7 +1215,7 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
       la.in_keys = ink;
       la.in_amps = ina;
       la.in_off = inoff;
-      la.cut = cut;
+      la.cutk = cut_key(cut);
       la.skeys = sk;
       la.samps = sa;
       la.scount = scount;
@@ -1184,6 +1223,7 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
       la.ovf = ovf;
       la.ovf_cap = OVF_CAP;
       la.uniq = scount + 1;
+      la.bad = (unsigned*)(scount + 2);
       SFCI_CUDA(cudaMemsetAsync(ovf, 0, sizeof(unsigned), c.stream));
       const unsigned lg = (unsigned)std::min<u64>((nleaves + LW_WARPS - 1) / LW_WARPS, leaf_resident);
       SFCI_LAUNCH(c, k_leafw<KT>, lg, LW_WARPS * 32, lsm, la);
@@ -1194,7 +1234,7 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
         // second tier: one CTA per overflowed leaf, all in one launch
         SFCI_CUDA(cudaMemsetAsync(ovf2, 0, sizeof(unsigned), c.stream));
         const unsigned cg = std::min<unsigned>(novf, leafgrid);
-        SFCI_LAUNCH(c, k_leafc<KT>, cg, LC_THREADS, (sizeof(KT) + sizeof(double)) * LC_SLOTS, la,
+        SFCI_LAUNCH(c, k_leafc<KT>, cg, LC_THREADS, (sizeof(KT) + SLOT_BYTES_EXTRA) * LC_SLOTS, la,
                     (const unsigned*)(ovf + 1), novf, ovf2);
         if ((st = read_words(c, ovf2, sizeof(unsigned), &novf))) return st;
         if (novf > OVF_CAP) return set_error(SFCI_ERR_NOMEM, "too many oversized SpMSpV leaves");
@@ -1211,22 +1251,23 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
           u64 tsz = 1;
           while (tsz < 2 * n) tsz <<= 1;
           KT* bk = (KT*)scratch_get(c, "sp_bigk", tsz * sizeof(KT));
-          double* ba = (double*)scratch_get(c, "sp_biga", tsz * sizeof(double));
+          u64* ba = (u64*)scratch_get(c, "sp_biga", 2 * tsz * sizeof(u64));
           unsigned* bu = (unsigned*)scratch_get(c, "sp_bigu", sizeof(unsigned));
           if (!bk || !ba || !bu) return SFCI_ERR_NOMEM;
           unsigned gr = (unsigned)std::min<u64>((tsz + 255) / 256, (u64)c.sm_count * 8);
-          SFCI_LAUNCH(c, k_fill_empty<KT>, gr, 256, 0, bk, ba, tsz);
+          SFCI_LAUNCH(c, k_fill_empty<KT>, gr, 256, 0, bk, (double*)nullptr, tsz);
+          SFCI_CUDA(cudaMemsetAsync(ba, 0, 2 * tsz * sizeof(u64), c.stream));
           SFCI_CUDA(cudaMemsetAsync(bu, 0, sizeof(unsigned), c.stream));
           gr = (unsigned)std::min<u64>((n + 255) / 256, (u64)c.sm_count * 8);
           if (gr == 0) gr = 1;
           SFCI_LAUNCH(c, k_big_insert<KT>, gr, 256, 0, (const KT*)srck, (const double*)srca, beg, end, bk, ba,
-                      (unsigned)(tsz - 1), bu);
+                      ba + tsz, (unsigned)(tsz - 1), bu, la.bad);
           uint32_t ib_ie[2];
           if ((st = read_words(c, inoff + id, 2 * sizeof(uint32_t), ib_ie))) return st;
           gr = (unsigned)std::min<u64>((tsz + 255) / 256, (u64)c.sm_count * 8);
-          SFCI_LAUNCH(c, k_big_finish<KT>, gr, 256, 0, (const KT*)bk, (const double*)ba, (unsigned)(tsz - 1),
-                      (const KT*)ink, (const double*)ina, (u64)ib_ie[0], (u64)ib_ie[1], cut, sk, sa, scount, dbig,
-                      scount + 1);
+          SFCI_LAUNCH(c, k_big_finish<KT>, gr, 256, 0, (const KT*)bk, (const u64*)ba, (const u64*)(ba + tsz),
+                      (unsigned)(tsz - 1), (const KT*)ink, (const double*)ina, (u64)ib_ie[0], (u64)ib_ie[1],
+                      la.cutk, sk, sa, scount, dbig, scount + 1);
         }
       }
       if ((st = read_words(c, scount, sizeof(u64), &scount_h))) return st;
@@ -1241,7 +1282,12 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
   double dl = 0.0;
   if ((st = read_words(c, dpart + leafgrid, sizeof(double), &dl))) return st;
   if ((st = read_words(c, dbig, sizeof(double), &dbig_h))) return st;
+  u64 fxbad = 0;
+  if ((st = read_words(c, scount + 2, sizeof(u64), &fxbad))) return st;
   phase_end(c, tok);
+  if (fxbad)
+    return set_error(SFCI_ERR_NUMERIC,
+                     "SpMSpV term with |amplitude| >= 2^40 or not finite: outside the merge accumulator's range");
   c.stats[3] = scount_h;
   u64 nout = scount_h;
   if (nout > cap) {

@@ -102,3 +102,22 @@ extern "C" long gh_terms(const uint64_t* kw, uint64_t* out_k, double* out_a, lon
   }
   return n;
 }
+
+// The merge's fixed-point accumulator (common.cuh) on the host: sums n terms
+// with the same carry rule as the device's atomic add and converts back.
+extern "C" double gh_fx_sum(const double* a, long n, int* bad) {
+  u64 lo = 0, hi = 0;
+  unsigned b = 0;
+  for (long i = 0; i < n; ++i) {
+    u64 xl, xh;
+    fx_from_double(a[i], xl, xh, b);
+    const u64 old = lo;
+    lo += xl;
+    hi += xh + (lo < old ? 1ull : 0ull);
+  }
+  *bad = (int)b;
+  return fx_to_double(lo, hi);
+}
+
+// one term converted in and straight back (truncation to the 2^-72 grid)
+extern "C" double gh_fx_roundtrip(double x, int* bad) { return gh_fx_sum(&x, 1, bad); }

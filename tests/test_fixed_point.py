@@ -1,0 +1,108 @@
+"""The merge's exact fixed-point amplitude accumulator (sfci_gb300/csrc/common.cuh),
+compiled for the host, against exact rational arithmetic.
+
+The merge sums each determinant's terms as 128-bit integers in units of 2^-72
+and converts the sum back to double once.  So a merged amplitude must equal the
+correctly rounded (nearest, ties to even) value of the exact sum of the terms,
+each truncated toward zero to the 2^-72 grid, whatever the order of the terms."""
+import ctypes as C
+import math
+import os
+import subprocess
+from fractions import Fraction
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+CSRC = os.path.join(ROOT, "sfci_gb300", "csrc")
+FRAC = 72
+
+
+@pytest.fixture(scope="module")
+def fx(tmp_path_factory):
+    d = tmp_path_factory.mktemp("fx")
+    so = str(d / "gen_host.so")
+    cmd = ["g++", "-std=c++17", "-O1", "-fPIC", "-shared", "-I" + CSRC, "-I/usr/local/cuda/include",
+           os.path.join(ROOT, "tests", "native", "gen_host.cpp"), os.path.join(CSRC, "ham.cpp"), "-o", so]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    L = C.CDLL(so)
+    L.gh_fx_sum.restype = C.c_double
+    L.gh_fx_sum.argtypes = [np.ctypeslib.ndpointer(np.float64), C.c_long, C.POINTER(C.c_int)]
+    L.gh_fx_roundtrip.restype = C.c_double
+    L.gh_fx_roundtrip.argtypes = [C.c_double, C.POINTER(C.c_int)]
+    return L
+
+
+def trunc_grid(x):
+    q = Fraction(x) * (1 << FRAC)
+    return int(q) if q >= 0 else -int(-q)
+
+
+def exact(terms):
+    return float(Fraction(sum(trunc_grid(float(t)) for t in terms), 1 << FRAC))
+
+
+def fsum(L, terms):
+    bad = C.c_int(0)
+    a = np.ascontiguousarray(terms, dtype=np.float64)
+    return L.gh_fx_sum(a, len(a), C.byref(bad)), bad.value
+
+
+def test_random_sums_are_correctly_rounded(fx):
+    rng = np.random.default_rng(7)
+    for trial in range(400):
+        n = int(rng.integers(1, 40))
+        mag = np.exp2(rng.uniform(-75, 39, n))
+        terms = mag * rng.choice([-1.0, 1.0], n)
+        got, bad = fsum(fx, terms)
+        assert bad == 0
+        assert got == exact(terms), (trial, terms)
+        rng.shuffle(terms)
+        assert fsum(fx, terms)[0] == got  # order-independent
+
+
+def test_cancellation_and_sign_changes(fx):
+    rng = np.random.default_rng(8)
+    for _ in range(200):
+        x = rng.uniform(-10, 10, 8)
+        terms = np.concatenate([x, -x[::-1], [rng.uniform(-1e-9, 1e-9)]])
+        got, _ = fsum(fx, terms)
+        assert got == exact(terms)
+    assert fsum(fx, np.array([1.0, -1.0]))[0] == 0.0
+    assert fsum(fx, np.array([3.5, -1.25, -2.25]))[0] == 0.0
+
+
+def test_rounding_ties_to_even(fx):
+    # 2^53 + 1 (in units of 2^-72 * 2^k) sits halfway between two doubles
+    for k in (0, 5, 30, 58):
+        ulp = math.ldexp(1.0, k - FRAC)
+        big = math.ldexp(1.0, 53 + k - FRAC)
+        for extra, want in ((1, big), (3, big + 4 * ulp)):
+            # big + extra*ulp built from exactly representable pieces
+            got, _ = fsum(fx, np.array([big, extra * ulp]))
+            assert got == want, (k, extra)
+        got, _ = fsum(fx, np.array([-big, -ulp]))
+        assert got == -big
+
+
+def test_truncation_below_the_grid(fx):
+    bad = C.c_int(0)
+    assert fx.gh_fx_roundtrip(math.ldexp(1.0, -73), C.byref(bad)) == 0.0
+    assert fx.gh_fx_roundtrip(math.ldexp(1.0, -72), C.byref(bad)) == math.ldexp(1.0, -72)
+    assert fx.gh_fx_roundtrip(-math.ldexp(1.5, -72), C.byref(bad)) == -math.ldexp(1.0, -72)
+    for x in (1e-5, -0.3, 123.456, -7.5e11, 5e-300, 0.0, -0.0):
+        assert fx.gh_fx_roundtrip(x, C.byref(bad)) == exact([x])
+    assert bad.value == 0
+
+
+def test_range_flag(fx):
+    for x in (math.ldexp(1.0, 40), -2e12, float("inf"), float("nan")):
+        bad = C.c_int(0)
+        assert fx.gh_fx_roundtrip(x, C.byref(bad)) == 0.0
+        assert bad.value == 1
+    bad = C.c_int(0)
+    fx.gh_fx_roundtrip(math.ldexp(1.0, 40) * (1 - 2 ** -53), C.byref(bad))
+    assert bad.value == 0

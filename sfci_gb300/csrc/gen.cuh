@@ -46,7 +46,22 @@ struct DetInfo {
   float inv_nv[2], inv_nvp[2], inv_nsb;
   unsigned char occ[2][64];
   unsigned char vir[2][64];
+  // single excitations of spin s: entry ii * nv[s] + aa = occ[s][ii] | vir[s][aa] << 8
+  // (na * nv <= 32 * 32 for 64 orbitals of a spin)
+  unsigned short ia[2][1024];
 };
+
+// fill the single-excitation tables; thread k0 of `step` threads
+template <class KT>
+SFCI_HD void det_fill_singles(DetInfo<KT>& d, unsigned k0, unsigned step) {
+  for (int s = 0; s < 2; ++s) {
+    const unsigned nv = d.nv[s], n = d.na[s] * nv;
+    for (unsigned k = k0; k < n; k += step) {
+      const unsigned ii = k / nv, aa = k - ii * nv;
+      d.ia[s][k] = (unsigned short)(d.occ[s][ii] | (d.vir[s][aa] << 8));
+    }
+  }
+}
 
 SFCI_HD unsigned c2(unsigned n) { return n * (n - 1) / 2; }
 
@@ -139,6 +154,22 @@ struct Exc {
   int i, j, a, b;
 };
 
+// 31-bit packed form (orbitals < 128)
+SFCI_HD unsigned exc_pack(const Exc& e) {
+  return (unsigned)e.cls | ((unsigned)e.s << 2) | ((unsigned)e.i << 3) | ((unsigned)e.j << 10) |
+         ((unsigned)e.a << 17) | ((unsigned)e.b << 24);
+}
+SFCI_HD Exc exc_unpack(unsigned p) {
+  Exc e;
+  e.cls = (int)(p & 3u);
+  e.s = (int)((p >> 2) & 1u);
+  e.i = (int)((p >> 3) & 127u);
+  e.j = (int)((p >> 10) & 127u);
+  e.a = (int)((p >> 17) & 127u);
+  e.b = (int)((p >> 24) & 127u);
+  return e;
+}
+
 // colex pair unranking table: k = y(y-1)/2 + x, x < y < 64
 SFCI_HD void pair_of(const unsigned short* pt, unsigned k, int& x, int& y) {
   unsigned short v = pt[k];
@@ -170,12 +201,10 @@ SFCI_HD Exc decode(const DetInfo<KT>& d, const unsigned short* pt, unsigned l) {
   if (l < d.c[2]) {
     e.cls = 1;
     int s = l < d.c[1] ? 0 : 1;
-    unsigned r = l - d.c[s];
-    unsigned ii = fdiv(r, d.nv[s], d.inv_nv[s]);
-    unsigned aa = r - ii * d.nv[s];
+    const unsigned short t = d.ia[s][l - d.c[s]];
     e.s = s;
-    e.i = d.occ[s][ii];
-    e.a = d.vir[s][aa];
+    e.i = t & 0xff;
+    e.a = t >> 8;
     return e;
   }
   if (l < d.c[4]) {
@@ -196,16 +225,12 @@ SFCI_HD Exc decode(const DetInfo<KT>& d, const unsigned short* pt, unsigned l) {
   }
   e.cls = 3;
   unsigned r = l - d.c[4];
-  unsigned sa = fdiv(r, d.nsb, d.inv_nsb);
-  unsigned sb = r - sa * d.nsb;
-  unsigned ii = fdiv(sa, d.nv[0], d.inv_nv[0]);
-  unsigned aa = sa - ii * d.nv[0];
-  unsigned jj = fdiv(sb, d.nv[1], d.inv_nv[1]);
-  unsigned bb = sb - jj * d.nv[1];
-  e.i = d.occ[0][ii];
-  e.a = d.vir[0][aa];
-  e.j = d.occ[1][jj];
-  e.b = d.vir[1][bb];
+  const unsigned sa = fdiv(r, d.nsb, d.inv_nsb);
+  const unsigned short t0 = d.ia[0][sa], t1 = d.ia[1][r - sa * d.nsb];
+  e.i = t0 & 0xff;
+  e.a = t0 >> 8;
+  e.j = t1 & 0xff;
+  e.b = t1 >> 8;
   return e;
 }
 

@@ -211,7 +211,7 @@ __host__ __device__ inline size_t gen_smem_bytes(int mode, unsigned nbp) {
   if (mode != M_ENERGY) s += al16(sizeof(uint32_t) * nbp);
   if (mode == M_SCATTER)
     s += al16(sizeof(uint32_t) * nbp) + al16(sizeof(u64) * nbp) + al16(sizeof(KT) * GEN_ROUND) +
-         al16(sizeof(double) * GEN_ROUND) + al16(sizeof(unsigned short) * GEN_ROUND);
+         al16(sizeof(unsigned) * GEN_ROUND) + al16(sizeof(unsigned short) * GEN_ROUND);
   return s;
 }
 
@@ -228,7 +228,7 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
   uint32_t* bst = reinterpret_cast<uint32_t*>(smem + off);
   u64* cur = nullptr;
   KT* sk = nullptr;
-  double* sa = nullptr;
+  unsigned* se = nullptr;
   unsigned short* sb = nullptr;
   if (MODE == M_SCATTER) {
     off += al16(sizeof(uint32_t) * nbp);
@@ -236,8 +236,8 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
     off += al16(sizeof(u64) * nbp);
     sk = reinterpret_cast<KT*>(smem + off);
     off += al16(sizeof(KT) * GEN_ROUND);
-    sa = reinterpret_cast<double*>(smem + off);
-    off += al16(sizeof(double) * GEN_ROUND);
+    se = reinterpret_cast<unsigned*>(smem + off);
+    off += al16(sizeof(unsigned) * GEN_ROUND);
     sb = reinterpret_cast<unsigned short*>(smem + off);
   }
   __shared__ u64 s_det;
@@ -270,12 +270,18 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
     const u64 dbeg = g.doff[det], dend = g.doff[det + 1];
     if (tid < 32) det_setup_warp(d, g.keys[det], g.coeff * g.amps[det], g.diagE[det], g.lambda, g.h.M);
     __syncthreads();
+    det_fill_singles(d, tid, GEN_THREADS);
+    __syncthreads();
     const unsigned l0 = (unsigned)(t0 - dbeg);
     const unsigned l1 = (unsigned)((t1 < dend ? t1 : dend) - dbeg);
     for (unsigned rb = l0; rb < l1; rb += GEN_ROUND) {
       if (MODE == M_SCATTER) {
+        // (1) decode every term of the round, keep those whose bin is in this
+        // pass; (2) stage them sorted by bin as key + packed excitation; (3)
+        // compute the amplitudes of the staged terms only, with full warps, and
+        // write each bin's run contiguously
         KT kk[GEN_IPT];
-        double aa[GEN_IPT];
+        unsigned ee[GEN_IPT];
         unsigned br[GEN_IPT];  // (rank << 16) | local bin, or ~0u
 #pragma unroll
         for (int it = 0; it < GEN_IPT; ++it) {
@@ -287,7 +293,7 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
             unsigned bin = (unsigned)(key_hash(key) >> shift1);
             if (bin >= g.bin_lo && bin < g.bin_hi) {
               kk[it] = key;
-              aa[it] = term_amp(d, e, g.h);
+              ee[it] = exc_pack(e);
               unsigned lb = bin - g.bin_lo;
               unsigned r = atomicAdd(&hist[lb], 1u);
               br[it] = (r << 16) | lb;
@@ -295,7 +301,6 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
           }
         }
         __syncthreads();
-        // stage the round sorted by bin, then write each bin's run contiguously
         uint32_t tot;
         uint32_t ex = block_excl_scan<uint32_t, GEN_THREADS>(tid < (int)nbp ? hist[tid] : 0u, &tot, s_scan);
         if (tid < (int)nbp) bst[tid] = ex;
@@ -305,7 +310,7 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
           if (br[it] != ~0u) {
             unsigned lb = br[it] & 0xffffu, p = bst[lb] + (br[it] >> 16);
             sk[p] = kk[it];
-            sa[p] = aa[it];
+            se[p] = ee[it];
             sb[p] = (unsigned short)lb;
           }
         }
@@ -314,7 +319,7 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
           unsigned lb = sb[i];
           u64 pos = cur[lb] + (i - bst[lb]);
           g.okeys[pos] = sk[i];
-          g.oamps[pos] = sa[i];
+          g.oamps[pos] = term_amp(d, exc_unpack(se[i]), g.h);
         }
         __syncthreads();
         if (tid < (int)nbp) {

@@ -39,6 +39,7 @@ static void setup_host(DetInfo<KT>& d, const KT& key, int M, double cc, double D
   d.c[3] = d.c[2] + c2(d.na[0]) * d.nvp[0];
   d.c[4] = d.c[3] + c2(d.na[1]) * d.nvp[1];
   d.c[5] = d.c[4] + d.na[0] * d.nv[0] * d.nsb;
+  det_fill_singles(d, 0, 1);
 }
 
 static void pair_table(unsigned short* pt) {
@@ -80,7 +81,7 @@ extern "C" long gh_terms(const uint64_t* kw, uint64_t* out_k, double* out_a, lon
     u64 key = kw[0];
     setup_host(d, key, g_h.M, 1.0, diag_host(key, h));
     for (unsigned l = 0; l < d.c[5]; ++l, ++n) {
-      Exc e = decode(d, pt, l);
+      Exc e = exc_unpack(exc_pack(decode(d, pt, l)));  // the packed form the scatter stages
       if (n < cap) {
         out_k[n] = target_key(d, e);
         out_a[n] = term_amp(d, e, h);
@@ -91,7 +92,7 @@ extern "C" long gh_terms(const uint64_t* kw, uint64_t* out_k, double* out_a, lon
     K128 key{kw[0], kw[1]};
     setup_host(d, key, g_h.M, 1.0, diag_host(key, h));
     for (unsigned l = 0; l < d.c[5]; ++l, ++n) {
-      Exc e = decode(d, pt, l);
+      Exc e = exc_unpack(exc_pack(decode(d, pt, l)));  // the packed form the scatter stages
       if (n < cap) {
         K128 t = target_key(d, e);
         out_k[2 * n] = t.lo;

@@ -137,16 +137,22 @@ SFCI_HD u64 abs_bits(double x) {
 // ---- exact amplitude accumulation -------------------------------------------
 // GB300 issues FP64 arithmetic at a small fraction of its integer rate, and a
 // double atomicAdd to shared memory is a compare-and-swap loop around an FP64
-// add.  The merge therefore accumulates amplitudes as 128-bit two's-complement
-// integers in units of 2^-FX_FRAC, with integer atomics only: the conversion
-// in and the sums are exact integer operations, so a merged amplitude does not
-// depend on the order in which its terms arrive, and the only rounding is the
+// add.  The merge therefore sums amplitudes as integers in units of
+// 2^-FX_FRAC, with integer reductions only, so a merged amplitude does not
+// depend on the order in which its terms arrive and the only rounding is the
 // final conversion back to double (round to nearest, ties to even).
-// A term's magnitude is truncated below 2^-FX_FRAC (2.1e-22) and must stay
-// below 2^FX_MAX_EXP (1.1e12); 2^15 terms of that size still fit the 2^55
-// range of a sum.
-constexpr int FX_FRAC = 72;
-constexpr int FX_MAX_EXP = 40;
+//
+// A term x becomes F = x * 2^FX_FRAC truncated toward zero (terms below
+// 2^-FX_FRAC = 5.4e-20 vanish; |x| must stay below 2^FX_MAX_EXP), split into
+// two addends: lo = F mod 2^FX_SPLIT (unsigned) and hi = F >> FX_SPLIT
+// (signed).  An accumulator is two 64-bit words that add the lo and hi addends
+// independently, without carries between them, so each add is a plain
+// fire-and-forget reduction.  Neither word can overflow while one accumulator
+// receives at most FX_MAX_TERMS terms; the value is hi * 2^FX_SPLIT + lo.
+constexpr int FX_FRAC = 64;
+constexpr int FX_MAX_EXP = 24;
+constexpr int FX_SPLIT = 44;
+constexpr unsigned FX_MAX_TERMS = 1u << 19;  // (2^(FX_MAX_EXP+FX_FRAC-FX_SPLIT) and 2^FX_SPLIT headroom)
 
 SFCI_HD u64 dbl_bits(double x) {
 #ifdef __CUDA_ARCH__
@@ -170,13 +176,13 @@ SFCI_HD int clz64(u64 x) {  // x != 0
 #endif
 }
 
-// x * 2^FX_FRAC as a 128-bit integer (hi:lo), truncated toward zero; sets
-// *bad for |x| >= 2^FX_MAX_EXP, infinities and NaNs (and returns zero).
-SFCI_HD void fx_from_double(double x, u64& lo, u64& hi, unsigned& bad) {
+// the two addends of x; sets *bad for |x| >= 2^FX_MAX_EXP, infinities and NaNs
+// (which then add nothing)
+SFCI_HD void fx_addends(double x, u64& lo, u64& hi, unsigned& bad) {
   const u64 b = dbl_bits(x);
   const int e = (int)((b >> 52) & 0x7ff);
   const u64 m = (b & 0xfffffffffffffull) | (1ull << 52);
-  const int s = e - (1075 - FX_FRAC);  // x * 2^FX_FRAC = m * 2^s
+  const int s = e - (1075 - FX_FRAC);  // F = m * 2^s
   lo = 0;
   hi = 0;
   if (e >= 1023 + FX_MAX_EXP) {
@@ -184,19 +190,30 @@ SFCI_HD void fx_from_double(double x, u64& lo, u64& hi, unsigned& bad) {
     return;
   }
   if (e == 0 || s <= -53) return;  // zero, subnormal or below the resolution
+  u64 l, h;                        // F as a 128-bit two's-complement (h:l), |F| < 2^(FX_MAX_EXP+FX_FRAC)
   if (s < 0) {
-    lo = m >> -s;
-  } else {  // s < 64 - 11 here
-    lo = m << s;
-    hi = s ? (m >> (64 - s)) : 0ull;
+    l = m >> -s;
+    h = 0;
+  } else {
+    l = m << s;
+    h = s ? (m >> (64 - s)) : 0ull;
   }
-  if (b >> 63) {  // negate
-    hi = ~hi + (lo == 0 ? 1ull : 0ull);
-    lo = 0ull - lo;
+  if (b >> 63) {
+    h = ~h + (l == 0 ? 1ull : 0ull);
+    l = 0ull - l;
   }
+  lo = l & ((1ull << FX_SPLIT) - 1ull);
+  hi = (l >> FX_SPLIT) | (h << (64 - FX_SPLIT));  // F >> FX_SPLIT (fits 64 bits)
 }
 
-// (hi:lo) * 2^-FX_FRAC rounded to the nearest double, ties to even
+// the 128-bit sum (H:L) an accumulator holds
+SFCI_HD void fx_value(u64 acc_lo, u64 acc_hi, u64& L, u64& H) {
+  const u64 l0 = acc_hi << FX_SPLIT;
+  L = l0 + acc_lo;
+  H = (u64)((long long)acc_hi >> (64 - FX_SPLIT)) + (L < l0 ? 1ull : 0ull);
+}
+
+// (H:L) * 2^-FX_FRAC rounded to the nearest double, ties to even
 SFCI_HD double fx_to_double(u64 lo, u64 hi) {
   const u64 neg = hi >> 63;
   if (neg) {
@@ -234,6 +251,13 @@ SFCI_HD double fx_to_double(u64 lo, u64 hi) {
     }
   }
   return bits_dbl((neg << 63) | ((u64)(top - FX_FRAC + 1023) << 52) | (mant & 0xfffffffffffffull));
+}
+
+// an accumulator's value as a double
+SFCI_HD double fx_acc_double(u64 acc_lo, u64 acc_hi) {
+  u64 L, H;
+  fx_value(acc_lo, acc_hi, L, H);
+  return fx_to_double(L, H);
 }
 
 // |x| > cut for a cut given as cut_key(cut): an integer compare of the bits

@@ -36,16 +36,18 @@ namespace sfci {
 constexpr int GEN_THREADS = 512;
 constexpr int GEN_IPT = 4;
 constexpr int GEN_ROUND = GEN_THREADS * GEN_IPT;  // terms staged per round
-constexpr int L1_BITS = 8;                        // level-1 bins of the generation sweep
+constexpr int L1_BITS = 9;                        // level-1 bins of the generation sweep
 constexpr int PT_THREADS = 512;
 constexpr int DIGIT_MAX = 9;                      // bits per partition level
 constexpr unsigned long long UNIT_ITEMS = 1ull << 16;  // partition work unit
 constexpr int LW_WARPS = 8;                       // warps per leaf-merge CTA
 constexpr int TW_MAX = 256;                       // hash slots per warp (fast tier)
-constexpr int TW_UNIQ = 48;                       // distinct keys a leaf is sized for
+constexpr int TW_UNIQ = 120;                      // distinct keys a leaf is sized for (at most)
 constexpr int LW_BATCH = 4;                       // leaf items per lane loaded ahead
 constexpr int LC_THREADS = 256;                   // second tier: one CTA per leaf
 constexpr int LC_SLOTS = 4096;
+constexpr unsigned LW_PROBE = 32;                 // probes before a warp table counts as overflowed
+constexpr unsigned LC_PROBE = 128;                // same for the second tier
 constexpr int B_MAX = 30;
 
 enum { M_COUNT = 0, M_SCATTER = 1, M_ENERGY = 2 };
@@ -82,16 +84,15 @@ __device__ __forceinline__ K128 vload(const volatile K128* p) {
   return k;
 }
 
-// Find or claim the slot of `key` in an open-addressing table; returns -1
-// once the table has claimed more than `limit` distinct keys (the caller then
-// falls back to a larger tier).  64-bit keys are read with one plain load
-// (single-copy atomic); a 128-bit key is read through the CAS itself so that a
-// concurrent claim is never seen torn.
+// Find or claim the slot of `key` in an open-addressing table, probing at most
+// `max_probe` slots from `slot`; -1 when none is free within that many (the
+// table is too full for this leaf: the caller falls back to a larger tier).
+// 64-bit keys are read with one plain load (single-copy atomic); a 128-bit key
+// is read through the CAS itself so that a concurrent claim is never seen torn.
 template <class KT>
-__device__ __forceinline__ int table_slot(KT* tk, unsigned mask, const KT& key, unsigned* nuniq, unsigned limit) {
-  unsigned slot = (unsigned)key_hash(key) & mask;
+__device__ __forceinline__ int table_slot(KT* tk, unsigned mask, const KT& key, unsigned slot, unsigned max_probe) {
   const KT empty = key_empty<KT>();
-  for (unsigned probe = 0; probe <= mask; ++probe) {
+  for (unsigned probe = 0; probe < max_probe; ++probe) {
     KT prev;
     if (sizeof(KT) == 8) {
       KT cur = vload((volatile KT*)&tk[slot]);
@@ -100,27 +101,69 @@ __device__ __forceinline__ int table_slot(KT* tk, unsigned mask, const KT& key, 
     } else {
       prev = cas_key(&tk[slot], empty, key);
     }
-    if (key_eq(prev, empty)) return atomicAdd(nuniq, 1u) < limit ? (int)slot : -1;
-    if (key_eq(prev, key)) return (int)slot;
+    if (key_eq(prev, empty) || key_eq(prev, key)) return (int)slot;
     slot = (slot + 1) & mask;
   }
   return -1;
 }
 
-// add a 128-bit fixed-point amplitude (hi:lo) to a slot's accumulator: the low
-// words add atomically, the carry out of them is recovered from the old value,
-// and the high word is touched only when it changes
-__device__ __forceinline__ void fx_add(u64* lo_p, u64* hi_p, u64 lo, u64 hi) {
-  if (lo) {
-    const u64 old = atomicAdd((unsigned long long*)lo_p, (unsigned long long)lo);
-    hi += (old + lo < lo) ? 1ull : 0ull;
+// Start slot inside a leaf's warp table of 2^tbits slots: the top bits of a
+// multiplicative hash of the key.  The leaf already fixed the top bits of
+// key_hash, so the slot needs an independent function; one multiply suffices
+// at the tables' load.
+__device__ __forceinline__ unsigned leaf_slot(const u64& k, int tbits) {
+  return (unsigned)((k * 0x9e3779b97f4a7c15ull) >> (64 - tbits));
+}
+__device__ __forceinline__ unsigned leaf_slot(const K128& k, int tbits) {
+  return (unsigned)(((k.lo * 0x9e3779b97f4a7c15ull) ^ (k.hi * 0xc2b2ae3d27d4eb4full)) >> (64 - tbits));
+}
+
+// The post-merge cut |a| > cut as an integer test on the accumulated sum: sums
+// whose magnitude is at most `below` (cut * 2^FX_FRAC * (1 - 2^-40), rounded
+// down) cannot survive and are dropped without converting them; the rest are
+// converted and compared exactly.  A negative cut keeps everything.
+struct FxCut {
+  u64 below_lo, below_hi;
+  long long cutk;  // cut_key(cut)
+  int all;
+};
+__device__ __forceinline__ bool fx_survives(u64 acc_lo, u64 acc_hi, const FxCut& c, double& v) {
+  u64 lo, hi;
+  fx_value(acc_lo, acc_hi, lo, hi);
+  if (!c.all) {
+    u64 mlo = lo, mhi = hi;
+    if ((long long)hi < 0) {
+      mhi = ~hi + (lo == 0 ? 1ull : 0ull);
+      mlo = 0ull - lo;
+    }
+    if (mhi < c.below_hi || (mhi == c.below_hi && mlo <= c.below_lo)) return false;
   }
+  v = fx_to_double(lo, hi);
+  return above_cut(v, c.cutk);
+}
+static FxCut fx_cut(double cut) {
+  FxCut c{};
+  c.cutk = cut_key(cut);
+  c.all = cut < 0.0 ? 1 : 0;
+  if (!c.all) {
+    // cut * 2^FX_FRAC is exact in double; the 2^-40 margin covers the rounding
+    // of the product below and of the final conversion
+    const double y = std::ldexp(cut, FX_FRAC) * (1.0 - std::ldexp(1.0, -40));
+    const unsigned __int128 t = y >= std::ldexp(1.0, 127) ? ~(unsigned __int128)0 >> 1 : (unsigned __int128)y;
+    c.below_lo = (u64)t;
+    c.below_hi = (u64)(t >> 64);
+  }
+  return c;
+}
+
+// add a term's two addends to an accumulator (results unused: reductions)
+__device__ __forceinline__ void fx_red(u64* lo_p, u64* hi_p, u64 lo, u64 hi) {
+  if (lo) atomicAdd((unsigned long long*)lo_p, (unsigned long long)lo);
   if (hi) atomicAdd((unsigned long long*)hi_p, (unsigned long long)hi);
 }
 
 template <class KT>
-__device__ __forceinline__ int table_find(const KT* tk, unsigned mask, const KT& key) {
-  unsigned slot = (unsigned)key_hash(key) & mask;
+__device__ __forceinline__ int table_find(const KT* tk, unsigned mask, const KT& key, unsigned slot) {
   const KT empty = key_empty<KT>();
   for (unsigned probe = 0; probe <= mask; ++probe) {
     KT cur = tk[slot];
@@ -534,7 +577,7 @@ struct LeafArgs {
   const KT* in_keys;   // input dets sorted by global leaf
   const double* in_amps;
   const uint32_t* in_off;  // [2^b + 1]
-  long long cutk;      // cut_key(coeff_cut)
+  FxCut cut;           // the post-merge cut
   KT* skeys;
   double* samps;
   u64* scount;
@@ -556,7 +599,7 @@ struct STable {
       : k(reinterpret_cast<KT*>(base)),
         lo(reinterpret_cast<u64*>(base + sizeof(KT) * n)),
         hi(reinterpret_cast<u64*>(base + (sizeof(KT) + sizeof(u64)) * n)) {}
-  __device__ __forceinline__ double amp(unsigned s) const { return fx_to_double(lo[s], hi[s]); }
+  __device__ __forceinline__ double amp(unsigned s) const { return fx_acc_double(lo[s], hi[s]); }
 };
 constexpr size_t SLOT_BYTES_EXTRA = 2 * sizeof(u64);
 
@@ -565,7 +608,6 @@ __global__ void __launch_bounds__(LW_WARPS * 32, sizeof(KT) == 8 ? 4 : 3) k_leaf
   extern __shared__ __align__(16) unsigned char smem[];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   STable<KT> t(smem + (sizeof(KT) + SLOT_BYTES_EXTRA) * TW_MAX * warp, TW_MAX);
-  __shared__ unsigned s_nu[LW_WARPS];
   __shared__ double s_red[LW_WARPS];
   __shared__ u64 s_uq[LW_WARPS];
   const KT empty = key_empty<KT>();
@@ -576,14 +618,16 @@ __global__ void __launch_bounds__(LW_WARPS * 32, sizeof(KT) == 8 ? 4 : 3) k_leaf
   for (u64 leaf = (u64)blockIdx.x * LW_WARPS + warp; leaf < a.nleaves; leaf += (u64)gridDim.x * LW_WARPS) {
     const u64 beg = a.loff[leaf], end = a.loff[leaf + 1], n = end - beg;
     unsigned tb = 32;
-    while (tb < (unsigned)TW_MAX && (u64)tb < 2 * n) tb <<= 1;
-    const unsigned limit = (tb * 3) / 4;
+    int tbits = 5;
+    while (tb < (unsigned)TW_MAX && (u64)tb < 2 * n) {
+      tb <<= 1;
+      ++tbits;
+    }
     for (unsigned s = lane; s < tb; s += 32) {
       t.k[s] = empty;
       t.lo[s] = 0;
       t.hi[s] = 0;
     }
-    if (lane == 0) s_nu[warp] = 0;
     __syncwarp();
     bool ovf = false;
     // batches of LW_BATCH items per lane: the loads of a batch are issued before
@@ -604,10 +648,10 @@ __global__ void __launch_bounds__(LW_WARPS * 32, sizeof(KT) == 8 ? 4 : 3) k_leaf
         const u64 e = e0 + (u64)q * 32 + lane;
         if (e < end && !ovf) {
           u64 xl, xh;
-          fx_from_double(ab[q], xl, xh, bad);
-          const int s = table_slot(t.k, tb - 1, kb[q], &s_nu[warp], limit);
+          fx_addends(ab[q], xl, xh, bad);
+          const int s = table_slot(t.k, tb - 1, kb[q], leaf_slot(kb[q], tbits), LW_PROBE);
           if (s < 0) ovf = true;
-          else fx_add(t.lo + s, t.hi + s, xl, xh);
+          else fx_red(t.lo + s, t.hi + s, xl, xh);
         }
       }
     }
@@ -623,14 +667,17 @@ __global__ void __launch_bounds__(LW_WARPS * 32, sizeof(KT) == 8 ? 4 : 3) k_leaf
     }
     const u64 gl = a.gleaf0 + leaf;
     for (u64 e = a.in_off[gl] + lane; e < a.in_off[gl + 1]; e += 32) {
-      int s = table_find(t.k, tb - 1, a.in_keys[e]);
+      const KT k = a.in_keys[e];
+      int s = table_find(t.k, tb - 1, k, leaf_slot(k, tbits));
       if (s >= 0) dacc += t.amp(s) * a.in_amps[e];
     }
     for (unsigned base = 0; base < tb; base += 32) {
       const unsigned s = base + lane;
       const KT k = t.k[s];
-      const double v = t.amp(s);
-      const bool keep = !key_eq(k, empty) && above_cut(v, a.cutk);
+      double v = 0.0;
+      const bool used = !key_eq(k, empty);
+      const bool keep = used && fx_survives(t.lo[s], t.hi[s], a.cut, v);
+      uq += __popc(__ballot_sync(0xffffffffu, used));
       const unsigned m = __ballot_sync(0xffffffffu, keep);
       if (m) {
         u64 b0 = 0;
@@ -643,7 +690,6 @@ __global__ void __launch_bounds__(LW_WARPS * 32, sizeof(KT) == 8 ? 4 : 3) k_leaf
         }
       }
     }
-    if (lane == 0) uq += s_nu[warp];
     __syncwarp();
   }
   if (bad) atomicOr(a.bad, 1u);
@@ -673,7 +719,7 @@ __global__ void __launch_bounds__(LC_THREADS) k_leafc(LeafArgs<KT> a, const unsi
                                                       unsigned* __restrict__ ovf2) {
   extern __shared__ __align__(16) unsigned char smem[];
   STable<KT> t(smem, LC_SLOTS);
-  __shared__ unsigned s_nuniq, s_ovf;
+  __shared__ unsigned s_nuniq, s_ovf;  // s_nuniq: claimed slots, counted after the inserts
   __shared__ u64 s_sum[LC_THREADS / 32 + 1];
   __shared__ double s_red[LC_THREADS / 32];
   __shared__ u64 s_base;
@@ -698,10 +744,11 @@ __global__ void __launch_bounds__(LC_THREADS) k_leafc(LeafArgs<KT> a, const unsi
     for (u64 e = beg + tid; e < end; e += LC_THREADS) {
       if (*(volatile unsigned*)&s_ovf) break;
       u64 xl, xh;
-      fx_from_double(a.amps[e], xl, xh, bad);
-      const int s = table_slot(t.k, LC_SLOTS - 1, a.keys[e], &s_nuniq, (LC_SLOTS * 3) / 4);
+      fx_addends(a.amps[e], xl, xh, bad);
+      const KT k = a.keys[e];
+      const int s = table_slot(t.k, LC_SLOTS - 1, k, (unsigned)key_hash(k) & (LC_SLOTS - 1), LC_PROBE);
       if (s < 0) s_ovf = 1;
-      else fx_add(t.lo + s, t.hi + s, xl, xh);
+      else fx_red(t.lo + s, t.hi + s, xl, xh);
     }
     __syncthreads();
     if (s_ovf) {
@@ -714,16 +761,22 @@ __global__ void __launch_bounds__(LC_THREADS) k_leafc(LeafArgs<KT> a, const unsi
     }
     const u64 gl = ids[q];
     for (u64 e = a.in_off[gl] + tid; e < a.in_off[gl + 1]; e += LC_THREADS) {
-      int s = table_find(t.k, LC_SLOTS - 1, a.in_keys[e]);
+      const KT k = a.in_keys[e];
+      int s = table_find(t.k, LC_SLOTS - 1, k, (unsigned)key_hash(k) & (LC_SLOTS - 1));
       if (s >= 0) dacc += t.amp(s) * a.in_amps[e];
     }
     constexpr int PER = LC_SLOTS / LC_THREADS;
-    unsigned c = 0;
+    unsigned c = 0, cu = 0;
 #pragma unroll
     for (int k = 0; k < PER; ++k) {
       int s = tid * PER + k;
-      if (!key_eq(t.k[s], empty) && above_cut(t.amp(s), a.cutk)) ++c;
+      double v;
+      if (!key_eq(t.k[s], empty)) {
+        ++cu;
+        if (fx_survives(t.lo[s], t.hi[s], a.cut, v)) ++c;
+      }
     }
+    if (cu) atomicAdd(&s_nuniq, cu);  // read by thread 0 after the scan's barriers
     u64 tot;
     u64 ex = block_excl_scan<u64, LC_THREADS>((u64)c, &tot, s_sum);
     if (tid == 0) {
@@ -735,8 +788,8 @@ __global__ void __launch_bounds__(LC_THREADS) k_leafc(LeafArgs<KT> a, const unsi
 #pragma unroll
     for (int k = 0; k < PER; ++k) {
       int s = tid * PER + k;
-      const double v = t.amp(s);
-      if (!key_eq(t.k[s], empty) && above_cut(v, a.cutk)) {
+      double v = 0.0;
+      if (!key_eq(t.k[s], empty) && fx_survives(t.lo[s], t.hi[s], a.cut, v)) {
         a.skeys[pos] = t.k[s];
         a.samps[pos] = v;
         ++pos;
@@ -759,20 +812,21 @@ __global__ void __launch_bounds__(LC_THREADS) k_leafc(LeafArgs<KT> a, const unsi
 // oversized leaf: global-memory table (keys tk, accumulators tl/th zeroed)
 template <class KT>
 __global__ void k_big_insert(const KT* __restrict__ keys, const double* __restrict__ amps, u64 beg, u64 end, KT* tk,
-                             u64* tl, u64* th, unsigned mask, unsigned* nuniq, unsigned* bad) {
+                             u64* tl, u64* th, unsigned mask, unsigned* bad) {
   unsigned b = 0;
   for (u64 e = beg + (u64)blockIdx.x * blockDim.x + threadIdx.x; e < end; e += (u64)gridDim.x * blockDim.x) {
     u64 xl, xh;
-    fx_from_double(amps[e], xl, xh, b);
-    const int s = table_slot(tk, mask, keys[e], nuniq, 0xffffffffu);
-    if (s >= 0) fx_add(tl + s, th + s, xl, xh);
+    fx_addends(amps[e], xl, xh, b);
+    const KT k = keys[e];
+    const int s = table_slot(tk, mask, k, (unsigned)key_hash(k) & mask, mask + 1u);
+    if (s >= 0) fx_red(tl + s, th + s, xl, xh);
   }
   if (b) atomicOr(bad, 1u);
 }
 
 template <class KT>
 __global__ void k_big_finish(const KT* tk, const u64* tl, const u64* th, unsigned mask, const KT* in_keys,
-                             const double* in_amps, u64 ib, u64 ie, long long cutk, KT* skeys, double* samps,
+                             const double* in_amps, u64 ib, u64 ie, FxCut cut, KT* skeys, double* samps,
                              u64* scount, double* dsum, u64* uniq) {
   const KT empty = key_empty<KT>();
   u64 gt = (u64)blockIdx.x * blockDim.x + threadIdx.x, gs = (u64)gridDim.x * blockDim.x;
@@ -786,8 +840,8 @@ __global__ void k_big_finish(const KT* tk, const u64* tl, const u64* th, unsigne
     KT k = ldcg_key(tk + s);
     if (key_eq(k, empty)) continue;
     atomicAdd(uniq, 1ull);
-    const double v = fx_to_double(__ldcg(tl + s), __ldcg(th + s));
-    if (above_cut(v, cutk)) {
+    double v = 0.0;
+    if (fx_survives(__ldcg(tl + s), __ldcg(th + s), cut, v)) {
       u64 p = atomicAdd(scount, 1ull);
       skeys[p] = k;
       samps[p] = v;
@@ -946,18 +1000,33 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
     ns = m;
   }
   c.stats[0] = ns;
+  {
+    // a merged determinant receives at most one term per input determinant
+    // connected to it, i.e. at most the term count of a determinant with its
+    // spin occupations; the merge accumulators are exact up to FX_MAX_TERMS
+    u64 conn = 0;
+    for (int a0 = 0; a0 <= c.ne; ++a0) {
+      const int a1 = c.ne - a0;
+      if (a0 > c.M || a1 > c.M) continue;
+      conn = std::max<u64>(conn, det_terms(a0, c.M - a0, a1, c.M - a1));
+    }
+    if (std::min<u64>(conn, ns) > FX_MAX_TERMS)
+      return set_error(SFCI_ERR_UNSUPPORTED, "SpMSpV: determinants connect to more than 2^19 others");
+  }
   // 2. term offsets + diagonal elements
   u64 *doff = nullptr, T = 0;
   double* diagE = nullptr;
   if ((st = prep_dets<W>(c, src_k, ns, &doff, &diagE, &T))) return st;
   c.stats[1] = T;
-  // hash digits: level 1 (generation) d0 bits, then nlev partition levels
-  // leaves sized so a warp table holds their distinct keys: the duplication
-  // (terms per distinct key) of the previous product on this context, default 8
+  // hash digits: level 1 (generation) d0 bits, then nlev partition levels.
+  // 2^b leaves: the fewest (so the fewest partition levels, each a full read
+  // and write of the terms, and the best amortised per-leaf table set-up) whose
+  // expected distinct keys stay within TW_UNIQ, so that a warp table takes a
+  // leaf.  The distinct count is estimated from the duplication (terms per
+  // distinct key) of the previous product on this context (default 8).
   const double dup = c.dup_est > 0.0 ? c.dup_est : 8.0;
-  const double leaf_avg = std::min(4096.0, std::max(64.0, TW_UNIQ * dup));
-  int b = (int)std::ceil(std::log2(std::max(2.0, (double)T / leaf_avg)));
-  b = std::max(1, std::min(b, B_MAX));
+  const double uniq_est = std::max(1.0, (double)T / std::max(1.0, dup));
+  const int b = std::max(1, std::min(B_MAX, (int)std::ceil(std::log2(std::max(2.0, uniq_est / TW_UNIQ)))));
   const int d0 = std::min(b, L1_BITS);
   const int rem = b - d0;
   const int nlev = rem ? (rem + DIGIT_MAX - 1) / DIGIT_MAX : 0;
@@ -1220,7 +1289,7 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
       la.in_keys = ink;
       la.in_amps = ina;
       la.in_off = inoff;
-      la.cutk = cut_key(cut);
+      la.cut = fx_cut(cut);
       la.skeys = sk;
       la.samps = sa;
       la.scount = scount;
@@ -1257,22 +1326,20 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
           while (tsz < 2 * n) tsz <<= 1;
           KT* bk = (KT*)scratch_get(c, "sp_bigk", tsz * sizeof(KT));
           u64* ba = (u64*)scratch_get(c, "sp_biga", 2 * tsz * sizeof(u64));
-          unsigned* bu = (unsigned*)scratch_get(c, "sp_bigu", sizeof(unsigned));
-          if (!bk || !ba || !bu) return SFCI_ERR_NOMEM;
+          if (!bk || !ba) return SFCI_ERR_NOMEM;
           unsigned gr = (unsigned)std::min<u64>((tsz + 255) / 256, (u64)c.sm_count * 8);
           SFCI_LAUNCH(c, k_fill_empty<KT>, gr, 256, 0, bk, (double*)nullptr, tsz);
           SFCI_CUDA(cudaMemsetAsync(ba, 0, 2 * tsz * sizeof(u64), c.stream));
-          SFCI_CUDA(cudaMemsetAsync(bu, 0, sizeof(unsigned), c.stream));
           gr = (unsigned)std::min<u64>((n + 255) / 256, (u64)c.sm_count * 8);
           if (gr == 0) gr = 1;
           SFCI_LAUNCH(c, k_big_insert<KT>, gr, 256, 0, (const KT*)srck, (const double*)srca, beg, end, bk, ba,
-                      ba + tsz, (unsigned)(tsz - 1), bu, la.bad);
+                      ba + tsz, (unsigned)(tsz - 1), la.bad);
           uint32_t ib_ie[2];
           if ((st = read_words(c, inoff + id, 2 * sizeof(uint32_t), ib_ie))) return st;
           gr = (unsigned)std::min<u64>((tsz + 255) / 256, (u64)c.sm_count * 8);
           SFCI_LAUNCH(c, k_big_finish<KT>, gr, 256, 0, (const KT*)bk, (const u64*)ba, (const u64*)(ba + tsz),
                       (unsigned)(tsz - 1), (const KT*)ink, (const double*)ina, (u64)ib_ie[0], (u64)ib_ie[1],
-                      la.cutk, sk, sa, scount, dbig, scount + 1);
+                      la.cut, sk, sa, scount, dbig, scount + 1);
         }
       }
       if ((st = read_words(c, scount, sizeof(u64), &scount_h))) return st;
@@ -1292,7 +1359,7 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
   phase_end(c, tok);
   if (fxbad)
     return set_error(SFCI_ERR_NUMERIC,
-                     "SpMSpV term with |amplitude| >= 2^40 or not finite: outside the merge accumulator's range");
+                     "SpMSpV term with |amplitude| >= 2^24 or not finite: outside the merge accumulator's range");
   c.stats[3] = scount_h;
   u64 nout = scount_h;
   if (nout > cap) {

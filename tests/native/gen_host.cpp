@@ -104,21 +104,21 @@ extern "C" long gh_terms(const uint64_t* kw, uint64_t* out_k, double* out_a, lon
   return n;
 }
 
-// The merge's fixed-point accumulator (common.cuh) on the host: sums n terms
-// with the same carry rule as the device's atomic add and converts back.
+// The merge's split fixed-point accumulator (common.cuh) on the host: adds the
+// two addends of n terms into the two words as the device reductions do, and
+// converts the sum back.
 extern "C" double gh_fx_sum(const double* a, long n, int* bad) {
-  u64 lo = 0, hi = 0;
+  u64 acc_lo = 0, acc_hi = 0;
   unsigned b = 0;
   for (long i = 0; i < n; ++i) {
     u64 xl, xh;
-    fx_from_double(a[i], xl, xh, b);
-    const u64 old = lo;
-    lo += xl;
-    hi += xh + (lo < old ? 1ull : 0ull);
+    fx_addends(a[i], xl, xh, b);
+    acc_lo += xl;
+    acc_hi += xh;
   }
   *bad = (int)b;
-  return fx_to_double(lo, hi);
+  return fx_acc_double(acc_lo, acc_hi);
 }
 
-// one term converted in and straight back (truncation to the 2^-72 grid)
+// one term converted in and straight back (truncation to the 2^-64 grid)
 extern "C" double gh_fx_roundtrip(double x, int* bad) { return gh_fx_sum(&x, 1, bad); }

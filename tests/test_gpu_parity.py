@@ -220,3 +220,28 @@ def test_full_size_properties_configs1_shape(golden_in, port):
     rk, ra, rd = be.spmspv(keys, amps, 2000000, 0.0, 1.0)
     compare_vectors(rk, ra, k, a, cut=CUT, capped=len(ra) == 2000000)
     assert close(d, rd)
+
+
+def test_cut_levels_select_from_one_exact_merge(golden_in):
+    """The merge sums each determinant's terms exactly (fixed point) and cuts once:
+    a product at a larger coeff_cut must be exactly the entries of a product at a
+    smaller one whose |amplitude| exceeds the larger cut, with identical bits."""
+    g, path = golden_in("r28")
+    rng = np.random.default_rng(21)
+    ints, amps = _sample_vector(rng, 56, 14, 2000)
+    keys = np.array(ints, np.uint64)
+    base = None
+    for cut in (1e-12, 1e-9, 1e-5, 1e-3, 0.02):
+        c = sg.Context(path, 56, 14, Nd=200000, coeff_cut=cut)
+        vin = c.vec_from(keys, amps)
+        out = c.vec(60000000)
+        d = c.SpMVMtply_bucket(vin, out, 0.0, 1.0)
+        k, a = out.download()
+        assert np.all(np.abs(a) > cut)
+        if base is None:
+            base = (k, a, d)
+            continue
+        sel = np.abs(base[1]) > cut
+        assert np.array_equal(k, base[0][sel])
+        assert np.array_equal(a.view(np.uint64), base[1][sel].view(np.uint64))
+        assert close(d, base[2])  # <v|Hv> sums leaves in launch order: equal to rounding

@@ -235,7 +235,7 @@ def run_gpu(args, rank, ws, local, dist):
     sg.load_library()
     path = workload_in()
     nd = args.nd
-    ctx = sg.Context(path, 2 * M_SPATIAL, NUM_E, Nd=nd, hpsi_cap=HPSI_CAP)
+    ctx = sg.Context(path, 2 * M_SPATIAL, NUM_E, Nd=nd, hpsi_cap=HPSI_CAP, mem_budget=args.mem_budget)
     # input: v_{k+1} = top-Nd(H v_k) normalised, from |HF>, until it holds Nd dets
     hf = np.array([(1 << NUM_E) - 1], np.uint64)
     vin = ctx.vec(nd)
@@ -377,6 +377,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-step-s", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--mem-budget", type=int, default=0,
+                    help="device bytes the SpMSpV may use (0: 80%% of free); a small budget forces several "
+                         "generation passes on a small case, e.g. for profiling")
     args = ap.parse_args()
     rank, ws, local, dist = dist_init()
     try:

@@ -120,8 +120,22 @@ SFCI_HD u64 mix64(u64 z) {
   z ^= z >> 31;
   return z;
 }
-SFCI_HD u64 key_hash(const u64& k) { return mix64(k + 0x9e3779b97f4a7c15ull); }
-SFCI_HD u64 key_hash(const K128& k) {
+// Partition hash: a multiplication by an odd constant (per word), whose top
+// bits spread determinants over bins, digits and leaves.  It is additive under
+// excitations: setting spin orbital x adds hash_bit(x), clearing it subtracts
+// it (mod 2^64), so a target's hash is its source's hash plus one precomputed
+// delta per moved electron.  Its low bits are weak; tables index by the top
+// bits or use slot_hash.
+constexpr u64 HMUL0 = 0x9e3779b97f4a7c15ull, HMUL1 = 0xc2b2ae3d27d4eb4full;
+SFCI_HD u64 key_hash(const u64& k) { return k * HMUL0; }
+SFCI_HD u64 key_hash(const K128& k) { return k.lo * HMUL0 + k.hi * HMUL1; }
+SFCI_HD u64 hash_bit(int x) { return x < 64 ? HMUL0 << x : HMUL1 << (x - 64); }
+// change of key_hash when an electron moves from occupied i to empty a
+SFCI_HD u64 hash_move(int i, int a) { return hash_bit(a) - hash_bit(i); }
+
+// Mixing hash for tables indexed by their low bits.
+SFCI_HD u64 slot_hash(const u64& k) { return mix64(k + 0x9e3779b97f4a7c15ull); }
+SFCI_HD u64 slot_hash(const K128& k) {
   return mix64(k.lo + 0x9e3779b97f4a7c15ull) ^ mix64(k.hi ^ 0x632be59bd9b4e019ull) * 0x9e3779b97f4a7c15ull;
 }
 

@@ -46,9 +46,12 @@ struct DetInfo {
   float inv_nv[2], inv_nvp[2], inv_nsb;
   unsigned char occ[2][64];
   unsigned char vir[2][64];
-  // single excitations of spin s: entry ii * nv[s] + aa = occ[s][ii] | vir[s][aa] << 8
-  // (na * nv <= 32 * 32 for 64 orbitals of a spin)
+  u64 hd;        // key_hash(key)
+  // single excitations of spin s, entry ii * nv[s] + aa (na * nv <= 32 * 32 for
+  // 64 orbitals of a spin): the orbitals occ[s][ii] | vir[s][aa] << 8, and the
+  // change of key_hash the move causes
   unsigned short ia[2][1024];
+  u64 hs[2][1024];
 };
 
 // fill the single-excitation tables; thread k0 of `step` threads
@@ -59,6 +62,7 @@ SFCI_HD void det_fill_singles(DetInfo<KT>& d, unsigned k0, unsigned step) {
     for (unsigned k = k0; k < n; k += step) {
       const unsigned ii = k / nv, aa = k - ii * nv;
       d.ia[s][k] = (unsigned short)(d.occ[s][ii] | (d.vir[s][aa] << 8));
+      d.hs[s][k] = hash_move(d.occ[s][ii], d.vir[s][aa]);
     }
   }
 }
@@ -106,6 +110,7 @@ __device__ void det_setup_warp(DetInfo<KT>& d, const KT& key, double cc, double 
   const int lane = threadIdx.x & 31;
   if (lane == 0) {
     d.key = key;
+    d.hd = key_hash(key);
     d.cc = cc;
     d.dterm = (D - lambda) * cc;
   }
@@ -232,6 +237,31 @@ SFCI_HD Exc decode(const DetInfo<KT>& d, const unsigned short* pt, unsigned l) {
   e.j = t1 & 0xff;
   e.b = t1 >> 8;
   return e;
+}
+
+// key_hash of the target of term l, from the source's hash and the per-move
+// deltas (equals key_hash(target_key(d, decode(d, pt, l))))
+template <class KT>
+SFCI_HD u64 term_hash(const DetInfo<KT>& d, const unsigned short* pt, unsigned l) {
+  if (l == 0) return d.hd;
+  if (l < d.c[2]) {
+    const int s = l < d.c[1] ? 0 : 1;
+    return d.hd + d.hs[s][l - d.c[s]];
+  }
+  if (l < d.c[4]) {
+    const int s = l < d.c[3] ? 0 : 1;
+    const unsigned r = l - d.c[2 + s];
+    const unsigned op = fdiv(r, d.nvp[s], d.inv_nvp[s]);
+    const unsigned vp = r - op * d.nvp[s];
+    int x, y, u, v;
+    pair_of(pt, op, x, y);
+    pair_of(pt, vp, u, v);
+    const unsigned nv = d.nv[s];
+    return d.hd + d.hs[s][x * nv + u] + d.hs[s][y * nv + v];
+  }
+  const unsigned r = l - d.c[4];
+  const unsigned sa = fdiv(r, d.nsb, d.inv_nsb);
+  return d.hd + d.hs[0][sa] + d.hs[1][r - sa * d.nsb];
 }
 
 template <class KT>

@@ -108,14 +108,14 @@ __device__ __forceinline__ int table_slot(KT* tk, unsigned mask, const KT& key, 
 }
 
 // Start slot inside a leaf's warp table of 2^tbits slots: the top bits of a
-// multiplicative hash of the key.  The leaf already fixed the top bits of
-// key_hash, so the slot needs an independent function; one multiply suffices
-// at the tables' load.
+// second multiplicative hash.  The leaf already fixed the top bits of
+// key_hash, so the slot uses other multipliers; within a leaf its collisions
+// match uniform hashing.
 __device__ __forceinline__ unsigned leaf_slot(const u64& k, int tbits) {
-  return (unsigned)((k * 0x9e3779b97f4a7c15ull) >> (64 - tbits));
+  return (unsigned)((k * 0xd6e8feb86659fd93ull) >> (64 - tbits));
 }
 __device__ __forceinline__ unsigned leaf_slot(const K128& k, int tbits) {
-  return (unsigned)(((k.lo * 0x9e3779b97f4a7c15ull) ^ (k.hi * 0xc2b2ae3d27d4eb4full)) >> (64 - tbits));
+  return (unsigned)(((k.lo * 0xd6e8feb86659fd93ull) ^ (k.hi * 0x94d049bb133111ebull)) >> (64 - tbits));
 }
 
 // The post-merge cut |a| > cut as an integer test on the accumulated sum: sums
@@ -187,7 +187,7 @@ __device__ __forceinline__ K128 ldcg_key(const K128* p) {
 
 template <class KT>
 __device__ __forceinline__ int table_find_global(const KT* tk, unsigned mask, const KT& key) {
-  unsigned slot = (unsigned)key_hash(key) & mask;
+  unsigned slot = (unsigned)slot_hash(key) & mask;
   const KT empty = key_empty<KT>();
   for (unsigned probe = 0; probe <= mask; ++probe) {
     KT cur = ldcg_key(tk + slot);
@@ -331,11 +331,10 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
           unsigned l = rb + it * GEN_THREADS + tid;
           br[it] = ~0u;
           if (l < l1) {
-            Exc e = decode(d, pt, l);
-            KT key = target_key(d, e);
-            unsigned bin = (unsigned)(key_hash(key) >> shift1);
+            const unsigned bin = (unsigned)(term_hash(d, pt, l) >> shift1);
             if (bin >= g.bin_lo && bin < g.bin_hi) {
-              kk[it] = key;
+              const Exc e = decode(d, pt, l);
+              kk[it] = target_key(d, e);
               ee[it] = exc_pack(e);
               unsigned lb = bin - g.bin_lo;
               unsigned r = atomicAdd(&hist[lb], 1u);
@@ -375,11 +374,11 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
         for (int it = 0; it < GEN_IPT; ++it) {
           unsigned l = rb + it * GEN_THREADS + tid;
           if (l < l1) {
-            Exc e = decode(d, pt, l);
-            KT key = target_key(d, e);
             if (MODE == M_COUNT) {
-              atomicAdd(&hist[(unsigned)(key_hash(key) >> shift1)], 1u);
+              atomicAdd(&hist[(unsigned)(term_hash(d, pt, l) >> shift1)], 1u);
             } else {
+              const Exc e = decode(d, pt, l);
+              const KT key = target_key(d, e);
               int s = table_find_global(g.tkeys, g.tmask, key);
               if (s >= 0) eacc += term_amp(d, e, g.h) * __ldcg(g.tvals + s);
             }
@@ -746,7 +745,7 @@ __global__ void __launch_bounds__(LC_THREADS) k_leafc(LeafArgs<KT> a, const unsi
       u64 xl, xh;
       fx_addends(a.amps[e], xl, xh, bad);
       const KT k = a.keys[e];
-      const int s = table_slot(t.k, LC_SLOTS - 1, k, (unsigned)key_hash(k) & (LC_SLOTS - 1), LC_PROBE);
+      const int s = table_slot(t.k, LC_SLOTS - 1, k, (unsigned)slot_hash(k) & (LC_SLOTS - 1), LC_PROBE);
       if (s < 0) s_ovf = 1;
       else fx_red(t.lo + s, t.hi + s, xl, xh);
     }
@@ -762,7 +761,7 @@ __global__ void __launch_bounds__(LC_THREADS) k_leafc(LeafArgs<KT> a, const unsi
     const u64 gl = ids[q];
     for (u64 e = a.in_off[gl] + tid; e < a.in_off[gl + 1]; e += LC_THREADS) {
       const KT k = a.in_keys[e];
-      int s = table_find(t.k, LC_SLOTS - 1, k, (unsigned)key_hash(k) & (LC_SLOTS - 1));
+      int s = table_find(t.k, LC_SLOTS - 1, k, (unsigned)slot_hash(k) & (LC_SLOTS - 1));
       if (s >= 0) dacc += t.amp(s) * a.in_amps[e];
     }
     constexpr int PER = LC_SLOTS / LC_THREADS;
@@ -818,7 +817,7 @@ __global__ void k_big_insert(const KT* __restrict__ keys, const double* __restri
     u64 xl, xh;
     fx_addends(amps[e], xl, xh, b);
     const KT k = keys[e];
-    const int s = table_slot(tk, mask, k, (unsigned)key_hash(k) & mask, mask + 1u);
+    const int s = table_slot(tk, mask, k, (unsigned)slot_hash(k) & mask, mask + 1u);
     if (s >= 0) fx_red(tl + s, th + s, xl, xh);
   }
   if (b) atomicOr(bad, 1u);
@@ -881,7 +880,7 @@ template <class KT>
 __global__ void k_table_build(const KT* __restrict__ keys, const double* __restrict__ amps, u64 n, KT* tk, double* ta,
                               unsigned mask) {
   for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (u64)gridDim.x * blockDim.x) {
-    unsigned slot = (unsigned)key_hash(keys[i]) & mask;
+    unsigned slot = (unsigned)slot_hash(keys[i]) & mask;
     const KT empty = key_empty<KT>();
     for (;;) {
       KT prev = cas_key(&tk[slot], empty, keys[i]);

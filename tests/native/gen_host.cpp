@@ -16,6 +16,7 @@ static HamHost g_h;
 template <class KT>
 static void setup_host(DetInfo<KT>& d, const KT& key, int M, double cc, double D) {
   d.key = key;
+  d.hd = key_hash(key);
   d.cc = cc;
   d.dterm = D * cc;
   for (int s = 0; s < 2; ++s) {
@@ -122,3 +123,24 @@ extern "C" double gh_fx_sum(const double* a, long n, int* bad) {
 
 // one term converted in and straight back (truncation to the 2^-64 grid)
 extern "C" double gh_fx_roundtrip(double x, int* bad) { return gh_fx_sum(&x, 1, bad); }
+
+// Terms of one source whose incremental hash (term_hash) differs from the hash
+// of the target key; 0 when generation and partitioning agree on every bin.
+extern "C" long gh_hash_mismatches(const uint64_t* kw, int words) {
+  static unsigned short pt[2016];
+  pair_table(pt);
+  long bad = 0;
+  if (words == 1) {
+    DetInfo<u64> d;
+    setup_host(d, (u64)kw[0], g_h.M, 1.0, 0.0);
+    for (unsigned l = 0; l < d.c[5]; ++l)
+      if (term_hash(d, pt, l) != key_hash(target_key(d, decode(d, pt, l)))) ++bad;
+  } else {
+    DetInfo<K128> d;
+    K128 key{kw[0], kw[1]};
+    setup_host(d, key, g_h.M, 1.0, 0.0);
+    for (unsigned l = 0; l < d.c[5]; ++l)
+      if (term_hash(d, pt, l) != key_hash(target_key(d, decode(d, pt, l)))) ++bad;
+  }
+  return bad;
+}

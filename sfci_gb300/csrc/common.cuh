@@ -46,6 +46,12 @@ template <class KT> SFCI_HD KT key_empty();
 template <> SFCI_HD u64 key_empty<u64>() { return ~0ull; }
 template <> SFCI_HD K128 key_empty<K128>() { K128 k; k.lo = ~0ull; k.hi = ~0ull; return k; }
 
+template <class KT> SFCI_HD KT key_zero();
+template <> SFCI_HD u64 key_zero<u64>() { return 0ull; }
+template <> SFCI_HD K128 key_zero<K128>() { K128 k; k.lo = 0ull; k.hi = 0ull; return k; }
+SFCI_HD void key_xor(u64& k, const u64& m) { k ^= m; }
+SFCI_HD void key_xor(K128& k, const K128& m) { k.lo ^= m.lo; k.hi ^= m.hi; }
+
 SFCI_HD void key_flip(u64& k, int b) { k ^= (1ull << b); }
 SFCI_HD void key_flip(K128& k, int b) {
   if (b < 64) k.lo ^= (1ull << b); else k.hi ^= (1ull << (b - 64));
@@ -121,17 +127,12 @@ SFCI_HD u64 mix64(u64 z) {
   return z;
 }
 // Partition hash: a multiplication by an odd constant (per word), whose top
-// bits spread determinants over bins, digits and leaves.  It is additive under
-// excitations: setting spin orbital x adds hash_bit(x), clearing it subtracts
-// it (mod 2^64), so a target's hash is its source's hash plus one precomputed
-// delta per moved electron.  Its low bits are weak; tables index by the top
-// bits or use slot_hash.
+// bits spread determinants over bins, digits and leaves about as evenly as a
+// full mixing hash does, for one or two multiplies.  Its low bits are weak;
+// tables index by the top bits or use slot_hash.
 constexpr u64 HMUL0 = 0x9e3779b97f4a7c15ull, HMUL1 = 0xc2b2ae3d27d4eb4full;
 SFCI_HD u64 key_hash(const u64& k) { return k * HMUL0; }
 SFCI_HD u64 key_hash(const K128& k) { return k.lo * HMUL0 + k.hi * HMUL1; }
-SFCI_HD u64 hash_bit(int x) { return x < 64 ? HMUL0 << x : HMUL1 << (x - 64); }
-// change of key_hash when an electron moves from occupied i to empty a
-SFCI_HD u64 hash_move(int i, int a) { return hash_bit(a) - hash_bit(i); }
 
 // Mixing hash for tables indexed by their low bits.
 SFCI_HD u64 slot_hash(const u64& k) { return mix64(k + 0x9e3779b97f4a7c15ull); }

@@ -34,6 +34,14 @@ struct HamView {
   double ecore;
 };
 
+// Single-excitation descriptor of spin orbitals i (occupied) -> a (empty):
+// i | a << 7 | spatial_pair(i>>1, a>>1) << 14 | phase << 26, where the phase
+// bit is the parity of the occupied orbitals strictly between i and a.
+SFCI_HD unsigned sd_i(unsigned t) { return t & 127u; }
+SFCI_HD unsigned sd_a(unsigned t) { return (t >> 7) & 127u; }
+SFCI_HD unsigned sd_pair(unsigned t) { return (t >> 14) & 4095u; }
+SFCI_HD unsigned sd_par(unsigned t) { return t >> 26; }
+
 template <class KT>
 struct DetInfo {
   KT key;
@@ -43,15 +51,14 @@ struct DetInfo {
   unsigned na[2], nv[2];
   unsigned nvp[2];  // C(nv, 2)
   unsigned nsb;     // na[1] * nv[1]
-  float inv_nv[2], inv_nvp[2], inv_nsb;
+  float inv_nvp[2], inv_nsb;
   unsigned char occ[2][64];
   unsigned char vir[2][64];
-  u64 hd;        // key_hash(key)
-  // single excitations of spin s, entry ii * nv[s] + aa (na * nv <= 32 * 32 for
-  // 64 orbitals of a spin): the orbitals occ[s][ii] | vir[s][aa] << 8, and the
-  // change of key_hash the move causes
-  unsigned short ia[2][1024];
-  u64 hs[2][1024];
+  // single excitations of spin s, entry ii * nv[s] + aa (na * nv <= 32 * 32
+  // for 64 orbitals of a spin): descriptor of occ[s][ii] -> vir[s][aa] and
+  // the two key bits it flips
+  unsigned sd[2][1024];
+  KT kx[2][1024];
 };
 
 // fill the single-excitation tables; thread k0 of `step` threads
@@ -61,8 +68,13 @@ SFCI_HD void det_fill_singles(DetInfo<KT>& d, unsigned k0, unsigned step) {
     const unsigned nv = d.nv[s], n = d.na[s] * nv;
     for (unsigned k = k0; k < n; k += step) {
       const unsigned ii = k / nv, aa = k - ii * nv;
-      d.ia[s][k] = (unsigned short)(d.occ[s][ii] | (d.vir[s][aa] << 8));
-      d.hs[s][k] = hash_move(d.occ[s][ii], d.vir[s][aa]);
+      const int i = d.occ[s][ii], a = d.vir[s][aa];
+      d.sd[s][k] = (unsigned)i | ((unsigned)a << 7) | ((unsigned)spatial_pair(i >> 1, a >> 1) << 14) |
+                   ((unsigned)between_parity(d.key, i, a) << 26);
+      KT m = key_zero<KT>();
+      key_flip(m, i);
+      key_flip(m, a);
+      d.kx[s][k] = m;
     }
   }
 }
@@ -110,7 +122,6 @@ __device__ void det_setup_warp(DetInfo<KT>& d, const KT& key, double cc, double 
   const int lane = threadIdx.x & 31;
   if (lane == 0) {
     d.key = key;
-    d.hd = key_hash(key);
     d.cc = cc;
     d.dterm = (D - lambda) * cc;
   }
@@ -136,7 +147,6 @@ __device__ void det_setup_warp(DetInfo<KT>& d, const KT& key, double cc, double 
       d.na[s] = cnt_o[s];
       d.nv[s] = cnt_v[s];
       d.nvp[s] = c2(cnt_v[s]);
-      d.inv_nv[s] = cnt_v[s] ? 1.0f / (float)cnt_v[s] : 0.f;
       d.inv_nvp[s] = d.nvp[s] ? 1.0f / (float)d.nvp[s] : 0.f;
     }
     d.nsb = cnt_o[1] * cnt_v[1];
@@ -152,31 +162,18 @@ __device__ void det_setup_warp(DetInfo<KT>& d, const KT& key, double cc, double 
 
 #endif  // __CUDACC__
 
-// decoded excitation
+// decoded excitation, as indices into the determinant's single-excitation
+// tables of spin s
 struct Exc {
   int cls;  // 0 diag, 1 single, 2 same-spin double, 3 opposite-spin double
   int s;    // spin of single / same-spin double
-  int i, j, a, b;
+  // cls 1: x = single; cls 2: occupied pair x < y and empty pair u < v (list
+  // positions); cls 3: x = spin-0 single, y = spin-1 single
+  unsigned x, y, u, v;
 };
 
-// 31-bit packed form (orbitals < 128)
-SFCI_HD unsigned exc_pack(const Exc& e) {
-  return (unsigned)e.cls | ((unsigned)e.s << 2) | ((unsigned)e.i << 3) | ((unsigned)e.j << 10) |
-         ((unsigned)e.a << 17) | ((unsigned)e.b << 24);
-}
-SFCI_HD Exc exc_unpack(unsigned p) {
-  Exc e;
-  e.cls = (int)(p & 3u);
-  e.s = (int)((p >> 2) & 1u);
-  e.i = (int)((p >> 3) & 127u);
-  e.j = (int)((p >> 10) & 127u);
-  e.a = (int)((p >> 17) & 127u);
-  e.b = (int)((p >> 24) & 127u);
-  return e;
-}
-
 // colex pair unranking table: k = y(y-1)/2 + x, x < y < 64
-SFCI_HD void pair_of(const unsigned short* pt, unsigned k, int& x, int& y) {
+SFCI_HD void pair_of(const unsigned short* pt, unsigned k, unsigned& x, unsigned& y) {
   unsigned short v = pt[k];
   x = v & 0xff;
   y = v >> 8;
@@ -197,134 +194,107 @@ __device__ __forceinline__ void fill_pair_table(unsigned short* pt) {
 template <class KT>
 SFCI_HD Exc decode(const DetInfo<KT>& d, const unsigned short* pt, unsigned l) {
   Exc e;
-  e.i = e.j = e.a = e.b = 0;
   e.s = 0;
+  e.x = e.y = e.u = e.v = 0;
   if (l == 0) {
     e.cls = 0;
     return e;
   }
   if (l < d.c[2]) {
     e.cls = 1;
-    int s = l < d.c[1] ? 0 : 1;
-    const unsigned short t = d.ia[s][l - d.c[s]];
-    e.s = s;
-    e.i = t & 0xff;
-    e.a = t >> 8;
+    e.s = l < d.c[1] ? 0 : 1;
+    e.x = l - d.c[e.s];
     return e;
   }
   if (l < d.c[4]) {
     e.cls = 2;
-    int s = l < d.c[3] ? 0 : 1;
-    unsigned r = l - d.c[2 + s];
-    unsigned op = fdiv(r, d.nvp[s], d.inv_nvp[s]);
-    unsigned vp = r - op * d.nvp[s];
-    int x, y, u, v;
-    pair_of(pt, op, x, y);
-    pair_of(pt, vp, u, v);
-    e.s = s;
-    e.i = d.occ[s][x];
-    e.j = d.occ[s][y];
-    e.a = d.vir[s][u];
-    e.b = d.vir[s][v];
-    return e;
-  }
-  e.cls = 3;
-  unsigned r = l - d.c[4];
-  const unsigned sa = fdiv(r, d.nsb, d.inv_nsb);
-  const unsigned short t0 = d.ia[0][sa], t1 = d.ia[1][r - sa * d.nsb];
-  e.i = t0 & 0xff;
-  e.a = t0 >> 8;
-  e.j = t1 & 0xff;
-  e.b = t1 >> 8;
-  return e;
-}
-
-// key_hash of the target of term l, from the source's hash and the per-move
-// deltas (equals key_hash(target_key(d, decode(d, pt, l))))
-template <class KT>
-SFCI_HD u64 term_hash(const DetInfo<KT>& d, const unsigned short* pt, unsigned l) {
-  if (l == 0) return d.hd;
-  if (l < d.c[2]) {
-    const int s = l < d.c[1] ? 0 : 1;
-    return d.hd + d.hs[s][l - d.c[s]];
-  }
-  if (l < d.c[4]) {
     const int s = l < d.c[3] ? 0 : 1;
     const unsigned r = l - d.c[2 + s];
     const unsigned op = fdiv(r, d.nvp[s], d.inv_nvp[s]);
-    const unsigned vp = r - op * d.nvp[s];
-    int x, y, u, v;
-    pair_of(pt, op, x, y);
-    pair_of(pt, vp, u, v);
-    const unsigned nv = d.nv[s];
-    return d.hd + d.hs[s][x * nv + u] + d.hs[s][y * nv + v];
+    e.s = s;
+    pair_of(pt, op, e.x, e.y);
+    pair_of(pt, r - op * d.nvp[s], e.u, e.v);
+    return e;
   }
+  e.cls = 3;
   const unsigned r = l - d.c[4];
-  const unsigned sa = fdiv(r, d.nsb, d.inv_nsb);
-  return d.hd + d.hs[0][sa] + d.hs[1][r - sa * d.nsb];
+  e.x = fdiv(r, d.nsb, d.inv_nsb);
+  e.y = r - e.x * d.nsb;
+  return e;
 }
 
 template <class KT>
 SFCI_HD KT target_key(const DetInfo<KT>& d, const Exc& e) {
   KT k = d.key;
-  if (e.cls == 0) return k;
-  key_flip(k, e.i);
-  key_flip(k, e.a);
-  if (e.cls >= 2) {
-    key_flip(k, e.j);
-    key_flip(k, e.b);
+  if (e.cls == 1) {
+    key_xor(k, d.kx[e.s][e.x]);
+  } else if (e.cls == 2) {
+    const unsigned nv = d.nv[e.s];
+    key_xor(k, d.kx[e.s][e.x * nv + e.u]);
+    key_xor(k, d.kx[e.s][e.y * nv + e.v]);
+  } else if (e.cls == 3) {
+    key_xor(k, d.kx[0][e.x]);
+    key_xor(k, d.kx[1][e.y]);
   }
   return k;
 }
 
-SFCI_HD double vget(const HamView& h, int blk, int m, int n, int p, int q) {
-  int pa = spatial_pair(m >> 1, n >> 1), pb = spatial_pair(p >> 1, q >> 1);
+// V[blk][pa][pb]
+SFCI_HD double vat(const HamView& h, int blk, unsigned pa, unsigned pb) {
   return SFCI_LDG(h.V + ((size_t)blk * h.P + pa) * h.P + pb);
 }
+SFCI_HD double vget(const HamView& h, int blk, int m, int n, int p, int q) {
+  return vat(h, blk, (unsigned)spatial_pair(m >> 1, n >> 1), (unsigned)spatial_pair(p >> 1, q >> 1));
+}
+SFCI_HD double signed_by(unsigned par, double x) { return par ? -x : x; }
 
 // Matrix element <target|H|source> times cc (diagonal: (D - lambda) * cc).
+// Phases follow signCal_bit: for the move pair (i->a, j->b) the parity of the
+// occupied orbitals strictly between each pair's ends, corrected where one
+// move's ends fall between the other's (the second move acts on the string the
+// first one left).
 template <class KT>
 SFCI_HD double term_amp(const DetInfo<KT>& d, const Exc& e, const HamView& h) {
-  const KT& D = d.key;
   if (e.cls == 0) return d.dterm;
   if (e.cls == 1) {
     // one-body h(a,i) + sum_k (ai|kk) - sum_{k same spin} (ak|ki), src/bitstr.cpp:230-262,269-300
-    const int s = e.s, a = e.a, i = e.i;
+    const int s = e.s;
+    const unsigned t = d.sd[s][e.x];
+    const int i = (int)sd_i(t), a = (int)sd_a(t);
     double v = SFCI_LDG(h.h1 + ((size_t)s * h.M + (a >> 1)) * h.M + (i >> 1));
-    const int pai = spatial_pair(a >> 1, i >> 1);
-    for (int t = 0; t < 2; ++t) {
-      const double* row = h.V + ((size_t)(2 * s + t) * h.P + pai) * h.P;
-      for (unsigned kk = 0; kk < d.na[t]; ++kk) {
-        int k = d.occ[t][kk];
+    const unsigned pai = sd_pair(t);
+    for (int u = 0; u < 2; ++u) {
+      const double* row = h.V + ((size_t)(2 * s + u) * h.P + pai) * h.P;
+      for (unsigned kk = 0; kk < d.na[u]; ++kk) {
+        int k = d.occ[u][kk];
         if (k == i) continue;
         int kp = k >> 1;
         v += SFCI_LDG(row + kp * (kp + 1) / 2 + kp);
-        if (t == s) v -= vget(h, 3 * s, a, k, k, i);
+        if (u == s) v -= vget(h, 3 * s, a, k, k, i);
       }
     }
-    return between_parity(D, a, i) ? -d.cc * v : d.cc * v;
+    return signed_by(sd_par(t), d.cc * v);
   }
   if (e.cls == 2) {
     // entries (a,i,b,j) and (b,i,a,j) of pair (i<j); the second has the opposite phase
-    const int i = e.i, j = e.j, a = e.a, b = e.b;
-    double v1 = vget(h, 3 * e.s, a, i, b, j);
-    double v2 = vget(h, 3 * e.s, b, i, a, j);
-    int par = between_parity2(D, b, j, a, i) ^ (int)strictly_between(j, a, i) ^ (int)strictly_between(b, a, i);
-    double v = v1 - v2;
-    return par ? -d.cc * v : d.cc * v;
+    const unsigned nv = d.nv[e.s];
+    const unsigned* sd = d.sd[e.s];
+    const unsigned t1 = sd[e.x * nv + e.u], t2 = sd[e.y * nv + e.v];  // i->a, j->b
+    const unsigned t3 = sd[e.x * nv + e.v], t4 = sd[e.y * nv + e.u];  // i->b, j->a
+    const int i = (int)sd_i(t1), a = (int)sd_a(t1), j = (int)sd_i(t2), b = (int)sd_a(t2);
+    const double v = vat(h, 3 * e.s, sd_pair(t1), sd_pair(t2)) - vat(h, 3 * e.s, sd_pair(t3), sd_pair(t4));
+    const unsigned par =
+        sd_par(t1) ^ sd_par(t2) ^ (unsigned)strictly_between(j, a, i) ^ (unsigned)strictly_between(b, a, i);
+    return signed_by(par, d.cc * v);
   }
   // opposite spin: the single entry of pair (min(i,j), max(i,j))
-  const int i = e.i, j = e.j, a = e.a, b = e.b;
-  double v;
-  int par;
-  if (i < j) {
-    v = vget(h, 1, a, i, b, j);
-    par = between_parity2(D, b, j, a, i) ^ (int)strictly_between(j, a, i) ^ (int)strictly_between(b, a, i);
-  } else {
-    v = vget(h, 2, b, j, a, i);
-    par = between_parity2(D, a, i, b, j) ^ (int)strictly_between(i, b, j) ^ (int)strictly_between(a, b, j);
-  }
-  return par ? -d.cc * v : d.cc * v;
+  const unsigned t0 = d.sd[0][e.x], t1 = d.sd[1][e.y];  // i->a (spin 0), j->b (spin 1)
+  const int i = (int)sd_i(t0), a = (int)sd_a(t0), j = (int)sd_i(t1), b = (int)sd_a(t1);
+  const bool ij = i < j;
+  const double v = ij ? vat(h, 1, sd_pair(t0), sd_pair(t1)) : vat(h, 2, sd_pair(t1), sd_pair(t0));
+  const unsigned cross = ij ? ((unsigned)strictly_between(j, a, i) ^ (unsigned)strictly_between(b, a, i))
+                            : ((unsigned)strictly_between(i, b, j) ^ (unsigned)strictly_between(a, b, j));
+  return signed_by(sd_par(t0) ^ sd_par(t1) ^ cross, d.cc * v);
 }
 
 #ifdef __CUDACC__

@@ -34,7 +34,7 @@
 namespace sfci {
 
 constexpr int GEN_THREADS = 512;
-constexpr int GEN_IPT = 4;
+constexpr int GEN_IPT = 8;
 constexpr int GEN_ROUND = GEN_THREADS * GEN_IPT;  // terms staged per round
 constexpr int L1_BITS = 9;                        // level-1 bins of the generation sweep
 constexpr int PT_THREADS = 512;
@@ -253,8 +253,7 @@ __host__ __device__ inline size_t gen_smem_bytes(int mode, unsigned nbp) {
   size_t s = al16(sizeof(DetInfo<KT>)) + al16(2016 * sizeof(unsigned short));
   if (mode != M_ENERGY) s += al16(sizeof(uint32_t) * nbp);
   if (mode == M_SCATTER)
-    s += al16(sizeof(uint32_t) * nbp) + al16(sizeof(u64) * nbp) + al16(sizeof(KT) * GEN_ROUND) +
-         al16(sizeof(unsigned) * GEN_ROUND) + al16(sizeof(unsigned short) * GEN_ROUND);
+    s += al16(sizeof(uint32_t) * nbp) + al16(sizeof(u64) * nbp) + 2 * al16(sizeof(unsigned short) * GEN_ROUND);
   return s;
 }
 
@@ -270,17 +269,14 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
   off += al16(sizeof(uint32_t) * (MODE == M_ENERGY ? 0 : nbp));
   uint32_t* bst = reinterpret_cast<uint32_t*>(smem + off);
   u64* cur = nullptr;
-  KT* sk = nullptr;
-  unsigned* se = nullptr;
-  unsigned short* sb = nullptr;
+  unsigned short* sx = nullptr;  // staged: term index within the round
+  unsigned short* sb = nullptr;  // staged: local bin
   if (MODE == M_SCATTER) {
     off += al16(sizeof(uint32_t) * nbp);
     cur = reinterpret_cast<u64*>(smem + off);
     off += al16(sizeof(u64) * nbp);
-    sk = reinterpret_cast<KT*>(smem + off);
-    off += al16(sizeof(KT) * GEN_ROUND);
-    se = reinterpret_cast<unsigned*>(smem + off);
-    off += al16(sizeof(unsigned) * GEN_ROUND);
+    sx = reinterpret_cast<unsigned short*>(smem + off);
+    off += al16(sizeof(unsigned short) * GEN_ROUND);
     sb = reinterpret_cast<unsigned short*>(smem + off);
   }
   __shared__ u64 s_det;
@@ -319,23 +315,18 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
     const unsigned l1 = (unsigned)((t1 < dend ? t1 : dend) - dbeg);
     for (unsigned rb = l0; rb < l1; rb += GEN_ROUND) {
       if (MODE == M_SCATTER) {
-        // (1) decode every term of the round, keep those whose bin is in this
-        // pass; (2) stage them sorted by bin as key + packed excitation; (3)
-        // compute the amplitudes of the staged terms only, with full warps, and
-        // write each bin's run contiguously
-        KT kk[GEN_IPT];
-        unsigned ee[GEN_IPT];
+        // (1) bin every term of the round by its hash alone and rank the ones
+        // in this pass; (2) stage their round indices sorted by bin; (3) decode,
+        // build the keys and amplitudes of the staged terms only, with full
+        // warps, and write each bin's run contiguously
         unsigned br[GEN_IPT];  // (rank << 16) | local bin, or ~0u
 #pragma unroll
         for (int it = 0; it < GEN_IPT; ++it) {
           unsigned l = rb + it * GEN_THREADS + tid;
           br[it] = ~0u;
           if (l < l1) {
-            const unsigned bin = (unsigned)(term_hash(d, pt, l) >> shift1);
+            const unsigned bin = (unsigned)(key_hash(target_key(d, decode(d, pt, l))) >> shift1);
             if (bin >= g.bin_lo && bin < g.bin_hi) {
-              const Exc e = decode(d, pt, l);
-              kk[it] = target_key(d, e);
-              ee[it] = exc_pack(e);
               unsigned lb = bin - g.bin_lo;
               unsigned r = atomicAdd(&hist[lb], 1u);
               br[it] = (r << 16) | lb;
@@ -351,17 +342,17 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
         for (int it = 0; it < GEN_IPT; ++it) {
           if (br[it] != ~0u) {
             unsigned lb = br[it] & 0xffffu, p = bst[lb] + (br[it] >> 16);
-            sk[p] = kk[it];
-            se[p] = ee[it];
+            sx[p] = (unsigned short)(it * GEN_THREADS + tid);
             sb[p] = (unsigned short)lb;
           }
         }
         __syncthreads();
         for (unsigned i = tid; i < tot; i += GEN_THREADS) {
-          unsigned lb = sb[i];
-          u64 pos = cur[lb] + (i - bst[lb]);
-          g.okeys[pos] = sk[i];
-          g.oamps[pos] = term_amp(d, exc_unpack(se[i]), g.h);
+          const unsigned lb = sb[i];
+          const u64 pos = cur[lb] + (i - bst[lb]);
+          const Exc e = decode(d, pt, rb + sx[i]);
+          g.okeys[pos] = target_key(d, e);
+          g.oamps[pos] = term_amp(d, e, g.h);
         }
         __syncthreads();
         if (tid < (int)nbp) {
@@ -375,7 +366,7 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
           unsigned l = rb + it * GEN_THREADS + tid;
           if (l < l1) {
             if (MODE == M_COUNT) {
-              atomicAdd(&hist[(unsigned)(term_hash(d, pt, l) >> shift1)], 1u);
+              atomicAdd(&hist[(unsigned)(key_hash(target_key(d, decode(d, pt, l))) >> shift1)], 1u);
             } else {
               const Exc e = decode(d, pt, l);
               const KT key = target_key(d, e);

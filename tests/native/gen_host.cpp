@@ -16,7 +16,6 @@ static HamHost g_h;
 template <class KT>
 static void setup_host(DetInfo<KT>& d, const KT& key, int M, double cc, double D) {
   d.key = key;
-  d.hd = key_hash(key);
   d.cc = cc;
   d.dterm = D * cc;
   for (int s = 0; s < 2; ++s) {
@@ -29,7 +28,6 @@ static void setup_host(DetInfo<KT>& d, const KT& key, int M, double cc, double D
     d.na[s] = no;
     d.nv[s] = nv;
     d.nvp[s] = c2(nv);
-    d.inv_nv[s] = nv ? 1.0f / (float)nv : 0.f;
     d.inv_nvp[s] = d.nvp[s] ? 1.0f / (float)d.nvp[s] : 0.f;
   }
   d.nsb = d.na[1] * d.nv[1];
@@ -82,7 +80,7 @@ extern "C" long gh_terms(const uint64_t* kw, uint64_t* out_k, double* out_a, lon
     u64 key = kw[0];
     setup_host(d, key, g_h.M, 1.0, diag_host(key, h));
     for (unsigned l = 0; l < d.c[5]; ++l, ++n) {
-      Exc e = exc_unpack(exc_pack(decode(d, pt, l)));  // the packed form the scatter stages
+      Exc e = decode(d, pt, l);
       if (n < cap) {
         out_k[n] = target_key(d, e);
         out_a[n] = term_amp(d, e, h);
@@ -93,7 +91,7 @@ extern "C" long gh_terms(const uint64_t* kw, uint64_t* out_k, double* out_a, lon
     K128 key{kw[0], kw[1]};
     setup_host(d, key, g_h.M, 1.0, diag_host(key, h));
     for (unsigned l = 0; l < d.c[5]; ++l, ++n) {
-      Exc e = exc_unpack(exc_pack(decode(d, pt, l)));  // the packed form the scatter stages
+      Exc e = decode(d, pt, l);
       if (n < cap) {
         K128 t = target_key(d, e);
         out_k[2 * n] = t.lo;
@@ -123,24 +121,3 @@ extern "C" double gh_fx_sum(const double* a, long n, int* bad) {
 
 // one term converted in and straight back (truncation to the 2^-64 grid)
 extern "C" double gh_fx_roundtrip(double x, int* bad) { return gh_fx_sum(&x, 1, bad); }
-
-// Terms of one source whose incremental hash (term_hash) differs from the hash
-// of the target key; 0 when generation and partitioning agree on every bin.
-extern "C" long gh_hash_mismatches(const uint64_t* kw, int words) {
-  static unsigned short pt[2016];
-  pair_table(pt);
-  long bad = 0;
-  if (words == 1) {
-    DetInfo<u64> d;
-    setup_host(d, (u64)kw[0], g_h.M, 1.0, 0.0);
-    for (unsigned l = 0; l < d.c[5]; ++l)
-      if (term_hash(d, pt, l) != key_hash(target_key(d, decode(d, pt, l)))) ++bad;
-  } else {
-    DetInfo<K128> d;
-    K128 key{kw[0], kw[1]};
-    setup_host(d, key, g_h.M, 1.0, 0.0);
-    for (unsigned l = 0; l < d.c[5]; ++l)
-      if (term_hash(d, pt, l) != key_hash(target_key(d, decode(d, pt, l)))) ++bad;
-  }
-  return bad;
-}

@@ -56,34 +56,3 @@ def test_decoder_matches_reference(gh, golden_in, name):
         assert np.array_equal(ko, rk), "connected set differs"
         scale = np.max(np.abs(ra))
         assert np.max(np.abs(ao - ra)) <= 1e-13 * scale + 1e-15
-
-
-@pytest.mark.parametrize("name", SYSTEMS)
-def test_term_hash_matches_key_hash(gh, golden_in, name):
-    """Generation bins each term by a hash built from the source's hash and
-    per-move deltas; it must equal the hash the partition levels recompute
-    from the target key, for every term."""
-    g, path = golden_in(name)
-    N = 2 * int(g["M"])
-    assert gh.gh_load(path.encode(), N) == 0
-    gh.gh_hash_mismatches.restype = C.c_long
-    gh.gh_hash_mismatches.argtypes = [np.ctypeslib.ndpointer(np.uint64), C.c_int]
-    for t in range(3):
-        det = np.array([g["off%d_det" % t]], np.uint64)
-        assert gh.gh_hash_mismatches(det, 1) == 0
-
-
-def test_term_hash_two_word_keys(gh, tmp_path):
-    from sfci_gb300 import fcidump as fd
-    M, ne = 40, 10
-    p = str(tmp_path / "h_IN")
-    fd.rhf_to_in_file(p, M, ne, 3)
-    assert gh.gh_load(p.encode(), 2 * M) == 0
-    gh.gh_hash_mismatches.restype = C.c_long
-    gh.gh_hash_mismatches.argtypes = [np.ctypeslib.ndpointer(np.uint64), C.c_int]
-    rng = np.random.default_rng(4)
-    for _ in range(3):
-        occ = rng.choice(2 * M, ne, replace=False)
-        lo = sum(1 << int(b) for b in occ if b < 64)
-        hi = sum(1 << int(b - 64) for b in occ if b >= 64)
-        assert gh.gh_hash_mismatches(np.array([lo, hi], np.uint64), 2) == 0

@@ -42,8 +42,9 @@ SFCI_HD unsigned sd_a(unsigned t) { return (t >> 7) & 127u; }
 SFCI_HD unsigned sd_pair(unsigned t) { return (t >> 14) & 4095u; }
 SFCI_HD unsigned sd_par(unsigned t) { return t >> 26; }
 
+// per-determinant scalars (kernels copy them to registers once per determinant)
 template <class KT>
-struct DetInfo {
+struct DetHead {
   KT key;
   double cc;     // coeff * amp
   double dterm;  // (D - lambda) * cc
@@ -52,6 +53,11 @@ struct DetInfo {
   unsigned nvp[2];  // C(nv, 2)
   unsigned nsb;     // na[1] * nv[1]
   float inv_nvp[2], inv_nsb;
+};
+
+template <class KT>
+struct DetInfo {
+  DetHead<KT> h;
   unsigned char occ[2][64];
   unsigned char vir[2][64];
   // single excitations of spin s, entry ii * nv[s] + aa (na * nv <= 32 * 32
@@ -65,12 +71,12 @@ struct DetInfo {
 template <class KT>
 SFCI_HD void det_fill_singles(DetInfo<KT>& d, unsigned k0, unsigned step) {
   for (int s = 0; s < 2; ++s) {
-    const unsigned nv = d.nv[s], n = d.na[s] * nv;
+    const unsigned nv = d.h.nv[s], n = d.h.na[s] * nv;
     for (unsigned k = k0; k < n; k += step) {
       const unsigned ii = k / nv, aa = k - ii * nv;
       const int i = d.occ[s][ii], a = d.vir[s][aa];
       d.sd[s][k] = (unsigned)i | ((unsigned)a << 7) | ((unsigned)spatial_pair(i >> 1, a >> 1) << 14) |
-                   ((unsigned)between_parity(d.key, i, a) << 26);
+                   ((unsigned)between_parity(d.h.key, i, a) << 26);
       KT m = key_zero<KT>();
       key_flip(m, i);
       key_flip(m, a);
@@ -121,9 +127,9 @@ template <class KT>
 __device__ void det_setup_warp(DetInfo<KT>& d, const KT& key, double cc, double D, double lambda, int M) {
   const int lane = threadIdx.x & 31;
   if (lane == 0) {
-    d.key = key;
-    d.cc = cc;
-    d.dterm = (D - lambda) * cc;
+    d.h.key = key;
+    d.h.cc = cc;
+    d.h.dterm = (D - lambda) * cc;
   }
   unsigned cnt_o[2] = {0, 0}, cnt_v[2] = {0, 0};
   for (int base = 0; base < M; base += 32) {
@@ -144,19 +150,19 @@ __device__ void det_setup_warp(DetInfo<KT>& d, const KT& key, double cc, double 
   }
   if (lane == 0) {
     for (int s = 0; s < 2; ++s) {
-      d.na[s] = cnt_o[s];
-      d.nv[s] = cnt_v[s];
-      d.nvp[s] = c2(cnt_v[s]);
-      d.inv_nvp[s] = d.nvp[s] ? 1.0f / (float)d.nvp[s] : 0.f;
+      d.h.na[s] = cnt_o[s];
+      d.h.nv[s] = cnt_v[s];
+      d.h.nvp[s] = c2(cnt_v[s]);
+      d.h.inv_nvp[s] = d.h.nvp[s] ? 1.0f / (float)d.h.nvp[s] : 0.f;
     }
-    d.nsb = cnt_o[1] * cnt_v[1];
-    d.inv_nsb = d.nsb ? 1.0f / (float)d.nsb : 0.f;
-    d.c[0] = 1;
-    d.c[1] = d.c[0] + cnt_o[0] * cnt_v[0];
-    d.c[2] = d.c[1] + cnt_o[1] * cnt_v[1];
-    d.c[3] = d.c[2] + c2(cnt_o[0]) * d.nvp[0];
-    d.c[4] = d.c[3] + c2(cnt_o[1]) * d.nvp[1];
-    d.c[5] = d.c[4] + cnt_o[0] * cnt_v[0] * d.nsb;
+    d.h.nsb = cnt_o[1] * cnt_v[1];
+    d.h.inv_nsb = d.h.nsb ? 1.0f / (float)d.h.nsb : 0.f;
+    d.h.c[0] = 1;
+    d.h.c[1] = d.h.c[0] + cnt_o[0] * cnt_v[0];
+    d.h.c[2] = d.h.c[1] + cnt_o[1] * cnt_v[1];
+    d.h.c[3] = d.h.c[2] + c2(cnt_o[0]) * d.h.nvp[0];
+    d.h.c[4] = d.h.c[3] + c2(cnt_o[1]) * d.h.nvp[1];
+    d.h.c[5] = d.h.c[4] + cnt_o[0] * cnt_v[0] * d.h.nsb;
   }
 }
 
@@ -191,8 +197,10 @@ __device__ __forceinline__ void fill_pair_table(unsigned short* pt) {
 }
 #endif  // __CUDACC__
 
+// (fields are selected, not indexed by spin, so that a register copy of the
+// head stays in registers)
 template <class KT>
-SFCI_HD Exc decode(const DetInfo<KT>& d, const unsigned short* pt, unsigned l) {
+SFCI_HD Exc decode(const DetHead<KT>& d, const unsigned short* pt, unsigned l) {
   Exc e;
   e.s = 0;
   e.x = e.y = e.u = e.v = 0;
@@ -203,17 +211,18 @@ SFCI_HD Exc decode(const DetInfo<KT>& d, const unsigned short* pt, unsigned l) {
   if (l < d.c[2]) {
     e.cls = 1;
     e.s = l < d.c[1] ? 0 : 1;
-    e.x = l - d.c[e.s];
+    e.x = l - (e.s ? d.c[1] : d.c[0]);
     return e;
   }
   if (l < d.c[4]) {
     e.cls = 2;
     const int s = l < d.c[3] ? 0 : 1;
-    const unsigned r = l - d.c[2 + s];
-    const unsigned op = fdiv(r, d.nvp[s], d.inv_nvp[s]);
+    const unsigned r = l - (s ? d.c[3] : d.c[2]);
+    const unsigned nvp = s ? d.nvp[1] : d.nvp[0];
+    const unsigned op = fdiv(r, nvp, s ? d.inv_nvp[1] : d.inv_nvp[0]);
     e.s = s;
     pair_of(pt, op, e.x, e.y);
-    pair_of(pt, r - op * d.nvp[s], e.u, e.v);
+    pair_of(pt, r - op * nvp, e.u, e.v);
     return e;
   }
   e.cls = 3;
@@ -224,12 +233,12 @@ SFCI_HD Exc decode(const DetInfo<KT>& d, const unsigned short* pt, unsigned l) {
 }
 
 template <class KT>
-SFCI_HD KT target_key(const DetInfo<KT>& d, const Exc& e) {
-  KT k = d.key;
+SFCI_HD KT target_key(const DetHead<KT>& h, const DetInfo<KT>& d, const Exc& e) {
+  KT k = h.key;
   if (e.cls == 1) {
     key_xor(k, d.kx[e.s][e.x]);
   } else if (e.cls == 2) {
-    const unsigned nv = d.nv[e.s];
+    const unsigned nv = e.s ? h.nv[1] : h.nv[0];
     key_xor(k, d.kx[e.s][e.x * nv + e.u]);
     key_xor(k, d.kx[e.s][e.y * nv + e.v]);
   } else if (e.cls == 3) {
@@ -254,8 +263,8 @@ SFCI_HD double signed_by(unsigned par, double x) { return par ? -x : x; }
 // move's ends fall between the other's (the second move acts on the string the
 // first one left).
 template <class KT>
-SFCI_HD double term_amp(const DetInfo<KT>& d, const Exc& e, const HamView& h) {
-  if (e.cls == 0) return d.dterm;
+SFCI_HD double term_amp(const DetHead<KT>& dh, const DetInfo<KT>& d, const Exc& e, const HamView& h) {
+  if (e.cls == 0) return dh.dterm;
   if (e.cls == 1) {
     // one-body h(a,i) + sum_k (ai|kk) - sum_{k same spin} (ak|ki), src/bitstr.cpp:230-262,269-300
     const int s = e.s;
@@ -265,7 +274,8 @@ SFCI_HD double term_amp(const DetInfo<KT>& d, const Exc& e, const HamView& h) {
     const unsigned pai = sd_pair(t);
     for (int u = 0; u < 2; ++u) {
       const double* row = h.V + ((size_t)(2 * s + u) * h.P + pai) * h.P;
-      for (unsigned kk = 0; kk < d.na[u]; ++kk) {
+      const unsigned nau = u ? dh.na[1] : dh.na[0];
+      for (unsigned kk = 0; kk < nau; ++kk) {
         int k = d.occ[u][kk];
         if (k == i) continue;
         int kp = k >> 1;
@@ -273,11 +283,11 @@ SFCI_HD double term_amp(const DetInfo<KT>& d, const Exc& e, const HamView& h) {
         if (u == s) v -= vget(h, 3 * s, a, k, k, i);
       }
     }
-    return signed_by(sd_par(t), d.cc * v);
+    return signed_by(sd_par(t), dh.cc * v);
   }
   if (e.cls == 2) {
     // entries (a,i,b,j) and (b,i,a,j) of pair (i<j); the second has the opposite phase
-    const unsigned nv = d.nv[e.s];
+    const unsigned nv = e.s ? dh.nv[1] : dh.nv[0];
     const unsigned* sd = d.sd[e.s];
     const unsigned t1 = sd[e.x * nv + e.u], t2 = sd[e.y * nv + e.v];  // i->a, j->b
     const unsigned t3 = sd[e.x * nv + e.v], t4 = sd[e.y * nv + e.u];  // i->b, j->a
@@ -285,7 +295,7 @@ SFCI_HD double term_amp(const DetInfo<KT>& d, const Exc& e, const HamView& h) {
     const double v = vat(h, 3 * e.s, sd_pair(t1), sd_pair(t2)) - vat(h, 3 * e.s, sd_pair(t3), sd_pair(t4));
     const unsigned par =
         sd_par(t1) ^ sd_par(t2) ^ (unsigned)strictly_between(j, a, i) ^ (unsigned)strictly_between(b, a, i);
-    return signed_by(par, d.cc * v);
+    return signed_by(par, dh.cc * v);
   }
   // opposite spin: the single entry of pair (min(i,j), max(i,j))
   const unsigned t0 = d.sd[0][e.x], t1 = d.sd[1][e.y];  // i->a (spin 0), j->b (spin 1)
@@ -294,7 +304,7 @@ SFCI_HD double term_amp(const DetInfo<KT>& d, const Exc& e, const HamView& h) {
   const double v = ij ? vat(h, 1, sd_pair(t0), sd_pair(t1)) : vat(h, 2, sd_pair(t1), sd_pair(t0));
   const unsigned cross = ij ? ((unsigned)strictly_between(j, a, i) ^ (unsigned)strictly_between(b, a, i))
                             : ((unsigned)strictly_between(i, b, j) ^ (unsigned)strictly_between(a, b, j));
-  return signed_by(sd_par(t0) ^ sd_par(t1) ^ cross, d.cc * v);
+  return signed_by(sd_par(t0) ^ sd_par(t1) ^ cross, dh.cc * v);
 }
 
 #ifdef __CUDACC__

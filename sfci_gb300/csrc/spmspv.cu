@@ -253,7 +253,7 @@ __host__ __device__ inline size_t gen_smem_bytes(int mode, unsigned nbp) {
   size_t s = al16(sizeof(DetInfo<KT>)) + al16(2016 * sizeof(unsigned short));
   if (mode != M_ENERGY) s += al16(sizeof(uint32_t) * nbp);
   if (mode == M_SCATTER)
-    s += al16(sizeof(uint32_t) * nbp) + al16(sizeof(u64) * nbp) + 2 * al16(sizeof(unsigned short) * GEN_ROUND);
+    s += al16(sizeof(uint32_t) * nbp) + 2 * al16(sizeof(u64) * nbp) + 2 * al16(sizeof(unsigned short) * GEN_ROUND);
   return s;
 }
 
@@ -268,12 +268,15 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
   uint32_t* hist = reinterpret_cast<uint32_t*>(smem + off);
   off += al16(sizeof(uint32_t) * (MODE == M_ENERGY ? 0 : nbp));
   uint32_t* bst = reinterpret_cast<uint32_t*>(smem + off);
-  u64* cur = nullptr;
+  u64* cur = nullptr;            // next output position of each bin
+  u64* rbase = nullptr;          // this round: output position of staged item 0's bin run, per bin
   unsigned short* sx = nullptr;  // staged: term index within the round
   unsigned short* sb = nullptr;  // staged: local bin
   if (MODE == M_SCATTER) {
     off += al16(sizeof(uint32_t) * nbp);
     cur = reinterpret_cast<u64*>(smem + off);
+    off += al16(sizeof(u64) * nbp);
+    rbase = reinterpret_cast<u64*>(smem + off);
     off += al16(sizeof(u64) * nbp);
     sx = reinterpret_cast<unsigned short*>(smem + off);
     off += al16(sizeof(unsigned short) * GEN_ROUND);
@@ -311,6 +314,7 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
     __syncthreads();
     det_fill_singles(d, tid, GEN_THREADS);
     __syncthreads();
+    const DetHead<KT> dh = d.h;
     const unsigned l0 = (unsigned)(t0 - dbeg);
     const unsigned l1 = (unsigned)((t1 < dend ? t1 : dend) - dbeg);
     for (unsigned rb = l0; rb < l1; rb += GEN_ROUND) {
@@ -325,7 +329,7 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
           unsigned l = rb + it * GEN_THREADS + tid;
           br[it] = ~0u;
           if (l < l1) {
-            const unsigned bin = (unsigned)(key_hash(target_key(d, decode(d, pt, l))) >> shift1);
+            const unsigned bin = (unsigned)(key_hash(target_key(dh, d, decode(dh, pt, l))) >> shift1);
             if (bin >= g.bin_lo && bin < g.bin_hi) {
               unsigned lb = bin - g.bin_lo;
               unsigned r = atomicAdd(&hist[lb], 1u);
@@ -334,9 +338,20 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
           }
         }
         __syncthreads();
+        // the owner of each bin takes its count (clearing it for the next
+        // round), scans, and advances the bin's output position
+        uint32_t cnt = 0;
+        if (tid < (int)nbp) {
+          cnt = hist[tid];
+          hist[tid] = 0;
+        }
         uint32_t tot;
-        uint32_t ex = block_excl_scan<uint32_t, GEN_THREADS>(tid < (int)nbp ? hist[tid] : 0u, &tot, s_scan);
-        if (tid < (int)nbp) bst[tid] = ex;
+        uint32_t ex = block_excl_scan<uint32_t, GEN_THREADS>(cnt, &tot, s_scan);
+        if (tid < (int)nbp) {
+          bst[tid] = ex;
+          rbase[tid] = cur[tid] - ex;
+          cur[tid] += cnt;
+        }
         __syncthreads();
 #pragma unroll
         for (int it = 0; it < GEN_IPT; ++it) {
@@ -347,31 +362,26 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
           }
         }
         __syncthreads();
+        // the next round touches rbase, sx and sb only after its own first
+        // barrier, which every thread reaches after finishing this loop
         for (unsigned i = tid; i < tot; i += GEN_THREADS) {
-          const unsigned lb = sb[i];
-          const u64 pos = cur[lb] + (i - bst[lb]);
-          const Exc e = decode(d, pt, rb + sx[i]);
-          g.okeys[pos] = target_key(d, e);
-          g.oamps[pos] = term_amp(d, e, g.h);
+          const u64 pos = rbase[sb[i]] + i;
+          const Exc e = decode(dh, pt, rb + sx[i]);
+          g.okeys[pos] = target_key(dh, d, e);
+          g.oamps[pos] = term_amp(dh, d, e, g.h);
         }
-        __syncthreads();
-        if (tid < (int)nbp) {
-          cur[tid] += hist[tid];
-          hist[tid] = 0;
-        }
-        __syncthreads();
       } else {
 #pragma unroll 2
         for (int it = 0; it < GEN_IPT; ++it) {
           unsigned l = rb + it * GEN_THREADS + tid;
           if (l < l1) {
             if (MODE == M_COUNT) {
-              atomicAdd(&hist[(unsigned)(key_hash(target_key(d, decode(d, pt, l))) >> shift1)], 1u);
+              atomicAdd(&hist[(unsigned)(key_hash(target_key(dh, d, decode(dh, pt, l))) >> shift1)], 1u);
             } else {
-              const Exc e = decode(d, pt, l);
-              const KT key = target_key(d, e);
+              const Exc e = decode(dh, pt, l);
+              const KT key = target_key(dh, d, e);
               int s = table_find_global(g.tkeys, g.tmask, key);
-              if (s >= 0) eacc += term_amp(d, e, g.h) * __ldcg(g.tvals + s);
+              if (s >= 0) eacc += term_amp(dh, d, e, g.h) * __ldcg(g.tvals + s);
             }
           }
         }

@@ -15,9 +15,9 @@ static HamHost g_h;
 
 template <class KT>
 static void setup_host(DetInfo<KT>& d, const KT& key, int M, double cc, double D) {
-  d.key = key;
-  d.cc = cc;
-  d.dterm = D * cc;
+  d.h.key = key;
+  d.h.cc = cc;
+  d.h.dterm = D * cc;
   for (int s = 0; s < 2; ++s) {
     unsigned no = 0, nv = 0;
     for (int o = 0; o < M; ++o) {
@@ -25,19 +25,19 @@ static void setup_host(DetInfo<KT>& d, const KT& key, int M, double cc, double D
       if (key_test(key, b)) d.occ[s][no++] = (unsigned char)b;
       else d.vir[s][nv++] = (unsigned char)b;
     }
-    d.na[s] = no;
-    d.nv[s] = nv;
-    d.nvp[s] = c2(nv);
-    d.inv_nvp[s] = d.nvp[s] ? 1.0f / (float)d.nvp[s] : 0.f;
+    d.h.na[s] = no;
+    d.h.nv[s] = nv;
+    d.h.nvp[s] = c2(nv);
+    d.h.inv_nvp[s] = d.h.nvp[s] ? 1.0f / (float)d.h.nvp[s] : 0.f;
   }
-  d.nsb = d.na[1] * d.nv[1];
-  d.inv_nsb = d.nsb ? 1.0f / (float)d.nsb : 0.f;
-  d.c[0] = 1;
-  d.c[1] = d.c[0] + d.na[0] * d.nv[0];
-  d.c[2] = d.c[1] + d.na[1] * d.nv[1];
-  d.c[3] = d.c[2] + c2(d.na[0]) * d.nvp[0];
-  d.c[4] = d.c[3] + c2(d.na[1]) * d.nvp[1];
-  d.c[5] = d.c[4] + d.na[0] * d.nv[0] * d.nsb;
+  d.h.nsb = d.h.na[1] * d.h.nv[1];
+  d.h.inv_nsb = d.h.nsb ? 1.0f / (float)d.h.nsb : 0.f;
+  d.h.c[0] = 1;
+  d.h.c[1] = d.h.c[0] + d.h.na[0] * d.h.nv[0];
+  d.h.c[2] = d.h.c[1] + d.h.na[1] * d.h.nv[1];
+  d.h.c[3] = d.h.c[2] + c2(d.h.na[0]) * d.h.nvp[0];
+  d.h.c[4] = d.h.c[3] + c2(d.h.na[1]) * d.h.nvp[1];
+  d.h.c[5] = d.h.c[4] + d.h.na[0] * d.h.nv[0] * d.h.nsb;
   det_fill_singles(d, 0, 1);
 }
 
@@ -79,24 +79,24 @@ extern "C" long gh_terms(const uint64_t* kw, uint64_t* out_k, double* out_a, lon
     DetInfo<u64> d;
     u64 key = kw[0];
     setup_host(d, key, g_h.M, 1.0, diag_host(key, h));
-    for (unsigned l = 0; l < d.c[5]; ++l, ++n) {
-      Exc e = decode(d, pt, l);
+    for (unsigned l = 0; l < d.h.c[5]; ++l, ++n) {
+      Exc e = decode(d.h, pt, l);
       if (n < cap) {
-        out_k[n] = target_key(d, e);
-        out_a[n] = term_amp(d, e, h);
+        out_k[n] = target_key(d.h, d, e);
+        out_a[n] = term_amp(d.h, d, e, h);
       }
     }
   } else {
     DetInfo<K128> d;
     K128 key{kw[0], kw[1]};
     setup_host(d, key, g_h.M, 1.0, diag_host(key, h));
-    for (unsigned l = 0; l < d.c[5]; ++l, ++n) {
-      Exc e = decode(d, pt, l);
+    for (unsigned l = 0; l < d.h.c[5]; ++l, ++n) {
+      Exc e = decode(d.h, pt, l);
       if (n < cap) {
-        K128 t = target_key(d, e);
+        K128 t = target_key(d.h, d, e);
         out_k[2 * n] = t.lo;
         out_k[2 * n + 1] = t.hi;
-        out_a[n] = term_amp(d, e, h);
+        out_a[n] = term_amp(d.h, d, e, h);
       }
     }
   }

@@ -317,21 +317,32 @@ def run_gpu(args, rank, ws, local, dist):
     hbm, how = peaks()
     T = stats["terms"]
     surv = stats["survivors"]
+    # partition levels: generation resolves L1_BITS of the leaf hash, each level up to DIGIT_BITS more
+    L1_BITS, DIGIT_BITS = 9, 9
+    b = max(1, int(round(np.log2(max(stats["leaves"], 1)))))
+    levels = -(-(b - min(b, L1_BITS)) // DIGIT_BITS)
     # algorithmic bytes per phase (all launches of the timed steps)
     alg = {
         "scatter": 16.0 * T * args.steps,                # generated (key, amp) terms written once
-        "partition": 40.0 * T * args.steps,              # read key (count) + read/write term (scatter)
+        "partition": 40.0 * T * levels * args.steps,     # per level: read key (count) + read/write term (scatter)
         "merge": (16.0 * T + 16.0 * surv) * args.steps,  # read every term once, write survivors
         "count": 0.0,                                    # keys only, kept on chip
         "select": 8.0 * surv * 6 * args.steps,
         "sort": 32.0 * out_len * 7 * args.steps,
         "other": 0.0,
     }
+    kernels = {"scatter": "k_gen<SCATTER>", "partition": "k_part<COUNT,SCATTER>", "merge": "k_leafw",
+               "count": "k_gen<COUNT>", "select": "select_threshold", "sort": "radix_sort_pairs", "other": "-"}
+    # DRAM bytes per generated term measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum over
+    # every launch of a 56-orbital Nd=1e4 run with 4 generation passes), scaled here to a launch by the
+    # terms it processes
+    ncu_bytes_per_term = {"scatter": 17.51, "partition": 50.53 * levels, "merge": 16.11}
     dom = max(prof, key=lambda k: prof[k][0])
     dms, dl = prof[dom]
     per_launch_bytes = alg[dom] / max(dl, 1)
     per_launch_ms = dms / max(dl, 1)
     achieved = per_launch_bytes / (per_launch_ms * 1e-3) / 1e9 if per_launch_ms > 0 else 0.0
+    traffic = (ncu_bytes_per_term[dom] * T * args.steps / max(dl, 1)) if dom in ncu_bytes_per_term else None
     value = T_conn * ws / (ms_max * 1e-3)
     e2e_val = T_conn * ws / e2e_s
     res = {
@@ -344,11 +355,12 @@ def run_gpu(args, rank, ws, local, dist):
                    "connected_per_det": C, "emitted_per_det_reference": emitted_per_det(M_SPATIAL, 7, 7),
                    "generated_terms_per_step": T, "merged_unique_per_step": stats["unique"],
                    "survivors_per_step": surv, "output_dets": out_len,
-                   "passes": stats["passes"], "leaves": stats["leaves"],
+                   "passes": stats["passes"], "leaves": stats["leaves"], "partition_levels": levels,
                    "l2": "inputs larger than L2: %.0f GB of terms per step vs 129 MB" % (16.0 * T / 1e9),
                    "parallelism": "replicas" if ws > 1 else "1 GPU"},
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "peak_source": how, "traffic": None,
+        "roofline": {"bound": "hbm", "kernel": kernels[dom], "phase": dom, "achieved": achieved, "peak": hbm,
+                     "unit": "GB/s", "frac": achieved / hbm, "peak_source": how, "traffic": traffic,
+                     "traffic_unit": "bytes per launch", "algorithmic_bytes_per_launch": per_launch_bytes,
                      "launches": dl, "ms_per_launch": per_launch_ms},
         "phases_ms_per_step": {k: v[0] / args.steps for k, v in prof.items()},
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,

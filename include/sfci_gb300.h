@@ -104,7 +104,10 @@ int sfci_vec_clear(sfci_vec* v);                                   /* setZeroVec
  *   out = top_cap( { k : |a_k| > coeff_cut } of merge( coeff * (H - lambda) * top_Nd(in) ) )
  * sorted by key, with *diag = coeff * <top_Nd(in)| (H - lambda) |top_Nd(in)>
  * evaluated before the cut.  An empty input leaves *diag untouched and
- * empties out, as the reference does (:529-533). */
+ * empties out, as the reference does (:529-533).  Merged amplitudes are exact
+ * sums rounded once; a term with |amplitude| >= 2^24 (or not finite) gives
+ * SFCI_ERR_NUMERIC, and determinants connected to more than 2^19 others give
+ * SFCI_ERR_UNSUPPORTED. */
 int sfci_spmspv(sfci_ctx* ctx, const sfci_vec* in, sfci_vec* out, double lambda, double coeff,
                 double* diag);
 /* DiagCal_bit (src/bitstr.cpp:433-476) for `n` host keys. */

@@ -85,8 +85,6 @@ def _sigs(L):
     L.sfci_lanczos_ground.argtypes = [_vp, _vp, C.c_int, C.c_int, _vp, C.POINTER(C.c_double)]
     L.sfci_minres.argtypes = [_vp, _vp, _vp, _vp, C.c_int, C.c_double, C.c_double, C.POINTER(C.c_int)]
     L.sfci_gsaes.argtypes = [C.c_int, _vp, _vp, _vp, _vp]
-    for name in dir(L):
-        pass
     return L
 
 

@@ -228,6 +228,45 @@ SFCI_HD void fx_value(u64 acc_lo, u64 acc_hi, u64& L, u64& H) {
   H = (u64)((long long)acc_hi >> (64 - FX_SPLIT)) + (L < l0 ? 1ull : 0ull);
 }
 
+// Narrow form for merge tables whose slots receive at most FX32_MAX_TERMS terms:
+// F (same units) as four signed base-2^21 digits, each summed in its own 32-bit
+// word (11 bits of headroom) with native 32-bit reductions.  A term below 2^-44
+// touches one word, a typical one three; |x| must stay below 2^FX32_MAX_EXP.
+constexpr int FX32_DIG = 21;
+constexpr int FX32_MAX_EXP = 18;
+constexpr unsigned FX32_MAX_TERMS = 1u << 11;
+
+// the four digits of x; sets *big for |x| >= 2^FX32_MAX_EXP or not finite
+SFCI_HD void fx32_digits(double x, int dg[4], unsigned& big) {
+  const u64 b = dbl_bits(x);
+  const int e = (int)((b >> 52) & 0x7ff);
+  dg[0] = dg[1] = dg[2] = dg[3] = 0;
+  if (e >= 1023 + FX32_MAX_EXP) {
+    big = 1u;
+    return;
+  }
+  const u64 m = (b & 0xfffffffffffffull) | (1ull << 52);
+  const int s = e - (1075 - FX_FRAC);  // |F| = m * 2^s < 2^(FX_FRAC + FX32_MAX_EXP)
+  if (e == 0 || s <= -53) return;
+  __int128 f = s < 0 ? (__int128)(m >> -s) : ((__int128)m << s);
+  if (b >> 63) f = -f;
+  for (int k = 0; k < 3; ++k) {
+    const long long d = (long long)(((unsigned long long)f + (1ull << (FX32_DIG - 1))) & ((1ull << FX32_DIG) - 1)) -
+                        (1ll << (FX32_DIG - 1));
+    dg[k] = (int)d;
+    f = (f - d) >> FX32_DIG;  // exact: the low FX32_DIG bits of f - d are zero
+  }
+  dg[3] = (int)f;  // |f| <= 2^(FX_FRAC + FX32_MAX_EXP - 3 * FX32_DIG) = 2^19: 2^11 of them fit a word
+}
+
+// the 128-bit sum (H:L) of four digit-word sums
+SFCI_HD void fx32_value(const int w[4], u64& L, u64& H) {
+  __int128 f = (__int128)w[3];
+  for (int k = 2; k >= 0; --k) f = f * (__int128)(1ll << FX32_DIG) + (__int128)w[k];
+  L = (u64)f;
+  H = (u64)(f >> 64);
+}
+
 // (H:L) * 2^-FX_FRAC rounded to the nearest double, ties to even
 SFCI_HD double fx_to_double(u64 lo, u64 hi) {
   const u64 neg = hi >> 63;

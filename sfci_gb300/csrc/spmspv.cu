@@ -127,9 +127,8 @@ struct FxCut {
   long long cutk;  // cut_key(cut)
   int all;
 };
-__device__ __forceinline__ bool fx_survives(u64 acc_lo, u64 acc_hi, const FxCut& c, double& v) {
-  u64 lo, hi;
-  fx_value(acc_lo, acc_hi, lo, hi);
+// the cut on a 128-bit sum (hi:lo) in units of 2^-FX_FRAC
+__device__ __forceinline__ bool fx_survives_value(u64 lo, u64 hi, const FxCut& c, double& v) {
   if (!c.all) {
     u64 mlo = lo, mhi = hi;
     if ((long long)hi < 0) {
@@ -140,6 +139,12 @@ __device__ __forceinline__ bool fx_survives(u64 acc_lo, u64 acc_hi, const FxCut&
   }
   v = fx_to_double(lo, hi);
   return above_cut(v, c.cutk);
+}
+// the cut on a split accumulator (acc_hi * 2^FX_SPLIT + acc_lo)
+__device__ __forceinline__ bool fx_survives(u64 acc_lo, u64 acc_hi, const FxCut& c, double& v) {
+  u64 lo, hi;
+  fx_value(acc_lo, acc_hi, lo, hi);
+  return fx_survives_value(lo, hi, c, v);
 }
 static FxCut fx_cut(double cut) {
   FxCut c{};
@@ -603,18 +608,38 @@ struct STable {
 };
 constexpr size_t SLOT_BYTES_EXTRA = 2 * sizeof(u64);
 
+// Warp-table layout with `n` slots: keys, then the four 32-bit digit-sum words
+// of the narrow accumulator (word k of slot s at w[k * n + s]).
+template <class KT>
+struct WTable {
+  KT* k;
+  unsigned* w;
+  unsigned n;
+  __device__ __forceinline__ WTable(unsigned char* base, unsigned n_)
+      : k(reinterpret_cast<KT*>(base)), w(reinterpret_cast<unsigned*>(base + sizeof(KT) * n_)), n(n_) {}
+  __device__ __forceinline__ void value(unsigned s, u64& L, u64& H) const {
+    const int v[4] = {(int)w[s], (int)w[n + s], (int)w[2 * n + s], (int)w[3 * n + s]};
+    fx32_value(v, L, H);
+  }
+  __device__ __forceinline__ double amp(unsigned s) const {
+    u64 L, H;
+    value(s, L, H);
+    return fx_to_double(L, H);
+  }
+};
+constexpr size_t WSLOT_BYTES_EXTRA = 4 * sizeof(unsigned);
+
 template <class KT>
 __global__ void __launch_bounds__(LW_WARPS * 32, sizeof(KT) == 8 ? 4 : 3) k_leafw(LeafArgs<KT> a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  STable<KT> t(smem + (sizeof(KT) + SLOT_BYTES_EXTRA) * TW_MAX * warp, TW_MAX);
+  WTable<KT> t(smem + (sizeof(KT) + WSLOT_BYTES_EXTRA) * TW_MAX * warp, TW_MAX);
   __shared__ double s_red[LW_WARPS];
   __shared__ u64 s_uq[LW_WARPS];
   const KT empty = key_empty<KT>();
   const unsigned lt = (1u << lane) - 1u;
   double dacc = 0.0;
   u64 uq = 0;
-  unsigned bad = 0;
   for (u64 leaf = (u64)blockIdx.x * LW_WARPS + warp; leaf < a.nleaves; leaf += (u64)gridDim.x * LW_WARPS) {
     const u64 beg = a.loff[leaf], end = a.loff[leaf + 1], n = end - beg;
     unsigned tb = 32;
@@ -625,11 +650,12 @@ __global__ void __launch_bounds__(LW_WARPS * 32, sizeof(KT) == 8 ? 4 : 3) k_leaf
     }
     for (unsigned s = lane; s < tb; s += 32) {
       t.k[s] = empty;
-      t.lo[s] = 0;
-      t.hi[s] = 0;
+#pragma unroll
+      for (int w = 0; w < 4; ++w) t.w[w * TW_MAX + s] = 0u;
     }
     __syncwarp();
-    bool ovf = false;
+    // a leaf too long for the narrow accumulators goes straight to the next tier
+    bool ovf = n > FX32_MAX_TERMS;
     // batches of LW_BATCH items per lane: the loads of a batch are issued before
     // any shared-memory atomic, so their latencies overlap
     for (u64 e0 = beg; e0 < end && !ovf; e0 += 32 * LW_BATCH) {
@@ -647,11 +673,17 @@ __global__ void __launch_bounds__(LW_WARPS * 32, sizeof(KT) == 8 ? 4 : 3) k_leaf
       for (int q = 0; q < LW_BATCH; ++q) {
         const u64 e = e0 + (u64)q * 32 + lane;
         if (e < end && !ovf) {
-          u64 xl, xh;
-          fx_addends(ab[q], xl, xh, bad);
-          const int s = table_slot(t.k, tb - 1, kb[q], leaf_slot(kb[q], tbits), LW_PROBE);
-          if (s < 0) ovf = true;
-          else fx_red(t.lo + s, t.hi + s, xl, xh);
+          int dg[4];
+          unsigned big = 0;
+          fx32_digits(ab[q], dg, big);  // out of the narrow range: the next tier takes the leaf
+          const int s = big ? -1 : table_slot(t.k, tb - 1, kb[q], leaf_slot(kb[q], tbits), LW_PROBE);
+          if (s < 0) {
+            ovf = true;
+          } else {
+#pragma unroll
+            for (int w = 0; w < 4; ++w)
+              if (dg[w]) atomicAdd(t.w + w * TW_MAX + s, (unsigned)dg[w]);
+          }
         }
       }
     }
@@ -676,7 +708,9 @@ __global__ void __launch_bounds__(LW_WARPS * 32, sizeof(KT) == 8 ? 4 : 3) k_leaf
       const KT k = t.k[s];
       double v = 0.0;
       const bool used = !key_eq(k, empty);
-      const bool keep = used && fx_survives(t.lo[s], t.hi[s], a.cut, v);
+      u64 L = 0, H = 0;
+      if (used) t.value(s, L, H);
+      const bool keep = used && fx_survives_value(L, H, a.cut, v);
       uq += __popc(__ballot_sync(0xffffffffu, used));
       const unsigned m = __ballot_sync(0xffffffffu, keep);
       if (m) {
@@ -692,7 +726,6 @@ __global__ void __launch_bounds__(LW_WARPS * 32, sizeof(KT) == 8 ? 4 : 3) k_leaf
     }
     __syncwarp();
   }
-  if (bad) atomicOr(a.bad, 1u);
   double v = warp_sum(dacc);
   if (lane == 0) {
     s_red[warp] = v;
@@ -711,9 +744,10 @@ __global__ void __launch_bounds__(LW_WARPS * 32, sizeof(KT) == 8 ? 4 : 3) k_leaf
   }
 }
 
-// Second tier: leaves whose distinct keys overflowed a warp table, one CTA per
-// leaf with a 4096-slot shared-memory table; leaves that overflow this too go
-// to the global-memory table below.
+// Second tier: leaves that a warp table could not take (too many distinct keys,
+// more than FX32_MAX_TERMS terms, or a term outside the narrow range), one CTA
+// per leaf with a 4096-slot shared-memory table and wide accumulators; leaves
+// that overflow this too go to the global-memory table below.
 template <class KT>
 __global__ void __launch_bounds__(LC_THREADS) k_leafc(LeafArgs<KT> a, const unsigned* __restrict__ ids, unsigned nids,
                                                       unsigned* __restrict__ ovf2) {
@@ -959,7 +993,7 @@ static int leaf_smem_config() {
   typedef typename KeyOf<W>::T KT;
   static bool done = false;
   if (!done) {
-    const int sm = (int)((sizeof(KT) + SLOT_BYTES_EXTRA) * TW_MAX * LW_WARPS);
+    const int sm = (int)((sizeof(KT) + WSLOT_BYTES_EXTRA) * TW_MAX * LW_WARPS);
     SFCI_CUDA(cudaFuncSetAttribute(k_leafw<KT>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     SFCI_CUDA(cudaFuncSetAttribute(k_leafc<KT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)((sizeof(KT) + SLOT_BYTES_EXTRA) * LC_SLOTS)));
@@ -1107,7 +1141,7 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
   {
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_leafw<KT>, LW_WARPS * 32,
-                                                      (sizeof(KT) + SLOT_BYTES_EXTRA) * TW_MAX * LW_WARPS) ==
+                                                      (sizeof(KT) + WSLOT_BYTES_EXTRA) * TW_MAX * LW_WARPS) ==
             cudaSuccess &&
         per_sm > 0)
       leaf_resident = std::min<unsigned>(leafgrid, (unsigned)per_sm * c.sm_count);
@@ -1156,7 +1190,7 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
   double* dbig = (double*)scratch_get(c, "sp_dbig", sizeof(double));
   if (!dbig) return SFCI_ERR_NOMEM;
   SFCI_CUDA(cudaMemsetAsync(dbig, 0, sizeof(double), c.stream));
-  const size_t lsm = (sizeof(KT) + SLOT_BYTES_EXTRA) * TW_MAX * LW_WARPS;
+  const size_t lsm = (sizeof(KT) + WSLOT_BYTES_EXTRA) * TW_MAX * LW_WARPS;
   std::vector<u64> segs, nsegs_h;
   std::vector<Unit> units;
   std::vector<u64> segbase;

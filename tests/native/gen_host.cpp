@@ -121,3 +121,20 @@ extern "C" double gh_fx_sum(const double* a, long n, int* bad) {
 
 // one term converted in and straight back (truncation to the 2^-64 grid)
 extern "C" double gh_fx_roundtrip(double x, int* bad) { return gh_fx_sum(&x, 1, bad); }
+
+// The narrow digit form: sums n terms as the warp tables do (four 32-bit words
+// of signed base-2^21 digits) and converts back.  *big reports an out-of-range
+// term.
+extern "C" double gh_fx32_sum(const double* a, long n, int* big) {
+  int w[4] = {0, 0, 0, 0};
+  unsigned b = 0;
+  for (long i = 0; i < n; ++i) {
+    int dg[4];
+    fx32_digits(a[i], dg, b);
+    for (int k = 0; k < 4; ++k) w[k] = (int)((unsigned)w[k] + (unsigned)dg[k]);
+  }
+  *big = (int)b;
+  u64 L, H;
+  fx32_value(w, L, H);
+  return fx_to_double(L, H);
+}

@@ -125,3 +125,43 @@ def test_many_terms_on_one_accumulator(fx):
     got, _ = fsum(fx, terms)
     assert got == float(Fraction(sum(trunc_grid(float(t)) for t in terms[:20000])
                                  + sum(trunc_grid(float(t)) for t in terms[20000:]), 1 << FRAC))
+
+
+@pytest.fixture(scope="module")
+def fx32(fx):
+    fx.gh_fx32_sum.restype = C.c_double
+    fx.gh_fx32_sum.argtypes = [np.ctypeslib.ndpointer(np.float64), C.c_long, C.POINTER(C.c_int)]
+    return fx
+
+
+def f32sum(L, terms):
+    big = C.c_int(0)
+    a = np.ascontiguousarray(terms, dtype=np.float64)
+    return L.gh_fx32_sum(a, len(a), C.byref(big)), big.value
+
+
+def test_digit_form_sums_exactly(fx32):
+    """The warp tables' narrow form (four words of signed base-2^21 digits) gives
+    the same exact, correctly rounded sums as the wide form."""
+    rng = np.random.default_rng(11)
+    for trial in range(300):
+        n = int(rng.integers(1, 60))
+        terms = np.exp2(rng.uniform(-70, 17.9, n)) * rng.choice([-1.0, 1.0], n)
+        got, big = f32sum(fx32, terms)
+        assert big == 0
+        assert got == exact(terms), (trial, terms)
+        rng.shuffle(terms)
+        assert f32sum(fx32, terms)[0] == got
+    x = rng.uniform(-5, 5, 9)
+    assert f32sum(fx32, np.concatenate([x, -x]))[0] == 0.0
+
+
+def test_digit_form_capacity_and_range(fx32):
+    n = 1 << 11  # terms one warp-table slot may receive
+    big = math.ldexp(1.0, 18) * (1 - 2 ** -53)
+    for sign in (1.0, -1.0):
+        got, flag = f32sum(fx32, np.full(n, sign * big))
+        assert flag == 0
+        assert got == sign * float(Fraction(trunc_grid(big)) * n / (1 << FRAC))
+    for x in (math.ldexp(1.0, 18), -3e5, float("inf"), float("nan")):
+        assert f32sum(fx32, np.array([x]))[1] == 1

@@ -95,6 +95,19 @@ int sfci_vec_upload(sfci_vec* v, const uint64_t* keys, const double* amps, uint6
 /* Device -> host: copies min(len, cap) entries, reports len. */
 int sfci_vec_download(const sfci_vec* v, uint64_t* keys, double* amps, uint64_t cap,
                       uint64_t* len);
+/* Restart-vector text files in the reference's wf_self_as_guess.out format
+ * (writer src/minres.cpp:59-70, reader readPsi src/main.cpp:288-307): the
+ * length on the first line, then "key amplitude" per line, the key in decimal
+ * (the whole 128-bit value for two-word keys) and the amplitude with 12
+ * significant digits.  sfci_vec_load checks keys against num_orb, returns
+ * SFCI_ERR_CAPACITY when the file holds more than the vector's capacity and
+ * sorts the vector by key.  The sfci_psi_* forms work on host arrays and need
+ * no GPU; sfci_psi_read with keys and amps NULL and cap 0 reports the length. */
+int sfci_vec_save(const sfci_vec* v, const char* path);
+int sfci_vec_load(sfci_vec* v, const char* path);
+int sfci_psi_write(const uint64_t* keys, const double* amps, uint64_t n, int key_words, const char* path);
+int sfci_psi_read(const char* path, int key_words, int num_orb, uint64_t* keys, double* amps, uint64_t cap,
+                  uint64_t* len);
 /* dynVec::naiveCopy (src/all.h:610-623); dst->cap must hold src->len. */
 int sfci_vec_copy(sfci_vec* dst, const sfci_vec* src);
 int sfci_vec_clear(sfci_vec* v);                                   /* setZeroVec :244 */

@@ -85,6 +85,10 @@ def _sigs(L):
     L.sfci_lanczos_ground.argtypes = [_vp, _vp, C.c_int, C.c_int, _vp, C.POINTER(C.c_double)]
     L.sfci_minres.argtypes = [_vp, _vp, _vp, _vp, C.c_int, C.c_double, C.c_double, C.POINTER(C.c_int)]
     L.sfci_gsaes.argtypes = [C.c_int, _vp, _vp, _vp, _vp]
+    L.sfci_vec_save.argtypes = [_vp, C.c_char_p]
+    L.sfci_vec_load.argtypes = [_vp, C.c_char_p]
+    L.sfci_psi_write.argtypes = [_vp, _vp, C.c_uint64, C.c_int, C.c_char_p]
+    L.sfci_psi_read.argtypes = [C.c_char_p, C.c_int, C.c_int, _vp, _vp, C.c_uint64, C.POINTER(C.c_uint64)]
     return L
 
 
@@ -153,6 +157,29 @@ def gsaes(K, S):
     _check(L.sfci_gsaes(n, K.ctypes.data_as(C.c_void_p), S.ctypes.data_as(C.c_void_p),
                         ev.ctypes.data_as(C.c_void_p), X.ctypes.data_as(C.c_void_p)))
     return ev, X
+
+
+def psi_write(path: str, keys, amps, key_words: int = 1):
+    """Write a restart-vector file from host arrays (no GPU): the length, then
+    "key amplitude" lines, keys in decimal, amplitudes with 12 significant digits."""
+    L = load_library()
+    keys = np.ascontiguousarray(keys, dtype=np.uint64)
+    amps = np.ascontiguousarray(amps, dtype=np.float64)
+    _check(L.sfci_psi_write(_ptr(keys), _ptr(amps), len(amps), int(key_words), os.fsencode(path)))
+
+
+def psi_read(path: str, num_orb: int, key_words: int = 1):
+    """Read a restart-vector file into host arrays (no GPU); keys are checked
+    against num_orb.  Returns (keys, amps), keys of shape (n, 2) for two words."""
+    L = load_library()
+    n = C.c_uint64()
+    _check(L.sfci_psi_read(os.fsencode(path), int(key_words), int(num_orb), None, None, 0, C.byref(n)))
+    keys = np.zeros((n.value, 2) if key_words == 2 else n.value, dtype=np.uint64)
+    amps = np.zeros(n.value)
+    _check(L.sfci_psi_read(os.fsencode(path), int(key_words), int(num_orb), _ptr(keys), _ptr(amps), n.value,
+                           C.byref(n)))
+    return keys, amps
+
 
 
 class Context:
@@ -329,6 +356,14 @@ class SpVec:
         got = C.c_uint64()
         _check(self.L.sfci_vec_download(self.h, _ptr(keys), _ptr(amps), n, C.byref(got)))
         return keys, amps
+
+    # restart-vector text file, wf_self_as_guess.out format (src/minres.cpp:59-70, src/main.cpp:288-307)
+    def writePsi(self, path: str):
+        _check(self.L.sfci_vec_save(self.h, os.fsencode(path)))
+
+    def readPsi(self, path: str):
+        _check(self.L.sfci_vec_load(self.h, os.fsencode(path)))
+        return self
 
     # dynVec method names (src/all.h)
     def naiveCopy(self, src: "SpVec"):

@@ -21,7 +21,7 @@ EXE = os.path.join(BUILD, "sfci")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_UNITS = ["prims.cu", "spmspv.cu", "vecops.cu", "noalloc.cu"]
-CXX_UNITS = ["abi.cpp", "solver.cpp", "ham.cpp"]
+CXX_UNITS = ["abi.cpp", "solver.cpp", "ham.cpp", "vecio.cpp"]
 
 
 def _cuda_home() -> str:

@@ -245,3 +245,25 @@ def test_cut_levels_select_from_one_exact_merge(golden_in):
         assert np.array_equal(k, base[0][sel])
         assert np.array_equal(a.view(np.uint64), base[1][sel].view(np.uint64))
         assert close(d, base[2])  # <v|Hv> sums leaves in launch order: equal to rounding
+
+
+def test_restart_vector_file_round_trip(golden_in, tmp_path):
+    """Device vector -> wf_self_as_guess.out text (src/minres.cpp:59-70) -> device
+    vector: keys exact, amplitudes at the file's 12 significant digits."""
+    g, path = golden_in("r28")
+    c = sg.Context(path, 56, 14, Nd=200000)
+    rng = np.random.default_rng(31)
+    ints, amps = _sample_vector(rng, 56, 14, 500)
+    v = c.vec_from(np.array(ints, np.uint64), amps)
+    k0, a0 = v.download()
+    p = tmp_path / "wf_self_as_guess.out"
+    v.writePsi(str(p))
+    kh, ah = sg.psi_read(str(p), 56)
+    assert np.array_equal(kh, k0)
+    w = c.vec(1000).readPsi(str(p))
+    k1, a1 = w.download()
+    assert np.array_equal(k1, k0)
+    assert np.array_equal(a1, np.array([float("%.12g" % x) for x in a0]))
+    with pytest.raises(sg.SfciError) as e:
+        c.vec(10).readPsi(str(p))
+    assert e.value.status == "SFCI_ERR_CAPACITY"

@@ -308,6 +308,50 @@ SFCI_HD double term_amp(const DetHead<KT>& dh, const DetInfo<KT>& d, const Exc& 
 }
 
 #ifdef __CUDACC__
+// lane `sub` of 16: its share of a single's sum over occupied orbitals
+template <class KT>
+__device__ double single_amp_sum(const DetHead<KT>& dh, const DetInfo<KT>& d, const Exc& e, const HamView& h,
+                                 int sub) {
+  const int s = e.s;
+  const unsigned t = d.sd[s][e.x];
+  const int i = (int)sd_i(t), a = (int)sd_a(t);
+  const unsigned pai = sd_pair(t);
+  double v = 0.0;
+#pragma unroll
+  for (int u = 0; u < 2; ++u) {
+    const double* row = h.V + ((size_t)(2 * s + u) * h.P + pai) * h.P;
+    const unsigned nau = u ? dh.na[1] : dh.na[0];
+    for (unsigned kk = sub; kk < nau; kk += 16) {
+      const int k = d.occ[u][kk];
+      if (k == i) continue;
+      const int kp = k >> 1;
+      v += SFCI_LDG(row + kp * (kp + 1) / 2 + kp);
+      if (u == s) v -= vget(h, 3 * s, a, k, k, i);
+    }
+  }
+  return v;
+}
+
+// term_amp of a single excitation evaluated by a half-warp: its 16 lanes split
+// the sum over occupied orbitals (one integral load each, all in flight
+// together) and combine it with a shuffle reduction within the half.  All 32
+// lanes must call it (each half with its own excitation; `active` false adds
+// nothing); every lane of a half returns that half's element.
+template <class KT>
+__device__ double single_amp_half(const DetHead<KT>& dh, const DetInfo<KT>& d, const Exc& e, const HamView& h,
+                                  bool active) {
+  const int sub = threadIdx.x & 15;
+  double v = 0.0;
+  if (active) v = single_amp_sum(dh, d, e, h, sub);
+#pragma unroll
+  for (int o = 8; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if (!active) return 0.0;
+  const unsigned t = d.sd[e.s][e.x];
+  const int i = (int)sd_i(t), a = (int)sd_a(t);
+  v += SFCI_LDG(h.h1 + ((size_t)e.s * h.M + (a >> 1)) * h.M + (i >> 1));
+  return signed_by(sd_par(t), dh.cc * v);
+}
+
 // <D|H|D>: E_core + sum_occ h(i,i) + sum_{i<j} [J_ij - delta_spin K_ij], with
 // J and K symmetrised over the two stored orientations as DiagCal_bit's
 // half-weighted scan of both entries does (src/bitstr.cpp:433-476).

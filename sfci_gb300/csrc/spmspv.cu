@@ -258,7 +258,7 @@ __host__ __device__ inline size_t gen_smem_bytes(int mode, unsigned nbp) {
   size_t s = al16(sizeof(DetInfo<KT>)) + al16(2016 * sizeof(unsigned short));
   if (mode != M_ENERGY) s += al16(sizeof(uint32_t) * nbp);
   if (mode == M_SCATTER)
-    s += al16(sizeof(uint32_t) * nbp) + 2 * al16(sizeof(u64) * nbp) + 2 * al16(sizeof(unsigned short) * GEN_ROUND);
+    s += al16(sizeof(uint32_t) * nbp) + 2 * al16(sizeof(u64) * nbp) + 3 * al16(sizeof(unsigned short) * GEN_ROUND);
   return s;
 }
 
@@ -277,6 +277,7 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
   u64* rbase = nullptr;          // this round: output position of staged item 0's bin run, per bin
   unsigned short* sx = nullptr;  // staged: term index within the round
   unsigned short* sb = nullptr;  // staged: local bin
+  unsigned short* sq = nullptr;  // staged positions of the round's single excitations
   if (MODE == M_SCATTER) {
     off += al16(sizeof(uint32_t) * nbp);
     cur = reinterpret_cast<u64*>(smem + off);
@@ -286,8 +287,11 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
     sx = reinterpret_cast<unsigned short*>(smem + off);
     off += al16(sizeof(unsigned short) * GEN_ROUND);
     sb = reinterpret_cast<unsigned short*>(smem + off);
+    off += al16(sizeof(unsigned short) * GEN_ROUND);
+    sq = reinterpret_cast<unsigned short*>(smem + off);
   }
   __shared__ u64 s_det;
+  __shared__ unsigned s_nsq;
   __shared__ double s_red[GEN_THREADS / 32];
   __shared__ uint32_t s_scan[GEN_THREADS / 32 + 1];
 
@@ -350,6 +354,7 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
           cnt = hist[tid];
           hist[tid] = 0;
         }
+        if (tid == 0) s_nsq = 0;
         uint32_t tot;
         uint32_t ex = block_excl_scan<uint32_t, GEN_THREADS>(cnt, &tot, s_scan);
         if (tid < (int)nbp) {
@@ -369,11 +374,35 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
         __syncthreads();
         // the next round touches rbase, sx and sb only after its own first
         // barrier, which every thread reaches after finishing this loop
+        // Singles (term indices 1 .. c[2]-1, so only in a determinant's first
+        // rounds) are deferred to a half-warp each: their element sums over all
+        // occupied orbitals, a chain of loads that would stall a whole warp.
+        const bool with_singles = rb < dh.c[2];
         for (unsigned i = tid; i < tot; i += GEN_THREADS) {
-          const u64 pos = rbase[sb[i]] + i;
           const Exc e = decode(dh, pt, rb + sx[i]);
+          if (with_singles && e.cls == 1) {
+            sq[atomicAdd(&s_nsq, 1u)] = (unsigned short)i;
+            continue;
+          }
+          const u64 pos = rbase[sb[i]] + i;
           g.okeys[pos] = target_key(dh, d, e);
           g.oamps[pos] = term_amp(dh, d, e, g.h);
+        }
+        if (with_singles) {
+          __syncthreads();
+          const unsigned nsq = s_nsq;
+          for (unsigned q0 = (tid >> 5) * 2; q0 < nsq; q0 += GEN_THREADS / 16) {
+            const unsigned q = q0 + ((tid >> 4) & 1u);
+            const bool act = q < nsq;
+            const unsigned i = act ? sq[q] : 0u;
+            const Exc e = decode(dh, pt, rb + sx[i]);
+            const double v = single_amp_half(dh, d, e, g.h, act && e.cls == 1);
+            if (act && (tid & 15) == 0) {
+              const u64 pos = rbase[sb[i]] + i;
+              g.okeys[pos] = target_key(dh, d, e);
+              g.oamps[pos] = v;
+            }
+          }
         }
       } else {
 #pragma unroll 2

@@ -307,6 +307,53 @@ SFCI_HD double term_amp(const DetHead<KT>& dh, const DetInfo<KT>& d, const Exc& 
   return signed_by(sd_par(t0) ^ sd_par(t1) ^ cross, dh.cc * v);
 }
 
+// Key and element of a term that is not a single (diagonal, same-spin or
+// opposite-spin double), computed on one straight-line path: the two classes
+// of doubles differ only in which table rows, divisor and integral block they
+// use, so a warp holding both kinds does not run two branches.  Gives the same
+// key and element as target_key and term_amp.
+template <class KT>
+SFCI_HD double double_term(const DetHead<KT>& dh, const DetInfo<KT>& d, const unsigned short* pt, const HamView& h,
+                           unsigned l, KT& key) {
+  const bool opp = l >= dh.c[4];                      // opposite-spin double
+  const int s = (!opp && l >= dh.c[3]) ? 1 : 0;        // spin of a same-spin double
+  const unsigned r = l - (opp ? dh.c[4] : (s ? dh.c[3] : dh.c[2]));
+  const unsigned dv = opp ? dh.nsb : (s ? dh.nvp[1] : dh.nvp[0]);
+  const float inv = opp ? dh.inv_nsb : (s ? dh.inv_nvp[1] : dh.inv_nvp[0]);
+  const unsigned q = fdiv(r, dv, inv), rem = r - q * dv;
+  unsigned k1, k2, k3 = 0, k4 = 0;  // single-table entries: i->a, j->b (and i->b, j->a for same spin)
+  if (opp) {
+    k1 = q;
+    k2 = rem;
+  } else {
+    unsigned x, y, u, v;
+    pair_of(pt, q, x, y);
+    pair_of(pt, rem, u, v);
+    const unsigned nv = s ? dh.nv[1] : dh.nv[0];
+    k1 = x * nv + u;
+    k2 = y * nv + v;
+    k3 = x * nv + v;
+    k4 = y * nv + u;
+  }
+  const int r1 = opp ? 0 : s, r2 = opp ? 1 : s;
+  const unsigned t1 = d.sd[r1][k1], t2 = d.sd[r2][k2];
+  key = dh.key;
+  key_xor(key, d.kx[r1][k1]);
+  key_xor(key, d.kx[r2][k2]);
+  const int i = (int)sd_i(t1), a = (int)sd_a(t1), j = (int)sd_i(t2), b = (int)sd_a(t2);
+  // opposite spin: the entry of pair (min(i,j), max(i,j)); same spin: (a,i,b,j) - (b,i,a,j)
+  const bool fwd = !opp || i < j;
+  const int blk = opp ? (fwd ? 1 : 2) : 3 * s;
+  double v = vat(h, blk, fwd ? sd_pair(t1) : sd_pair(t2), fwd ? sd_pair(t2) : sd_pair(t1));
+  if (!opp) {
+    const unsigned t3 = d.sd[s][k3], t4 = d.sd[s][k4];
+    v -= vat(h, blk, sd_pair(t3), sd_pair(t4));
+  }
+  const unsigned cross = fwd ? ((unsigned)strictly_between(j, a, i) ^ (unsigned)strictly_between(b, a, i))
+                             : ((unsigned)strictly_between(i, b, j) ^ (unsigned)strictly_between(a, b, j));
+  return signed_by(sd_par(t1) ^ sd_par(t2) ^ cross, dh.cc * v);
+}
+
 #ifdef __CUDACC__
 // lane `sub` of 16: its share of a single's sum over occupied orbitals
 template <class KT>

@@ -377,16 +377,25 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
         // Singles (term indices 1 .. c[2]-1, so only in a determinant's first
         // rounds) are deferred to a half-warp each: their element sums over all
         // occupied orbitals, a chain of loads that would stall a whole warp.
+        // Doubles (most terms) take one branch-free path whatever their kind.
         const bool with_singles = rb < dh.c[2];
         for (unsigned i = tid; i < tot; i += GEN_THREADS) {
-          const Exc e = decode(dh, pt, rb + sx[i]);
-          if (with_singles && e.cls == 1) {
+          const unsigned l = rb + sx[i];
+          if (with_singles && l != 0 && l < dh.c[2]) {
             sq[atomicAdd(&s_nsq, 1u)] = (unsigned short)i;
             continue;
           }
           const u64 pos = rbase[sb[i]] + i;
-          g.okeys[pos] = target_key(dh, d, e);
-          g.oamps[pos] = term_amp(dh, d, e, g.h);
+          KT key;
+          double amp;
+          if (l == 0) {
+            key = dh.key;
+            amp = dh.dterm;
+          } else {
+            amp = double_term(dh, d, pt, g.h, l, key);
+          }
+          g.okeys[pos] = key;
+          g.oamps[pos] = amp;
         }
         if (with_singles) {
           __syncthreads();

@@ -138,3 +138,32 @@ extern "C" double gh_fx32_sum(const double* a, long n, int* big) {
   fx32_value(w, L, H);
   return fx_to_double(L, H);
 }
+
+// Doubles of one source whose branch-free key and element (double_term) differ
+// in any bit from target_key / term_amp; 0 when the paths agree.
+extern "C" long gh_double_term_mismatches(const uint64_t* kw, int words) {
+  static unsigned short pt[2016];
+  pair_table(pt);
+  HamView h{g_h.N, g_h.M, g_h.P, g_h.h1.data(), g_h.V.data(), g_h.ecore};
+  long bad = 0;
+  auto run = [&](auto& d) {
+    for (unsigned l = d.h.c[2]; l < d.h.c[5]; ++l) {
+      const Exc e = decode(d.h, pt, l);
+      auto k0 = target_key(d.h, d, e);
+      const double a0 = term_amp(d.h, d, e, h);
+      decltype(k0) k1;
+      const double a1 = double_term(d.h, d, pt, h, l, k1);
+      if (!key_eq(k0, k1) || dbl_bits(a0) != dbl_bits(a1)) ++bad;
+    }
+  };
+  if (words == 1) {
+    DetInfo<u64> d;
+    setup_host(d, (u64)kw[0], g_h.M, 0.37, 0.0);
+    run(d);
+  } else {
+    DetInfo<K128> d;
+    setup_host(d, K128{kw[0], kw[1]}, g_h.M, 0.37, 0.0);
+    run(d);
+  }
+  return bad;
+}

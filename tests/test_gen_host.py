@@ -56,3 +56,34 @@ def test_decoder_matches_reference(gh, golden_in, name):
         assert np.array_equal(ko, rk), "connected set differs"
         scale = np.max(np.abs(ra))
         assert np.max(np.abs(ao - ra)) <= 1e-13 * scale + 1e-15
+
+
+def _double_term_check(gh, det, words):
+    gh.gh_double_term_mismatches.restype = C.c_long
+    gh.gh_double_term_mismatches.argtypes = [np.ctypeslib.ndpointer(np.uint64), C.c_int]
+    return gh.gh_double_term_mismatches(det, words)
+
+
+@pytest.mark.parametrize("name", SYSTEMS)
+def test_branch_free_doubles_match(gh, golden_in, name):
+    """The generation kernel computes doubles on one branch-free path; its keys and
+    elements must equal the class-by-class decoder's bit for bit."""
+    g, path = golden_in(name)
+    assert gh.gh_load(path.encode(), 2 * int(g["M"])) == 0
+    for t in range(3):
+        assert _double_term_check(gh, np.array([g["off%d_det" % t]], np.uint64), 1) == 0
+
+
+def test_branch_free_doubles_two_word_keys(gh, tmp_path):
+    from sfci_gb300 import fcidump as fd
+    M, ne = 40, 10
+    p = str(tmp_path / "d_IN")
+    fd.uhf_to_in_file(p, M, ne, 3, 4)
+    assert gh.gh_load(p.encode(), 2 * M) == 0
+    rng = np.random.default_rng(5)
+    for _ in range(3):
+        occ = list(rng.choice(np.arange(0, 2 * M, 2), ne // 2, replace=False)) + \
+              list(rng.choice(np.arange(1, 2 * M, 2), ne // 2, replace=False))
+        lo = sum(1 << int(b) for b in occ if b < 64)
+        hi = sum(1 << int(b - 64) for b in occ if b >= 64)
+        assert _double_term_check(gh, np.array([lo, hi], np.uint64), 2) == 0

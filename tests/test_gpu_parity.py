@@ -267,3 +267,30 @@ def test_restart_vector_file_round_trip(golden_in, tmp_path):
     with pytest.raises(sg.SfciError) as e:
         c.vec(10).readPsi(str(p))
     assert e.value.status == "SFCI_ERR_CAPACITY"
+
+
+def test_pass_plans_give_identical_products(golden_in):
+    """Device budgets that force 2 to 4 generation passes (planned passes with
+    recorded pass ids) and more (passes planned from the counts) must give the
+    single-pass product bit for bit: the merge sums are exact."""
+    g, path = golden_in("r28")
+    rng = np.random.default_rng(41)
+    ints, amps = _sample_vector(rng, 56, 14, 3000)
+    keys = np.array(ints, np.uint64)
+    ref = None
+    seen = []
+    for budget in (0, 1536 << 20, 1 << 30, 640 << 20, 400 << 20):
+        c = sg.Context(path, 56, 14, Nd=200000, mem_budget=budget)
+        vin = c.vec_from(keys, amps)
+        out = c.vec(2000000)
+        d = c.SpMVMtply_bucket(vin, out, 0.0, 1.0)
+        k, a = out.download()
+        seen.append(c.last_stats()["passes"])
+        if ref is None:
+            ref = (k, a, d)
+            assert seen[0] == 1
+            continue
+        assert np.array_equal(k, ref[0])
+        assert np.array_equal(a.view(np.uint64), ref[1].view(np.uint64))
+        assert close(d, ref[2])
+    assert any(2 <= p <= 4 for p in seen[1:]) and any(p > 4 for p in seen[1:]), seen

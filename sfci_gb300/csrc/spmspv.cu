@@ -813,14 +813,35 @@ __global__ void __launch_bounds__(LC_THREADS) k_leafc(LeafArgs<KT> a, const unsi
       s_ovf = 0;
     }
     __syncthreads();
-    for (u64 e = beg + tid; e < end; e += LC_THREADS) {
-      if (*(volatile unsigned*)&s_ovf) break;
-      u64 xl, xh;
-      fx_addends(a.amps[e], xl, xh, bad);
-      const KT k = a.keys[e];
-      const int s = table_slot(t.k, LC_SLOTS - 1, k, (unsigned)slot_hash(k) & (LC_SLOTS - 1), LC_PROBE);
-      if (s < 0) s_ovf = 1;
-      else fx_red(t.lo + s, t.hi + s, xl, xh);
+    // Leaves reach this tier mostly because one hot determinant (receiving up
+    // to tens of thousands of terms) makes them long, so lanes of a warp that
+    // hit the same slot first combine their addends with shuffles and one lane
+    // adds the sum: the slot sees one atomic per warp batch, not one per term.
+    // The loop is warp-uniform (its body holds warp collectives).
+    for (u64 e0 = beg + (tid & ~31); e0 < end; e0 += LC_THREADS) {
+      if (__any_sync(0xffffffffu, *(volatile unsigned*)&s_ovf != 0u)) break;
+      const u64 e = e0 + lane;
+      u64 xl = 0, xh = 0;
+      int s = -1;
+      if (e < end) {
+        fx_addends(a.amps[e], xl, xh, bad);
+        const KT k = a.keys[e];
+        s = table_slot(t.k, LC_SLOTS - 1, k, (unsigned)slot_hash(k) & (LC_SLOTS - 1), LC_PROBE);
+        if (s < 0) s_ovf = 1;
+      }
+      const unsigned grp = __match_any_sync(0xffffffffu, s >= 0 ? s : -1 - lane);
+      const bool lead = s >= 0 && lane == __ffs(grp) - 1;
+      unsigned rest = lead ? (grp & (grp - 1u)) : 0u;  // the other members, for the leader
+      while (__any_sync(0xffffffffu, rest != 0u)) {
+        const int src = rest ? __ffs(rest) - 1 : lane;
+        const u64 ol = __shfl_sync(0xffffffffu, xl, src), oh = __shfl_sync(0xffffffffu, xh, src);
+        if (rest) {
+          xl += ol;  // lo addends are below 2^44: 32 of them cannot overflow
+          xh += oh;
+          rest &= rest - 1u;
+        }
+      }
+      if (lead) fx_red(t.lo + s, t.hi + s, xl, xh);
     }
     __syncthreads();
     if (s_ovf) {

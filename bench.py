@@ -336,7 +336,7 @@ def run_gpu(args, rank, ws, local, dist):
     # DRAM bytes per generated term measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum over
     # every launch of a 56-orbital Nd=1e4 run with 4 generation passes), scaled here to a launch by the
     # terms it processes
-    ncu_bytes_per_term = {"scatter": 17.51, "partition": 50.53 * levels, "merge": 16.11}
+    ncu_bytes_per_term = {"scatter": 17.79, "partition": 50.53 * levels, "merge": 16.11}
     dom = max(prof, key=lambda k: prof[k][0])
     dms, dl = prof[dom]
     per_launch_bytes = alg[dom] / max(dl, 1)

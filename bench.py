@@ -37,8 +37,13 @@ sys.path.insert(0, ROOT)
 
 METRIC = "SpMSpV s/iter and merged terms/s at Nd=1e7; learned-screened vs plain, ΔE≤10 μEh"
 UNIT = "merged terms/s"
-M_SPATIAL, NUM_E, SEED = 28, 14, 1
 HPSI_CAP = 60000000
+# Systems of the configurations (synthetic integrals of the generator's
+# distributions): 1 is the default workload; 2 has two-word keys.
+SYSTEMS = {
+    1: dict(M=28, ne=14, seeds=(1,), text="56 spin orbitals, 14 electrons, synthetic RHF seed 1"),
+    2: dict(M=64, ne=20, seeds=(2, 3), text="128 spin orbitals, 20 electrons, synthetic UHF seeds 2 (alpha) and 3 (beta)"),
+}
 
 
 def connected_per_det(M, na, nb):
@@ -57,15 +62,30 @@ def emitted_per_det(M, na, nb):
     return 2 * dss + na * va * nb * vb + S * (ne + na - 1)
 
 
-def workload_in(cache_dir=None):
+def workload_in(sysd=SYSTEMS[1], cache_dir=None):
     from sfci_gb300 import fcidump as fd
     d = cache_dir or os.path.join(tempfile.gettempdir(), "sfci_bench")
     os.makedirs(d, exist_ok=True)
-    p = os.path.join(d, "m%d_ne%d_s%d_IN" % (M_SPATIAL, NUM_E, SEED))
+    M, ne, seeds = sysd["M"], sysd["ne"], sysd["seeds"]
+    p = os.path.join(d, "m%d_ne%d_s%s_IN" % (M, ne, "_".join(map(str, seeds))))
     if not os.path.exists(p):
-        fd.rhf_to_in_file(p + ".tmp", M_SPATIAL, NUM_E, SEED, fcidump_path=p + ".fcidump")
+        if len(seeds) == 1:
+            fd.rhf_to_in_file(p + ".tmp", M, ne, seeds[0], fcidump_path=p + ".fcidump")
+        else:
+            fd.uhf_to_in_file(p + ".tmp", M, ne, seeds[0], seeds[1], fcidump_path=p + ".fcidump")
         os.replace(p + ".tmp", p)
     return p
+
+
+def key_words(sysd):
+    return 1 if 2 * sysd["M"] <= 64 else 2
+
+
+def hf_key(sysd):
+    hf = (1 << sysd["ne"]) - 1  # lowest ne spin orbitals, alpha/beta interleaved
+    if key_words(sysd) == 1:
+        return np.array([hf], np.uint64)
+    return np.array([[hf & (2 ** 64 - 1), hf >> 64]], np.uint64)
 
 
 class ClockSampler:
@@ -133,13 +153,13 @@ def peaks():
 # CPU baseline (oracle restatement of the reference algorithm)
 # ---------------------------------------------------------------------------
 
-def cpu_baseline(path, sample_keys, sample_amps_fn, target_s=15.0, threads=None):
+def cpu_baseline(sysd, path, sample_keys, sample_amps_fn, target_s=15.0, threads=None):
     from oracle import oracle as orc
     orc.build_port()
     threads = threads or os.cpu_count() or 1
-    be = orc.PortLib(words=1)
-    be.setup(path, 2 * M_SPATIAL, NUM_E, 10 ** 7, nthread=threads)
-    C = connected_per_det(M_SPATIAL, NUM_E // 2, NUM_E // 2)
+    be = orc.PortLib(words=key_words(sysd))
+    be.setup(path, 2 * sysd["M"], sysd["ne"], 10 ** 7, nthread=threads)
+    C = connected_per_det(sysd["M"], sysd["ne"] // 2, sysd["ne"] // 2)
     n = 100
     while True:
         k, a = sample_keys[:n], sample_amps_fn(n)
@@ -190,15 +210,15 @@ def run_reference(args, rank, ws, dist):
     if rank != 0:
         return
     from oracle import oracle as orc
-    path = workload_in()
+    sysd = SYSTEMS[args.config]
+    path = workload_in(sysd)
     threads = os.cpu_count() or 1
     orc.build_port()
-    be = orc.PortLib(words=1)
-    be.setup(path, 2 * M_SPATIAL, NUM_E, args.nd, nthread=threads)
-    hf = np.array([(1 << NUM_E) - 1], np.uint64)
-    k1, a1, _ = be.spmspv(hf, np.array([1.0]), 10 ** 7, 0.0, 1.0)
+    be = orc.PortLib(words=key_words(sysd))
+    be.setup(path, 2 * sysd["M"], sysd["ne"], args.nd, nthread=threads)
+    k1, a1, _ = be.spmspv(hf_key(sysd), np.array([1.0]), 10 ** 7, 0.0, 1.0)
     order = np.argsort(-np.abs(a1), kind="stable")
-    C = connected_per_det(M_SPATIAL, NUM_E // 2, NUM_E // 2)
+    C = connected_per_det(sysd["M"], sysd["ne"] // 2, sysd["ne"] // 2)
     # size each step for ~args.ref_step_s seconds of CPU work
     n = 200
     for _ in range(6):
@@ -221,8 +241,8 @@ def run_reference(args, rank, ws, dist):
     out = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": "SpMSpV of a Krylov vector, 56 spin orbitals, 14 electrons, synthetic RHF seed 1",
-                      "num_orb": 56, "num_e": NUM_E, "Nd": args.nd, "sample_dets": n,
+           "config": {"workload": "SpMSpV of a Krylov vector, " + sysd["text"],
+                      "num_orb": 2 * sysd["M"], "num_e": sysd["ne"], "Nd": args.nd, "sample_dets": n,
                       "parallelism": "CPU, %d threads" % threads},
            "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
                             "sample": "top-%d determinants of H|HF>, one SpMSpV per step" % n},
@@ -233,11 +253,13 @@ def run_reference(args, rank, ws, dist):
 def run_gpu(args, rank, ws, local, dist):
     import sfci_gb300 as sg
     sg.load_library()
-    path = workload_in()
+    sysd = SYSTEMS[args.config]
+    path = workload_in(sysd)
     nd = args.nd
-    ctx = sg.Context(path, 2 * M_SPATIAL, NUM_E, Nd=nd, hpsi_cap=HPSI_CAP, mem_budget=args.mem_budget)
+    M, NE, W = sysd["M"], sysd["ne"], key_words(sysd)
+    ctx = sg.Context(path, 2 * M, NE, Nd=nd, hpsi_cap=HPSI_CAP, mem_budget=args.mem_budget)
     # input: v_{k+1} = top-Nd(H v_k) normalised, from |HF>, until it holds Nd dets
-    hf = np.array([(1 << NUM_E) - 1], np.uint64)
+    hf = hf_key(sysd)
     vin = ctx.vec(nd)
     vin.upload(hf, np.array([1.0]))
     tmp = ctx.vec(HPSI_CAP)
@@ -250,7 +272,7 @@ def run_gpu(args, rank, ws, local, dist):
     n_in = vin.len
     del tmp
     out = ctx.vec(HPSI_CAP)
-    C = connected_per_det(M_SPATIAL, NUM_E // 2, NUM_E // 2)
+    C = connected_per_det(M, NE // 2, NE // 2)
     T_conn = n_in * C
     for _ in range(args.warmup):
         ctx.SpMVMtply_bucket(vin, out, 0.0, 1.0)
@@ -283,15 +305,15 @@ def run_gpu(args, rank, ws, local, dist):
         import torch
         pk = torch.empty(keys_h.size, dtype=torch.int64, pin_memory=True)
         pa = torch.empty(amps_h.size, dtype=torch.float64, pin_memory=True)
-        pk.numpy()[:] = keys_h.view(np.int64)
+        pk.numpy()[:] = keys_h.reshape(-1).view(np.int64)
         pa.numpy()[:] = amps_h
-        ok = torch.empty(HPSI_CAP, dtype=torch.int64, pin_memory=True)
+        ok = torch.empty(HPSI_CAP * W, dtype=torch.int64, pin_memory=True)
         oa = torch.empty(HPSI_CAP, dtype=torch.float64, pin_memory=True)
         host = (pk.data_ptr(), pa.data_ptr(), ok.data_ptr(), oa.data_ptr())
     except Exception:
         keys_p = np.ascontiguousarray(keys_h)
         amps_p = np.ascontiguousarray(amps_h)
-        ok_np = np.zeros(HPSI_CAP, np.uint64)
+        ok_np = np.zeros(HPSI_CAP * W, np.uint64)
         oa_np = np.zeros(HPSI_CAP)
         host = (keys_p.ctypes.data, amps_p.ctypes.data, ok_np.ctypes.data, oa_np.ctypes.data)
     import ctypes as C_
@@ -308,8 +330,9 @@ def run_gpu(args, rank, ws, local, dist):
                                    C_.byref(got)) == 0
     e2e_s = (time.perf_counter() - t0) / args.steps
     e2e_s = reduce_max(dist, e2e_s, local)
-    h2d = n_in * 16
-    d2h = got.value * 16 + 8
+    tbytes = 8 * W + 8  # one determinant: key words + FP64 amplitude
+    h2d = n_in * tbytes
+    d2h = got.value * tbytes + 8
     if rank != 0:
         barrier(dist)
         return
@@ -323,9 +346,9 @@ def run_gpu(args, rank, ws, local, dist):
     levels = -(-(b - min(b, L1_BITS)) // DIGIT_BITS)
     # algorithmic bytes per phase (all launches of the timed steps)
     alg = {
-        "scatter": 16.0 * T * args.steps,                # generated (key, amp) terms written once
-        "partition": 40.0 * T * levels * args.steps,     # per level: read key (count) + read/write term (scatter)
-        "merge": (16.0 * T + 16.0 * surv) * args.steps,  # read every term once, write survivors
+        "scatter": tbytes * T * args.steps,                      # generated (key, amp) terms written once
+        "partition": (8.0 * W + 2 * tbytes) * T * levels * args.steps,  # per level: key (count), term in + out
+        "merge": (tbytes * T + tbytes * surv) * args.steps,      # read every term once, write survivors
         "count": 0.0,                                    # keys only, kept on chip
         "select": 8.0 * surv * 6 * args.steps,
         "sort": 32.0 * out_len * 7 * args.steps,
@@ -342,21 +365,21 @@ def run_gpu(args, rank, ws, local, dist):
     per_launch_bytes = alg[dom] / max(dl, 1)
     per_launch_ms = dms / max(dl, 1)
     achieved = per_launch_bytes / (per_launch_ms * 1e-3) / 1e9 if per_launch_ms > 0 else 0.0
-    traffic = (ncu_bytes_per_term[dom] * T * args.steps / max(dl, 1)) if dom in ncu_bytes_per_term else None
+    traffic = (ncu_bytes_per_term[dom] * T * args.steps / max(dl, 1)) if (dom in ncu_bytes_per_term and W == 1) \
+        else None  # measured for one-word keys
     value = T_conn * ws / (ms_max * 1e-3)
     e2e_val = T_conn * ws / e2e_s
     res = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_max, "s_per_iter": ms_max / 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "SpMSpV of a Krylov vector (top-Nd of H^k|HF>, k=%d), 56 spin orbitals, "
-                               "14 electrons, synthetic RHF seed 1" % steps_in,
-                   "num_orb": 2 * M_SPATIAL, "num_e": NUM_E, "Nd": nd, "input_dets": n_in,
-                   "connected_per_det": C, "emitted_per_det_reference": emitted_per_det(M_SPATIAL, 7, 7),
+        "config": {"workload": "SpMSpV of a Krylov vector (top-Nd of H^k|HF>, k=%d), %s" % (steps_in, sysd["text"]),
+                   "num_orb": 2 * M, "num_e": NE, "Nd": nd, "input_dets": n_in,
+                   "connected_per_det": C, "emitted_per_det_reference": emitted_per_det(M, NE // 2, NE // 2),
                    "generated_terms_per_step": T, "merged_unique_per_step": stats["unique"],
                    "survivors_per_step": surv, "output_dets": out_len,
                    "passes": stats["passes"], "leaves": stats["leaves"], "partition_levels": levels,
-                   "l2": "inputs larger than L2: %.0f GB of terms per step vs 129 MB" % (16.0 * T / 1e9),
+                   "l2": "inputs larger than L2: %.0f GB of terms per step vs 129 MB" % (tbytes * T / 1e9),
                    "parallelism": "replicas" if ws > 1 else "1 GPU"},
         "roofline": {"bound": "hbm", "kernel": kernels[dom], "phase": dom, "achieved": achieved, "peak": hbm,
                      "unit": "GB/s", "frac": achieved / hbm, "peak_source": how, "traffic": traffic,
@@ -372,7 +395,7 @@ def run_gpu(args, rank, ws, local, dist):
     if not args.no_cpu_baseline:
         keys_sorted = keys_h[np.argsort(-np.abs(amps_h), kind="stable")]
         amps_sorted = amps_h[np.argsort(-np.abs(amps_h), kind="stable")]
-        res["cpu_baseline"] = cpu_baseline(path, keys_sorted,
+        res["cpu_baseline"] = cpu_baseline(sysd, path, keys_sorted,
                                            lambda n: amps_sorted[:n] / np.linalg.norm(amps_sorted[:n]),
                                            target_s=args.cpu_seconds)
     print(json.dumps(res), flush=True)
@@ -386,6 +409,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--nd", type=int, default=1000000)
+    ap.add_argument("--config", type=int, default=1, choices=sorted(SYSTEMS),
+                    help="system: 1 = 56 spin orbitals / 14 electrons (the default workload), "
+                         "2 = 128 spin orbitals / 20 electrons with two-word keys")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-step-s", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -8,20 +8,22 @@
 //   2. per-determinant term counts -> exclusive scan -> term offsets; diagonal
 //      elements D_j (DiagCal_bit, src/bitstr.cpp:433)
 //   3. COUNT sweep: every CTA generates the target keys of a fixed contiguous
-//      slice of the term space and histograms the top 8 bits of hash(key)
-//      (one row of a [bin x CTA] count matrix, no global atomics)
+//      slice of the term space and histograms the top d0 <= 9 bits of
+//      hash(key) (one row of a [bin x CTA] count matrix, no global atomics)
 //   4. the scanned matrix gives every CTA a private write cursor per bin; bins
 //      are grouped into passes that fit the device-memory budget
 //   5. per pass, SCATTER sweep: regenerate, keep the pass's bins, stage a round
 //      of terms in shared memory sorted by bin, and write coalesced runs
-//   6. per group of bins, MSD radix partition on further hash digits (<= 9 bits,
-//      segment-aligned units, count matrix + staged coalesced writes) down to
-//      leaves of ~512 terms; then one warp per leaf merges duplicates in a
-//      private shared-memory hash table (FP64 sums, :646-731), adds the leaf's
-//      share of <v|H|v> (:674-677) and emits survivors |a| > cut (:750)
+//   6. per group of bins, MSD radix partition on further hash digits (levels
+//      of <= 9 bits, segment-aligned units, count matrix + staged coalesced
+//      writes) down to 2^b leaves, b chosen so that a leaf's expected distinct
+//      keys fit a warp table; then one warp per leaf merges duplicates in a
+//      private shared-memory hash table with exact fixed-point sums (the FP64
+//      sums of :646-731, made order-independent), adds the leaf's share of
+//      <v|H|v> (:674-677) and emits survivors |a| > cut (:750)
 //   7. top-cap of the survivors (radix select) and LSD radix sort by key (:777-793)
-// A leaf with more distinct keys than a warp table holds is merged in a
-// global-memory table instead.
+// A leaf that overflows a warp table is merged by one CTA in a 4096-slot
+// shared-memory table; one that overflows that, in a global-memory table.
 #include <algorithm>
 #include <cmath>
 #include <cstring>

@@ -158,6 +158,22 @@ int sfci_lanczos_ground(sfci_ctx* ctx, sfci_vec* v, int Nl, int restarts, double
 int sfci_minres(sfci_ctx* ctx, const sfci_vec* rhs, const sfci_vec* guess, sfci_vec* result,
                 int iters, double tol, double lambda, int* iters_done);
 
+/* ---- subspace eigenproblems ----------------------------------------------------
+ * calc_CISD (src/sparse_solver.cpp:15-114): lowest eigenpairs of H on the block
+ * spanned by ref_key (key_words words) and every determinant it connects to.
+ * `out` receives eigenvector state_idx over the whole block, keys ascending
+ * (capacity >= *block_size, which is set before the capacity check); evals
+ * [0..n_evals) the lowest eigenvalues ascending (the reference prints 10);
+ * *resid (nullable) the norm of H x - E x.  The eigenvector sign is fixed so that
+ * its largest component is positive. */
+int sfci_cisd(sfci_ctx* ctx, const uint64_t* ref_key, int state_idx, int n_evals, double* evals,
+              sfci_vec* out, double* resid, uint64_t* block_size);
+/* fci (src/dense_algo.cpp:77-124) over generateBasis (:55-74): lowest eigenvalues
+ * of H on every determinant with num_e/2 alpha and num_e/2 beta electrons
+ * (num_e even).  `ground` (nullable) receives the ground state, keys ascending;
+ * *dim (nullable) the dimension. */
+int sfci_fci(sfci_ctx* ctx, int n_evals, double* evals, sfci_vec* ground, double* resid, uint64_t* dim);
+
 /* ---- allocation-free variant (no counterpart in the reference) -----------------
  * Sparse dot product of two key-sorted vectors held in caller-owned DEVICE arrays
  * (keys: n * key_words uint64 words; amplitudes: n doubles).  The result goes to

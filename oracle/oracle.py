@@ -17,7 +17,11 @@ Two CPU backends with one interface:
 On top of either backend, ``lanczos`` restates sparse_krylov_solve_eigenval
 (src/sparse_solver.cpp:246-548) and ``minres`` restates minres_sp
 (src/minres.cpp:73-225) line by line; the generalised eigensolve is
-scipy.linalg.eigh(K, S) (Eigen's GSAES at :450 in the reference).
+scipy.linalg.eigh(K, S) (Eigen's GSAES at :450 in the reference).  ``cisd``
+restates calc_CISD (src/sparse_solver.cpp:15-114) and ``fci`` restates fci over
+generateBasis (src/dense_algo.cpp:14-124): dense blocks filled from the
+backend's OffDiagGen_bit_e and DiagCal_bit, diagonalised by numpy.linalg.eigh
+(Eigen's SelfAdjointEigenSolver in the reference; both read the lower triangle).
 """
 from __future__ import annotations
 
@@ -320,3 +324,106 @@ def minres(be, rhs, guess, iters, tol, lam, Nd):
         eta = -s * eta
         it += 1
     return x, done
+
+
+# ---------------------------------------------------------------------------
+# dense subspace diagonalisations
+# ---------------------------------------------------------------------------
+
+def _rows(be, keys):
+    """(n, words) uint64 rows of a key array."""
+    return np.ascontiguousarray(keys, dtype=np.uint64).reshape(-1, be.words)
+
+
+def _void(rows):
+    """One opaque sortable scalar per key row (byte order; a consistent total order)."""
+    r = np.ascontiguousarray(rows)
+    return r.view(np.dtype((np.void, r.shape[1] * 8))).reshape(-1)
+
+
+def _ints(rows):
+    return [int(r[0]) | (int(r[1]) << 64) if r.size > 1 else int(r[0]) for r in rows]
+
+
+def _sort_by_key(rows, amps):
+    order = sorted(range(len(rows)), key=lambda i: _ints(rows[i:i + 1])[0])
+    return rows[order], amps[order]
+
+
+def fix_sign(x):
+    """The device results' sign convention: the largest |x| (lowest index on ties) is positive."""
+    x = np.asarray(x, np.float64)
+    i = int(np.argmax(np.abs(x)))
+    return -x if x[i] < 0 else x
+
+
+def dense_block(be, basis):
+    """H restricted to ``basis`` (rows of key words), filled row by row as
+    calc_CISD does (src/sparse_solver.cpp:54-85): H[i, i] = DiagCal_bit, and
+    H[i, p] = the summed OffDiagGen_bit_e amplitudes of basis[i] that land on
+    basis[p] (summed in emission order, as its unordered_map accumulates)."""
+    basis = _rows(be, basis)
+    n = basis.shape[0]
+    bv = _void(basis)
+    order = np.argsort(bv, kind="stable")
+    sorted_v = bv[order]
+    H = np.zeros((n, n))
+    diag = be.diag(basis)
+    cap = 4000000
+    for i in range(n):
+        det = basis[i] if be.words > 1 else basis[i, 0]
+        k, a = be.offdiag(det, cap)
+        while a.size == cap:  # possibly truncated: retry wider
+            cap *= 4
+            k, a = be.offdiag(det, cap)
+        cap = max(cap if i else 0, 2 * a.size + 1024)
+        kv = _void(_rows(be, k))
+        u, inv = np.unique(kv, return_inverse=True)
+        sums = np.zeros(u.size)
+        np.add.at(sums, inv, a)
+        H[i, i] = diag[i]
+        loc = np.searchsorted(sorted_v, u)
+        ok = loc < n
+        ok[ok] = sorted_v[loc[ok]] == u[ok]
+        H[i, order[loc[ok]]] = sums[ok]
+    return H
+
+
+def cisd(be, ref_det, state_idx=0, n_evals=10):
+    """calc_CISD, restated (src/sparse_solver.cpp:15-114).  Returns (keys ascending,
+    eigenvector state_idx with fix_sign applied, the n_evals lowest eigenvalues)."""
+    ref = _rows(be, ref_det)[:1]
+    k, _ = be.offdiag(ref[0] if be.words > 1 else ref[0, 0])
+    kr = _rows(be, k)
+    # basis: ref_det, then the distinct targets in first-appearance order (:28-43)
+    _, first = np.unique(_void(kr), return_index=True)
+    basis = np.concatenate([ref, kr[np.sort(first)]])
+    H = dense_block(be, basis)
+    ev, X = np.linalg.eigh(H, UPLO="L")
+    keys, amps = _sort_by_key(basis, X[:, state_idx])
+    keys = keys if be.words > 1 else keys[:, 0]
+    return keys, fix_sign(amps), ev[:n_evals]
+
+
+def fci_basis(be, N, ne):
+    """Every determinant with ne/2 alpha (even bits) and ne/2 beta (odd bits)
+    electrons: the set comb_det keeps (src/dense_algo.cpp:14-52), keys ascending."""
+    import itertools
+    M = N // 2
+    na = nb = ne // 2
+    alphas = [sum(1 << (2 * o) for o in c) for c in itertools.combinations(range(M), na)]
+    betas = [sum(1 << (2 * o + 1) for o in c) for c in itertools.combinations(range(M), nb)]
+    dets = sorted(a | b for a in alphas for b in betas)
+    m = (1 << 64) - 1
+    rows = np.array([[d & m, d >> 64] if be.words > 1 else [d] for d in dets], dtype=np.uint64)
+    return rows
+
+
+def fci(be, N, ne, n_evals=1):
+    """fci, restated (src/dense_algo.cpp:77-124).  Returns (the n_evals lowest
+    eigenvalues, keys ascending, ground state with fix_sign applied)."""
+    basis = fci_basis(be, N, ne)
+    H = dense_block(be, basis)
+    ev, X = np.linalg.eigh(H, UPLO="L")
+    keys = basis if be.words > 1 else basis[:, 0]
+    return ev[:n_evals], keys, fix_sign(X[:, 0])

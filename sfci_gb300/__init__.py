@@ -6,7 +6,8 @@ Python mirror of the reference's operator interface, over the C ABI of
 * :class:`Context` — integrals + options; ``SpMVMtply_bucket`` (src/functions.cpp:511),
   ``calc_energy`` (:1272), ``DiagCal_bit`` (src/bitstr.cpp:433),
   ``sparse_krylov_solve_eigenval`` (src/sparse_solver.cpp:246), ``minres_sp``
-  (src/minres.cpp:73);
+  (src/minres.cpp:73), ``calc_CISD`` (src/sparse_solver.cpp:15), ``fci``
+  (src/dense_algo.cpp:77);
 * :class:`SpVec` — a device-resident ``dynVec`` (src/all.h:150) with the
   reference's method names (``dot``, ``addTwo``, ``addThree``, ``shrinkFrom``,
   ``norm``, ``normalize``, ``scalarMtply``, ``naiveCopy``, ``setZeroVec``).
@@ -89,6 +90,8 @@ def _sigs(L):
     L.sfci_vec_load.argtypes = [_vp, C.c_char_p]
     L.sfci_psi_write.argtypes = [_vp, _vp, C.c_uint64, C.c_int, C.c_char_p]
     L.sfci_psi_read.argtypes = [C.c_char_p, C.c_int, C.c_int, _vp, _vp, C.c_uint64, C.POINTER(C.c_uint64)]
+    L.sfci_cisd.argtypes = [_vp, _vp, C.c_int, C.c_int, _vp, _vp, C.POINTER(C.c_double), C.POINTER(C.c_uint64)]
+    L.sfci_fci.argtypes = [_vp, C.c_int, _vp, _vp, C.POINTER(C.c_double), C.POINTER(C.c_uint64)]
     return L
 
 
@@ -110,7 +113,7 @@ def load_library(path: str | None = None, build: bool = True):
                "sfci_vec_upload", "sfci_vec_download", "sfci_vec_copy", "sfci_vec_clear", "sfci_spmspv",
                "sfci_diag_elements", "sfci_energy", "sfci_dot", "sfci_norm", "sfci_scale", "sfci_normalize",
                "sfci_add_two", "sfci_add_three", "sfci_shrink_from", "sfci_combine", "sfci_lanczos_ground",
-               "sfci_minres", "sfci_gsaes"):
+               "sfci_minres", "sfci_gsaes", "sfci_cisd", "sfci_fci"):
         getattr(L, fn)
     _LIB = _sigs(L)
     return _LIB
@@ -265,6 +268,41 @@ class Context:
         _check(self.L.sfci_minres(self.h, rhs.h, guess.h, result.h, int(iters), float(tol), float(lam),
                                   C.byref(done)))
         return done.value
+
+    def calc_CISD(self, ref_det, state_idx: int = 0, n_evals: int = 10):
+        """calc_CISD (src/sparse_solver.cpp:15-114): eigenvector ``state_idx`` of H on
+        the block of ``ref_det`` and every determinant it connects to, keys
+        ascending, largest component positive.  Returns (SpVec, the n_evals lowest
+        eigenvalues, norm of the residual H x - E x)."""
+        key = keys_from_ints([int(ref_det)], self.words).reshape(-1)
+        occ = [b for b in range(self.num_orb) if int(ref_det) >> b & 1]
+        M = self.num_orb // 2
+        na = sum(1 for b in occ if b % 2 == 0)
+        nb = len(occ) - na
+        c2 = lambda x: x * (x - 1) // 2
+        size = (1 + na * (M - na) + nb * (M - nb) + c2(na) * c2(M - na) + c2(nb) * c2(M - nb)
+                + na * (M - na) * nb * (M - nb))
+        out = SpVec(self, max(1, size))
+        ev = np.full(max(0, int(n_evals)), np.nan)
+        r = C.c_double()
+        bs = C.c_uint64()
+        _check(self.L.sfci_cisd(self.h, _ptr(key), int(state_idx), int(n_evals), _ptr(ev), out.h, C.byref(r),
+                                C.byref(bs)))
+        return out, ev, r.value
+
+    def fci(self, n_evals: int = 1, ground: bool = True):
+        """fci (src/dense_algo.cpp:77-124): the n_evals lowest eigenvalues of H on
+        every determinant with num_e/2 electrons of each spin.  Returns (eigenvalues,
+        ground state as an SpVec or None, residual norm of the ground state)."""
+        import math
+        n = math.comb(self.num_orb // 2, self.num_e // 2) ** 2
+        g = SpVec(self, max(1, n)) if ground else None
+        ev = np.full(max(0, int(n_evals)), np.nan)
+        r = C.c_double()
+        d = C.c_uint64()
+        _check(self.L.sfci_fci(self.h, int(n_evals), _ptr(ev), g.h if g is not None else None, C.byref(r),
+                               C.byref(d)))
+        return ev, g, r.value
 
     def combine(self, dst: "SpVec", vecs, coef):
         coef = np.ascontiguousarray(coef, dtype=np.float64)

@@ -444,6 +444,25 @@ int sfci_energy(sfci_ctx* x, const sfci_vec* psi, double* E) {
   return op_energy(x->c, psi->v, E);
 }
 
+// ---- subspace eigenproblems -----------------------------------------------------
+
+int sfci_cisd(sfci_ctx* x, const uint64_t* ref_key, int state_idx, int n_evals, double* evals, sfci_vec* out,
+              double* resid, uint64_t* block_size) {
+  if (!x || !ref_key || vec_check(out) || state_idx < 0 || n_evals < 0 || (n_evals && !evals))
+    return set_error(SFCI_ERR_ARG, "bad cisd arguments");
+  if (out->v.ctx != &x->c) return set_error(SFCI_ERR_ARG, "output vector belongs to another context");
+  Ctx& c = x->c;
+  return SFCI_W(c, cisd_impl, c, (const u64*)ref_key, state_idx, n_evals, evals, out->v, resid, (u64*)block_size);
+}
+
+int sfci_fci(sfci_ctx* x, int n_evals, double* evals, sfci_vec* ground, double* resid, uint64_t* dim) {
+  if (!x || n_evals < 0 || (n_evals && !evals)) return set_error(SFCI_ERR_ARG, "bad fci arguments");
+  if (ground && (vec_check(ground) || ground->v.ctx != &x->c))
+    return set_error(SFCI_ERR_ARG, "ground vector belongs to another context");
+  Ctx& c = x->c;
+  return SFCI_W(c, fci_impl, c, n_evals, evals, ground ? &ground->v : nullptr, resid, (u64*)dim);
+}
+
 int sfci_dot(sfci_ctx* x, const sfci_vec* a, const sfci_vec* b, double* out) {
   if (!x || vec_check(a) || vec_check(b) || !out) return set_error(SFCI_ERR_ARG, "null argument");
   return op_dot(x->c, a->v, b->v, out);

@@ -18,6 +18,11 @@ template <int W> int shrink_impl(Ctx& c, Vec& dst, const Vec& src);
 template <int W> int combine_impl(Ctx& c, Vec& dst, const Vec* const* vs, const double* coef, int n);
 template <int W> int sort_vec_impl(Ctx& c, Vec& v);
 int scale_impl(Ctx& c, Vec& v, double a);
+
+// subspace eigenproblems (subspace.cu)
+template <int W> int cisd_impl(Ctx& c, const u64* ref_key, int state_idx, int n_evals, double* evals, Vec& out,
+                               double* resid, u64* block_size);
+template <int W> int fci_impl(Ctx& c, int n_evals, double* evals, Vec* ground, double* resid, u64* dim);
 int norm_impl(Ctx& c, const Vec& v, double* out);
 
 // width dispatch used by the ABI and the drivers

@@ -3,13 +3,17 @@
 Run in a checkout that has the reference tree (the x86 development container):
 
     python tests/golden/make_golden.py [REF_ROOT]
+    python tests/golden/make_golden.py --subspace [REF_ROOT]
 
 It (1) runs the reference converter ``util/convert_fcidump.py`` on small
 synthetic FCIDUMPs and stores the resulting ``_IN`` files, and (2) builds the
 reference SpMSpV sources into ``oracle/_ref/libsfci_ref.so`` and records, for a
 few synthetic systems, the outputs of DiagCal_bit, OffDiagGen_bit_e,
 SpMVMtply_bucket, calc_energy, dynVec::dot/addTwo/addThree/shrinkFrom and a
-restated Lanczos driver over those primitives.  The fixtures pin both the
+restated Lanczos driver over those primitives.  With ``--subspace`` it writes
+only the ``sub_*.npz`` fixtures: calc_CISD and fci (src/sparse_solver.cpp:15-114,
+src/dense_algo.cpp:77-124) restated by oracle.cisd / oracle.fci over the
+reference's own DiagCal_bit and OffDiagGen_bit_e.  The fixtures pin both the
 oracle restatement (oracle/sfci_port.cpp) and the GPU path; neither needs the
 reference tree afterwards.
 """
@@ -32,7 +36,8 @@ from sfci_gb300 import fcidump as fd  # noqa: E402
 from oracle import oracle as orc  # noqa: E402
 
 BUNIT = 1000000
-REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SFCI_REFERENCE_ROOT", "/root/reference")
+_ARGS = [a for a in sys.argv[1:] if not a.startswith("--")]
+REF = _ARGS[0] if _ARGS else os.environ.get("SFCI_REFERENCE_ROOT", "/root/reference")
 
 # name, kind, M, ne, seeds, Nd for the Lanczos case (0 = no Lanczos)
 SYSTEMS = [
@@ -224,5 +229,55 @@ def exact_fci(ref, N, ne, hf):
     return float(sl.eigh(H, eigvals_only=True)[0])
 
 
+# name, kind, M, ne, seeds, CISD states (empty: none), FCI (bool)
+SUBSPACE = [
+    ("c1", "rhf", 10, 10, (0,), (0, 2), False),
+    ("r16", "rhf", 16, 8, (1,), (0,), False),
+    ("u8", "uhf", 8, 6, (2, 3), (0,), True),
+    ("r8", "rhf", 8, 8, (11,), (), True),
+]
+
+
+def subspace():
+    so = orc.build_ref(REF)
+    if not so:
+        raise SystemExit("reference sources not available under %s" % REF)
+    ref = orc.RefLib(so)
+    for name, kind, M, ne, seeds, states, with_fci in SUBSPACE:
+        N = 2 * M
+        tmp = tempfile.mkdtemp()
+        try:
+            fpath = os.path.join(tmp, "sys_fcidump")
+            if kind == "rhf":
+                h, q, v, e = fd.synthetic_rhf(M, seeds[0])
+                fd.write_fcidump_rhf(fpath, h, q, v, e, ne)
+                txt = ref_convert(fpath, "-r")
+            else:
+                hs, aa, bb, ab, e = fd.synthetic_uhf(M, seeds[0], seeds[1])
+                fd.write_fcidump_uhf(fpath, hs, aa, bb, ab, e, ne)
+                txt = ref_convert(fpath, "-u")
+            inp = os.path.join(tmp, "sys_IN")
+            open(inp, "w").write(txt)
+            ref.setup(inp, N, ne, 200000, bucket_unit=BUNIT, nthread=os.cpu_count(), num_connected=2000000)
+            hf = (1 << ne) - 1
+            out = {"M": M, "ne": ne, "kind": kind, "seeds": np.array(seeds), "hf": np.uint64(hf),
+                   "in_sha256": hashlib.sha256(txt.encode()).hexdigest()}
+            for st in states:
+                k, a, ev = orc.cisd(ref, hf, st, 10)
+                out["cisd_keys"] = k
+                out["cisd%d_amps" % st] = a
+                out["cisd_evals"] = ev
+            if with_fci:
+                ev, k, a = orc.fci(ref, N, ne, 5)
+                out.update(fci_evals=ev, fci_keys=k, fci_amps=a)
+            np.savez_compressed(os.path.join(HERE, "sub_%s.npz" % name), **out)
+            print(name, {k: (v.shape if hasattr(v, "shape") else v) for k, v in out.items() if "keys" not in k})
+        finally:
+            shutil.rmtree(tmp)
+
+
 if __name__ == "__main__":
-    main()
+    if "--subspace" in sys.argv[1:]:
+        subspace()
+    else:
+        main()

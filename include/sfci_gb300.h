@@ -158,6 +158,30 @@ int sfci_lanczos_ground(sfci_ctx* ctx, sfci_vec* v, int Nl, int restarts, double
 int sfci_minres(sfci_ctx* ctx, const sfci_vec* rhs, const sfci_vec* guess, sfci_vec* result,
                 int iters, double tol, double lambda, int* iters_done);
 
+/* ---- linear (shift-invert) solver ------------------------------------------------
+ * spmspvm_bucket_linear (src/functions.cpp:858-1094) with current_idx =
+ * nbasis - 1: w = (H - lambda) in merged over the whole input (no top-Nd slice);
+ * hij[j] = <w, basis[j]> for j < nbasis (1..64), before anything is removed;
+ * out = top-out.cap of { |a| > cut } of w - hij[nb-1] basis[nb-1] - hij[nb-2]
+ * basis[nb-2], keys ascending.  An empty input gives an empty out and leaves hij
+ * as it was (:880-884). */
+int sfci_spmspv_linear(sfci_ctx* ctx, const sfci_vec* in, sfci_vec* out, double lambda,
+                       const sfci_vec* const* basis, int nbasis, double* hij);
+/* spmspvm_bucket_res_norm (src/functions.cpp:1096-1269): r = top-r.cap of the cut
+ * of merge((H - lambda) x) - b; *res = |merge((H - lambda) x) - b| before the cut. */
+int sfci_res_norm(sfci_ctx* ctx, const sfci_vec* x, sfci_vec* r, const sfci_vec* b, double lambda,
+                  double* res);
+/* sparse_krylov_solve_linear (src/sparse_solver.cpp:561-730): (H - E_t) x = b with
+ * x0 = 0, num_iter + 1 non-orthogonal Krylov vectors per restart (num_iter <= 63),
+ * least squares on the projected system, x truncated to Nd; residues[r] (nullable)
+ * receives |A x - b| after restart r. */
+int sfci_krylov_linear(sfci_ctx* ctx, const sfci_vec* b, sfci_vec* result, double target_energy,
+                       int num_iter, int num_restart, double* residues);
+/* sparse_solve_SI (src/sparse_solver.cpp:732-771): one shift-invert step; b is
+ * replaced by the normalised solution and *energy receives its calc_energy. */
+int sfci_shift_invert(sfci_ctx* ctx, sfci_vec* b, double target_energy, int num_iter, int num_restart,
+                      double* energy);
+
 /* ---- subspace eigenproblems ----------------------------------------------------
  * calc_CISD (src/sparse_solver.cpp:15-114): lowest eigenpairs of H on the block
  * spanned by ref_key (key_words words) and every determinant it connects to.

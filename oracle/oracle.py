@@ -82,6 +82,10 @@ class _Backend:
         f("sort_merge").argtypes = [_u64p, _f64p, _ui]
         f("sort_merge").restype = _ui
         f("offdiag").restype = _ui
+        f("spmspv_linear").argtypes = [_u64p, _f64p, np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS"), _ui,
+                                       _ui, C.c_double, _ui, _u64p, _f64p, _pu, _f64p]
+        f("res_norm").restype = C.c_double
+        f("res_norm").argtypes = [_u64p, _f64p, _ui, _u64p, _f64p, _ui, C.c_double, _ui, _u64p, _f64p, _pu]
         self.f = f
 
     def _k(self, keys):
@@ -176,6 +180,32 @@ class _Backend:
                               C.byref(ol))
         m = ol.value
         return self._shape(ok[: m * self.words]), oa[:m].copy()
+
+    def spmspv_linear(self, basis, cur, lam, out_cap):
+        """spmspvm_bucket_linear with input basis[cur]; basis is a list of (keys, amps).
+        Returns (keys, amps, Hij[0..len(basis)))."""
+        bk = np.concatenate([self._k(k) for k, _ in basis]) if basis else np.zeros(0, np.uint64)
+        ba = np.concatenate([np.asarray(a, np.float64) for _, a in basis])
+        bl = np.array([np.asarray(a).size for _, a in basis], np.uint32)
+        ok = np.zeros(max(out_cap, 1) * self.words, np.uint64)
+        oa = np.zeros(max(out_cap, 1))
+        ol = C.c_uint()
+        h = np.zeros(len(basis))
+        self.f("spmspv_linear")(np.ascontiguousarray(bk), np.ascontiguousarray(ba), bl, len(basis), cur, lam, out_cap,
+                                ok, oa, C.byref(ol), h)
+        m = ol.value
+        return self._shape(ok[: m * self.words]), oa[:m].copy(), h
+
+    def res_norm(self, xk, xa, bk, ba, lam, out_cap):
+        """spmspvm_bucket_res_norm: (keys, amps) of the cut, top-capped A x - b and |A x - b|."""
+        ok = np.zeros(max(out_cap, 1) * self.words, np.uint64)
+        oa = np.zeros(max(out_cap, 1))
+        ol = C.c_uint()
+        r = self.f("res_norm")(self._k(xk), np.ascontiguousarray(xa, np.float64), np.asarray(xa).size, self._k(bk),
+                               np.ascontiguousarray(ba, np.float64), np.asarray(ba).size, lam, out_cap, ok, oa,
+                               C.byref(ol))
+        m = ol.value
+        return self._shape(ok[: m * self.words]), oa[:m].copy(), r
 
     def sort_merge(self, keys, amps):
         k = self._k(keys).copy()
@@ -427,3 +457,48 @@ def fci(be, N, ne, n_evals=1):
     ev, X = np.linalg.eigh(H, UPLO="L")
     keys = basis if be.words > 1 else basis[:, 0]
     return ev[:n_evals], keys, fix_sign(X[:, 0])
+
+
+# ---------------------------------------------------------------------------
+# linear (shift-invert) solver
+# ---------------------------------------------------------------------------
+
+def krylov_linear(be, b, target_energy, num_iter, num_restart, Nd, log=None):
+    """sparse_krylov_solve_linear, restated (src/sparse_solver.cpp:561-730), on a
+    backend's spmspv_linear / res_norm / dot / norm / add_two primitives; the
+    least-squares solve is numpy.linalg.lstsq (Eigen's colPivHouseholderQr at
+    :692).  b = (keys, amps); returns (x keys, x amps, residual norms per restart)."""
+    bk, ba = np.asarray(b[0]), np.asarray(b[1], np.float64)
+    n1 = num_iter + 1
+    x = (bk[:0].copy(), np.zeros(0))
+    r0 = (bk.copy(), ba.copy())
+    hess = np.zeros((n1, n1))
+    S = np.zeros((n1, n1))
+    res_hist = []
+    for res in range(num_restart):
+        beta = be.norm(*r0)
+        V = [(r0[0].copy(), r0[1] / be.norm(*r0))]
+        if log:
+            log("initial residue: %.12g" % beta)
+        for i in range(n1):
+            wk, wa, h = be.spmspv_linear(V, i, target_energy, Nd)
+            for j in range(i, -1, -1):
+                hess[j, i] = h[j]
+                hess[i, j] = hess[j, i]
+                S[i, j] = be.dot(V[j][0], V[j][1], V[i][0], V[i][1])
+                S[j, i] = S[i, j]
+            wa = wa / be.norm(wk, wa)
+            if i < num_iter:
+                V.append((wk, wa))
+        y = np.linalg.lstsq(S @ hess[:, :num_iter], S[:, 0] * beta, rcond=None)[0]
+        # add_bucketed_vec (src/functions.cpp:807-856): sum_j y_j V_j, merged, no cut
+        ck = np.concatenate([V[j][0] for j in range(num_iter)])
+        ca = np.concatenate([V[j][1] * y[j] for j in range(num_iter)])
+        rk, ra = be.sort_merge(ck, ca)
+        x = be.add_two(x[0], x[1], Nd, rk, ra, 1.0)
+        r0k, r0a, rn = be.res_norm(x[0], x[1], bk, ba, target_energy, Nd)
+        r0 = (r0k, -r0a)
+        res_hist.append(rn)
+        if log:
+            log("residue after truncation: %.12g" % rn)
+    return x[0], x[1], np.array(res_hist)

@@ -45,6 +45,10 @@ void introsort_amp(colvec&, int);
 unsigned int merge_bucket(colvec&, unsigned int);
 FLOAT_TYPE calc_energy(const colvec&);
 void OffDiagGen_bit_e(const DET_TYPE, colvec&);
+int make_bucket(const colvec&, vector<colvec>&);
+void spmspvm_bucket_linear(const colvec&, colvec&, FLOAT_TYPE, vector<FLOAT_TYPE>&, vector<vector<colvec>>&, int,
+                           int);
+FLOAT_TYPE spmspvm_bucket_res_norm(const colvec&, colvec&, vector<colvec>&, FLOAT_TYPE, int);
 
 static std::ostringstream g_sink;
 static std::streambuf* g_saved = nullptr;
@@ -194,6 +198,43 @@ unsigned ref_sort_merge(uint64_t* k, double* a, unsigned len) {
   unsigned out;
   drain(v, k, a, &out);
   return out;
+}
+
+// spmspvm_bucket_linear (src/functions.cpp:858-1094) with input = basis vector
+// `cur` of the nb vectors given back to back (lengths blen), as the linear
+// driver calls it (src/sparse_solver.cpp:663-669); Hij[0..nb) receives the dots.
+void ref_spmspv_linear(const uint64_t* bk, const double* ba, const unsigned* blen, unsigned nb, unsigned cur,
+                       double lam, unsigned ocap, uint64_t* ok, double* oa, unsigned* olen, double* hij) {
+  std::vector<colvec> basis(nb);
+  std::vector<std::vector<colvec>> bb(nb);
+  int maxb = 0;
+  size_t off = 0;
+  for (unsigned j = 0; j < nb; ++j) {
+    basis[j].reserveMem(blen[j] ? blen[j] : 1);
+    fill(basis[j], bk + off, ba + off, blen[j]);
+    off += blen[j];
+    int m = make_bucket(basis[j], bb[j]);
+    if (m > maxb) maxb = m;
+  }
+  std::vector<FLOAT_TYPE> h(nb, 0.0);
+  colvec out(ocap);
+  spmspvm_bucket_linear(basis[cur], out, lam, h, bb, maxb, (int)cur);
+  drain(out, ok, oa, olen);
+  for (unsigned j = 0; j < nb; ++j) hij[j] = h[j];
+}
+
+// spmspvm_bucket_res_norm (src/functions.cpp:1096-1269): r = top-ocap of the cut
+// of merge((H - lam) x) - b, sorted; returns |merge((H - lam) x) - b| before the cut.
+double ref_res_norm(const uint64_t* xk, const double* xa, unsigned xl, const uint64_t* bk, const double* ba,
+                    unsigned bl, double lam, unsigned ocap, uint64_t* ok, double* oa, unsigned* olen) {
+  colvec x(xl ? xl : 1), b(bl ? bl : 1), out(ocap);
+  fill(x, xk, xa, xl);
+  fill(b, bk, ba, bl);
+  std::vector<colvec> bb;
+  int maxb = make_bucket(b, bb);
+  double r = spmspvm_bucket_res_norm(x, out, bb, lam, maxb);
+  drain(out, ok, oa, olen);
+  return r;
 }
 
 }  // extern "C"

@@ -372,6 +372,107 @@ template <class D> void shrink_from(std::vector<Term<D>>& dst, size_t cap, std::
   std::sort(dst.begin(), dst.end(), by_key<D>);
 }
 
+// merge((H - lambda) in) per hash bucket, coefficient 1 and no top-Nd slice: the
+// product that spmspvm_bucket_linear (src/functions.cpp:903-966) and
+// spmspvm_bucket_res_norm (:1161-1211) build before their bucket-level steps
+template <class D>
+std::vector<std::vector<Term<D>>> merged_product(const std::vector<Term<D>>& in, double lambda, size_t nb) {
+  const int T = g_threads;
+  auto bucket_of = [nb](D k) { return (size_t)(hash_det(k) % nb); };
+  std::vector<std::vector<Term<D>>> res((size_t)T * nb);
+#pragma omp parallel num_threads(T)
+  {
+    const int tid = omp_get_thread_num();
+#pragma omp for schedule(static, 32)
+    for (long long i = 0; i < (long long)in.size(); ++i) {
+      const D bi = in[i].k;
+      const double t = in[i].a;
+      off_diag_gen<D>(bi, t, [&](D k, double a) { res[tid + (size_t)T * bucket_of(k)].push_back({k, a}); });
+      res[tid + (size_t)T * bucket_of(bi)].push_back({bi, (diag_cal<D>(bi) - lambda) * t});
+    }
+  }
+  std::vector<std::vector<Term<D>>> local(nb);
+#pragma omp parallel for schedule(dynamic) num_threads(T)
+  for (long long b = 0; b < (long long)nb; ++b) {
+    auto& L = local[b];
+    for (int j = 0; j < T; ++j) {
+      auto& r = res[j + (size_t)T * b];
+      L.insert(L.end(), r.begin(), r.end());
+    }
+    std::sort(L.begin(), L.end(), by_key<D>);
+    L.resize(merge_runs(L, L.size()));
+  }
+  return local;
+}
+
+// make_bucket, src/functions.cpp:466-509 (same bucket function as the product)
+template <class D> std::vector<std::vector<Term<D>>> bucketed(const std::vector<Term<D>>& v, size_t nb) {
+  std::vector<std::vector<Term<D>>> out(nb);
+  for (auto& t : v) out[(size_t)(hash_det(t.k) % nb)].push_back(t);
+  for (auto& b : out) std::sort(b.begin(), b.end(), by_key<D>);
+  return out;
+}
+
+// serial cut + top-cap + key sort of the buckets (src/functions.cpp:1007-1086)
+template <class D>
+void cut_cap_sort(const std::vector<std::vector<Term<D>>>& local, size_t out_cap, std::vector<Term<D>>& out) {
+  std::vector<Term<D>> fin;
+  for (auto& L : local)
+    for (auto& t : L)
+      if (std::fabs(t.a) > kCut) fin.push_back(t);
+  std::stable_sort(fin.begin(), fin.end(), by_abs<D>);
+  size_t s0 = fin.size() < out_cap ? 0 : fin.size() - out_cap;
+  out.assign(fin.begin() + s0, fin.end());
+  std::sort(out.begin(), out.end(), by_key<D>);
+}
+
+// spmspvm_bucket_linear, src/functions.cpp:858-1094: w = (H - lambda) v_cur
+// merged; Hij[j] = <w, v_j> for j <= cur before anything is removed (:971-978);
+// w -= Hij[cur] v_cur + Hij[cur-1] v_{cur-1} bucket by bucket (:989-997); then
+// the cut, the top-cap and the key sort
+template <class D>
+void spmspv_linear(const std::vector<std::vector<Term<D>>>& basis, unsigned cur, double lambda, size_t out_cap,
+                   std::vector<Term<D>>& out, double* hij) {
+  out.clear();
+  if (basis[cur].empty()) return;  // :880-884 (Hij left as it was)
+  for (size_t j = 0; j < basis.size(); ++j) hij[j] = 0.0;
+  const size_t nb = (size_t)g_threads * 64;
+  auto local = merged_product<D>(basis[cur], lambda, nb);
+  std::vector<std::vector<std::vector<Term<D>>>> bb;
+  for (auto& v : basis) bb.push_back(bucketed<D>(v, nb));
+  for (int j = (int)cur; j >= 0; --j) {
+    double s = 0.0;
+    for (size_t b = 0; b < nb; ++b) s += dot_sorted(local[b].data(), local[b].size(), bb[j][b].data(), bb[j][b].size());
+    hij[j] = s;
+  }
+  const size_t big = ~(size_t)0;
+  for (size_t b = 0; b < nb; ++b) {
+    add_two<D>(local[b], big, bb[cur][b], -hij[cur]);
+    if (cur > 0) add_two<D>(local[b], big, bb[cur - 1][b], -hij[cur - 1]);
+  }
+  cut_cap_sort<D>(local, out_cap, out);
+}
+
+// spmspvm_bucket_res_norm, src/functions.cpp:1096-1269: w = merge((H - lambda) x)
+// - b bucket by bucket; returns |w| before the cut, out = the cut, top-capped w
+template <class D>
+double res_norm(const std::vector<Term<D>>& x, const std::vector<Term<D>>& bv, double lambda, size_t out_cap,
+                std::vector<Term<D>>& out) {
+  const size_t nb = (size_t)g_threads * 64;
+  auto local = merged_product<D>(x, lambda, nb);
+  auto bb = bucketed<D>(bv, nb);
+  const size_t big = ~(size_t)0;
+  double r = 0.0;
+  for (size_t b = 0; b < nb; ++b) {
+    add_two<D>(local[b], big, bb[b], -1.0);
+    double q = 0.0;
+    for (auto& t : local[b]) q += t.a * t.a;
+    r += q;
+  }
+  cut_cap_sort<D>(local, out_cap, out);
+  return std::sqrt(r);
+}
+
 // ---- word-array <-> determinant conversion -----------------------------------
 template <class D> D from_words(const u64* w);
 template <> u64 from_words<u64>(const u64* w) { return w[0]; }
@@ -419,6 +520,27 @@ int setup(const char* path, unsigned norb, unsigned ne, unsigned nd, unsigned nt
     std::vector<Term<D>> out;                                                                                    \
     spmspv<D>(load<D>(ik, ia, il), ocap, lam, coeff, out, dg);                                                   \
     store<D>(out, ok, oa, ol);                                                                                   \
+  }                                                                                                              \
+  extern "C" void port##W##_spmspv_linear(const u64* bk, const double* ba, const unsigned* blen, unsigned nbv,   \
+                                          unsigned cur, double lam, unsigned ocap, u64* ok, double* oa,         \
+                                          unsigned* ol, double* hij) {                                          \
+    std::vector<std::vector<Term<D>>> basis(nbv);                                                                \
+    size_t off = 0;                                                                                              \
+    for (unsigned j = 0; j < nbv; ++j) {                                                                         \
+      basis[j] = load<D>(bk + off * words<D>(), ba + off, blen[j]);                                              \
+      off += blen[j];                                                                                            \
+    }                                                                                                            \
+    std::vector<Term<D>> out;                                                                                    \
+    spmspv_linear<D>(basis, cur, lam, ocap, out, hij);                                                           \
+    store<D>(out, ok, oa, ol);                                                                                   \
+  }                                                                                                              \
+  extern "C" double port##W##_res_norm(const u64* xk, const double* xa, unsigned xl, const u64* bk,             \
+                                       const double* ba, unsigned bl, double lam, unsigned ocap, u64* ok,        \
+                                       double* oa, unsigned* ol) {                                               \
+    std::vector<Term<D>> out;                                                                                    \
+    double r = res_norm<D>(load<D>(xk, xa, xl), load<D>(bk, ba, bl), lam, ocap, out);                            \
+    store<D>(out, ok, oa, ol);                                                                                   \
+    return r;                                                                                                    \
   }                                                                                                              \
   extern "C" double port##W##_energy(const u64* k, const double* a, unsigned n) { return energy<D>(load<D>(k, a, n)); } \
   extern "C" double port##W##_dot(const u64* k1, const double* a1, unsigned l1, const u64* k2, const double* a2, \

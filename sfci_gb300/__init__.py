@@ -92,6 +92,10 @@ def _sigs(L):
     L.sfci_psi_read.argtypes = [C.c_char_p, C.c_int, C.c_int, _vp, _vp, C.c_uint64, C.POINTER(C.c_uint64)]
     L.sfci_cisd.argtypes = [_vp, _vp, C.c_int, C.c_int, _vp, _vp, C.POINTER(C.c_double), C.POINTER(C.c_uint64)]
     L.sfci_fci.argtypes = [_vp, C.c_int, _vp, _vp, C.POINTER(C.c_double), C.POINTER(C.c_uint64)]
+    L.sfci_spmspv_linear.argtypes = [_vp, _vp, _vp, C.c_double, C.POINTER(_vp), C.c_int, _vp]
+    L.sfci_res_norm.argtypes = [_vp, _vp, _vp, _vp, C.c_double, C.POINTER(C.c_double)]
+    L.sfci_krylov_linear.argtypes = [_vp, _vp, _vp, C.c_double, C.c_int, C.c_int, _vp]
+    L.sfci_shift_invert.argtypes = [_vp, _vp, C.c_double, C.c_int, C.c_int, C.POINTER(C.c_double)]
     return L
 
 
@@ -113,7 +117,8 @@ def load_library(path: str | None = None, build: bool = True):
                "sfci_vec_upload", "sfci_vec_download", "sfci_vec_copy", "sfci_vec_clear", "sfci_spmspv",
                "sfci_diag_elements", "sfci_energy", "sfci_dot", "sfci_norm", "sfci_scale", "sfci_normalize",
                "sfci_add_two", "sfci_add_three", "sfci_shrink_from", "sfci_combine", "sfci_lanczos_ground",
-               "sfci_minres", "sfci_gsaes", "sfci_cisd", "sfci_fci"):
+               "sfci_minres", "sfci_gsaes", "sfci_cisd", "sfci_fci", "sfci_spmspv_linear", "sfci_res_norm",
+               "sfci_krylov_linear", "sfci_shift_invert"):
         getattr(L, fn)
     _LIB = _sigs(L)
     return _LIB
@@ -303,6 +308,36 @@ class Context:
         _check(self.L.sfci_fci(self.h, int(n_evals), _ptr(ev), g.h if g is not None else None, C.byref(r),
                                C.byref(d)))
         return ev, g, r.value
+
+    def spmspvm_bucket_linear(self, vin: "SpVec", vout: "SpVec", lam: float, basis) -> np.ndarray:
+        """spmspvm_bucket_linear (src/functions.cpp:858): returns Hij[0..len(basis))."""
+        arr = (_vp * len(basis))(*[v.h for v in basis])
+        h = np.zeros(len(basis))
+        _check(self.L.sfci_spmspv_linear(self.h, vin.h, vout.h, float(lam), arr, len(basis), _ptr(h)))
+        return h
+
+    def spmspvm_bucket_res_norm(self, x: "SpVec", r: "SpVec", b: "SpVec", lam: float) -> float:
+        """spmspvm_bucket_res_norm (src/functions.cpp:1096): r = cut, capped A x - b;
+        returns |A x - b| before the cut."""
+        res = C.c_double()
+        _check(self.L.sfci_res_norm(self.h, x.h, r.h, b.h, float(lam), C.byref(res)))
+        return res.value
+
+    def sparse_krylov_solve_linear(self, b: "SpVec", result: "SpVec", target_energy: float, num_iter: int,
+                                   num_restart: int) -> np.ndarray:
+        """sparse_krylov_solve_linear (src/sparse_solver.cpp:561): returns |A x - b| per restart."""
+        res = np.zeros(int(num_restart))
+        _check(self.L.sfci_krylov_linear(self.h, b.h, result.h, float(target_energy), int(num_iter), int(num_restart),
+                                         _ptr(res)))
+        return res
+
+    def sparse_solve_SI(self, b: "SpVec", target_energy: float, num_iter: int, num_restart: int) -> float:
+        """sparse_solve_SI (src/sparse_solver.cpp:732): b becomes the normalised
+        shift-invert iterate; returns its energy."""
+        e = C.c_double()
+        _check(self.L.sfci_shift_invert(self.h, b.h, float(target_energy), int(num_iter), int(num_restart),
+                                        C.byref(e)))
+        return e.value
 
     def combine(self, dst: "SpVec", vecs, coef):
         coef = np.ascontiguousarray(coef, dtype=np.float64)

@@ -166,6 +166,18 @@ int op_copy(Ctx& c, Vec& dst, const Vec& src) {
   return SFCI_OK;
 }
 
+int op_spmspv_linear(Ctx& c, const Vec& in, Vec& out, double lambda, const Vec* const* basis, int nb, double* hij) {
+  int st = SFCI_W(c, spmspv_linear_impl, c, in, out, lambda, basis, nb, hij);
+  phase_collect(c);
+  return st;
+}
+
+int op_res_norm(Ctx& c, const Vec& x, Vec& r, const Vec& b, double lambda, double* res) {
+  int st = SFCI_W(c, res_norm_impl, c, x, r, b, lambda, res);
+  phase_collect(c);
+  return st;
+}
+
 }  // namespace sfci
 
 using namespace sfci;
@@ -442,6 +454,29 @@ int sfci_diag_elements(sfci_ctx* x, const uint64_t* keys, uint64_t n, double* ou
 int sfci_energy(sfci_ctx* x, const sfci_vec* psi, double* E) {
   if (!x || vec_check(psi) || !E) return set_error(SFCI_ERR_ARG, "null argument");
   return op_energy(x->c, psi->v, E);
+}
+
+// ---- linear solver products ------------------------------------------------------
+
+int sfci_spmspv_linear(sfci_ctx* x, const sfci_vec* in, sfci_vec* out, double lambda, const sfci_vec* const* basis,
+                       int nbasis, double* hij) {
+  if (!x || vec_check(in) || vec_check(out) || !basis || nbasis < 1 || nbasis > 64 || !hij)
+    return set_error(SFCI_ERR_ARG, "bad spmspv_linear arguments");
+  if (in == out) return set_error(SFCI_ERR_ARG, "spmspv_linear input and output must differ");
+  std::vector<const Vec*> bp(nbasis);
+  for (int j = 0; j < nbasis; ++j) {
+    if (vec_check(basis[j])) return SFCI_ERR_ARG;
+    if (basis[j] == out) return set_error(SFCI_ERR_ARG, "spmspv_linear output is one of the basis vectors");
+    bp[j] = &basis[j]->v;
+  }
+  return op_spmspv_linear(x->c, in->v, out->v, lambda, bp.data(), nbasis, hij);
+}
+
+int sfci_res_norm(sfci_ctx* x, const sfci_vec* xv, sfci_vec* r, const sfci_vec* b, double lambda, double* res) {
+  if (!x || vec_check(xv) || vec_check(r) || vec_check(b) || !res)
+    return set_error(SFCI_ERR_ARG, "bad res_norm arguments");
+  if (r == xv || r == b) return set_error(SFCI_ERR_ARG, "res_norm output must differ from its inputs");
+  return op_res_norm(x->c, xv->v, r->v, b->v, lambda, res);
 }
 
 // ---- subspace eigenproblems -----------------------------------------------------

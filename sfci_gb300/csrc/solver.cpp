@@ -4,7 +4,9 @@
 // sfci_lanczos_ground follows sparse_krylov_solve_eigenval
 // (src/sparse_solver.cpp:246-548) step for step; sfci_minres follows minres_sp
 // (src/minres.cpp:73-225), including its quirk of comparing the squared
-// residual with the unsquared tolerance (:211).  Every sparse-vector operation
+// residual with the unsquared tolerance (:211); sfci_krylov_linear follows
+// sparse_krylov_solve_linear (src/sparse_solver.cpp:561-730) and
+// sfci_shift_invert sparse_solve_SI (:732-771).  Every sparse-vector operation
 // runs on the GPU; only the Nl x Nl projected matrices and scalars live on the
 // host.
 #include <algorithm>
@@ -244,6 +246,147 @@ int lanczos_ground(Ctx& c, Vec& v, int Nl, int restarts, double* energies, doubl
   return SFCI_OK;
 }
 
+// ---- least squares min |A y - e|, A m x n column-major (m >= n) -----------------
+// Householder QR with column pivoting, as Eigen's colPivHouseholderQr: columns
+// whose remaining norm falls below eps * max(m, n) * |R(0,0)| are left out
+// (their y entries are zero).
+static void lstsq_qr(int m, int n, std::vector<double> A, std::vector<double> e, std::vector<double>& y) {
+  auto at = [&](int i, int j) -> double& { return A[(size_t)j * m + i]; };
+  std::vector<int> perm(n);
+  for (int j = 0; j < n; ++j) perm[j] = j;
+  std::vector<double> cn(n, 0.0);
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < m; ++i) cn[j] += at(i, j) * at(i, j);
+  int rank = 0;
+  double r00 = 0.0;
+  const int kmax = std::min(m, n);
+  for (int k = 0; k < kmax; ++k) {
+    int p = k;
+    for (int j = k + 1; j < n; ++j)
+      if (cn[j] > cn[p]) p = j;
+    if (p != k) {
+      for (int i = 0; i < m; ++i) std::swap(at(i, k), at(i, p));
+      std::swap(cn[k], cn[p]);
+      std::swap(perm[k], perm[p]);
+    }
+    double nx = 0.0;
+    for (int i = k; i < m; ++i) nx += at(i, k) * at(i, k);
+    nx = std::sqrt(nx);
+    if (k == 0) r00 = nx;
+    if (nx <= std::numeric_limits<double>::epsilon() * std::max(m, n) * r00 || nx == 0.0) break;
+    const double alpha = at(k, k) > 0 ? -nx : nx;
+    std::vector<double> v(m - k);
+    for (int i = k; i < m; ++i) v[i - k] = at(i, k);
+    v[0] -= alpha;
+    double vn = 0.0;
+    for (double t : v) vn += t * t;
+    if (vn > 0.0) {
+      for (int j = k; j < n; ++j) {
+        double d = 0.0;
+        for (int i = k; i < m; ++i) d += v[i - k] * at(i, j);
+        d = 2.0 * d / vn;
+        for (int i = k; i < m; ++i) at(i, j) -= d * v[i - k];
+      }
+      double d = 0.0;
+      for (int i = k; i < m; ++i) d += v[i - k] * e[i];
+      d = 2.0 * d / vn;
+      for (int i = k; i < m; ++i) e[i] -= d * v[i - k];
+    }
+    for (int j = k + 1; j < n; ++j) cn[j] -= at(k, j) * at(k, j);
+    rank = k + 1;
+  }
+  std::vector<double> z(n, 0.0);
+  for (int k = rank - 1; k >= 0; --k) {
+    double s = e[k];
+    for (int j = k + 1; j < rank; ++j) s -= at(k, j) * z[j];
+    z[k] = s / at(k, k);
+  }
+  y.assign(n, 0.0);
+  for (int k = 0; k < n; ++k) y[perm[k]] = z[k];
+}
+
+int krylov_linear(Ctx& c, const Vec& b, Vec& result, double target_energy, int num_iter, int num_restart,
+                  double* residues) {
+  const bool vb = c.opts.verbose != 0;
+  const uint64_t Nd = c.opts.Nd;
+  if (b.len > Nd) return set_error(SFCI_ERR_CAPACITY, "right-hand side longer than Nd");
+  const int n1 = num_iter + 1;
+  std::vector<std::unique_ptr<DVec>> V(n1);
+  for (int i = 0; i < n1; ++i) {
+    V[i].reset(new DVec);
+    TRY(V[i]->alloc(c, Nd));
+  }
+  DVec w, r0, xm, sum;
+  TRY(w.alloc(c, Nd));
+  TRY(r0.alloc(c, Nd));
+  TRY(xm.alloc(c, Nd));
+  TRY(sum.alloc(c, (uint64_t)num_iter * Nd));
+  std::vector<double> hess((size_t)n1 * n1, 0.0), S((size_t)n1 * n1, 0.0), hij(n1, 0.0);
+  auto hm = [&](int i, int j) -> double& { return hess[(size_t)j * n1 + i]; };
+  auto sm = [&](int i, int j) -> double& { return S[(size_t)j * n1 + i]; };
+  TRY(op_copy(c, r0.v, b));  // x0 = 0: r0 = b (:615-616)
+  for (int res = 0; res < num_restart; ++res) {
+    double beta = 0.0;
+    TRY(norm_of(c, r0.v, &beta));
+    TRY(op_copy(c, V[0]->v, r0.v));
+    if (beta > 0.0) TRY(scale_impl(c, V[0]->v, 1.0 / beta));
+    if (vb) printf("initial residue: %.12g\n", beta);
+    std::vector<const Vec*> bp;
+    for (int i = 0; i < n1; ++i) {
+      bp.push_back(&V[i]->v);
+      std::fill(hij.begin(), hij.end(), 0.0);
+      TRY(op_spmspv_linear(c, V[i]->v, w.v, target_energy, bp.data(), i + 1, hij.data()));
+      for (int j = i; j >= 0; --j) {
+        hm(j, i) = hij[j];
+        hm(i, j) = hij[j];
+        double d = 0.0;
+        TRY(op_dot(c, V[j]->v, V[i]->v, &d));
+        sm(i, j) = d;
+        sm(j, i) = d;
+      }
+      double wn = 0.0;
+      TRY(norm_of(c, w.v, &wn));
+      if (!(wn > 0.0)) return set_error(SFCI_ERR_NUMERIC, "linear solver: the Krylov vector vanished");
+      TRY(scale_impl(c, w.v, 1.0 / wn));
+      if (i < num_iter) TRY(op_copy(c, V[i + 1]->v, w.v));
+    }
+    // (S H_rec) y = beta S e_0 in the least-squares sense (:679-692)
+    std::vector<double> A((size_t)n1 * num_iter, 0.0), e(n1);
+    for (int i = 0; i < n1; ++i) {
+      e[i] = sm(i, 0) * beta;
+      for (int j = 0; j < num_iter; ++j) {
+        double t = 0.0;
+        for (int k = 0; k < n1; ++k) t += sm(i, k) * hm(k, j);
+        A[(size_t)j * n1 + i] = t;
+      }
+    }
+    std::vector<double> y;
+    lstsq_qr(n1, num_iter, A, e, y);
+    // x_m += V_m y: merged, no cut (add_bucketed_vec, src/functions.cpp:807-856),
+    // then addTwo's top-Nd
+    TRY(op_combine(c, sum.v, bp.data(), y.data(), num_iter));
+    TRY(op_add_two(c, xm.v, sum.v, 1.0));
+    double rn = 0.0;
+    TRY(op_res_norm(c, xm.v, r0.v, b, target_energy, &rn));
+    TRY(scale_impl(c, r0.v, -1.0));
+    if (residues) residues[res] = rn;
+    if (vb) printf("residue after truncation: %.12g\n*************************restart %d ends*************************\n",
+                   rn, res);
+  }
+  return op_copy(c, result, xm.v);
+}
+
+int shift_invert(Ctx& c, Vec& b, double target_energy, int num_iter, int num_restart, double* energy) {
+  DVec result;
+  TRY(result.alloc(c, c.opts.Nd));
+  TRY(krylov_linear(c, b, result.v, target_energy, num_iter, num_restart, nullptr));
+  TRY(op_copy(c, b, result.v));
+  double nb = 0.0;
+  TRY(norm_of(c, b, &nb));
+  if (nb > 0.0) TRY(scale_impl(c, b, 1.0 / nb));
+  return op_energy(c, b, energy);
+}
+
 int minres(Ctx& c, const Vec& rhs, const Vec& guess, Vec& result, int iters, double tol, double lambda,
            int* iters_done) {
   const uint64_t N = c.opts.Nd;
@@ -322,6 +465,21 @@ int sfci_lanczos_ground(sfci_ctx* x, sfci_vec* v, int Nl, int restarts, double* 
     return set_error(SFCI_ERR_ARG, "bad lanczos arguments");
   if (v->v.len == 0) return set_error(SFCI_ERR_ARG, "lanczos start vector is empty");
   return lanczos_ground(x->c, v->v, Nl, restarts, energies, final_e);
+}
+
+int sfci_krylov_linear(sfci_ctx* x, const sfci_vec* b, sfci_vec* result, double target_energy, int num_iter,
+                       int num_restart, double* residues) {
+  if (!x || !b || !result || num_iter < 1 || num_iter > 63 || num_restart < 1 || b == result)
+    return set_error(SFCI_ERR_ARG, "bad krylov_linear arguments");
+  if (b->v.len == 0) return set_error(SFCI_ERR_ARG, "krylov_linear right-hand side is empty");
+  return krylov_linear(x->c, b->v, result->v, target_energy, num_iter, num_restart, residues);
+}
+
+int sfci_shift_invert(sfci_ctx* x, sfci_vec* b, double target_energy, int num_iter, int num_restart, double* energy) {
+  if (!x || !b || !energy || num_iter < 1 || num_iter > 63 || num_restart < 1)
+    return set_error(SFCI_ERR_ARG, "bad shift_invert arguments");
+  if (b->v.len == 0) return set_error(SFCI_ERR_ARG, "shift_invert start vector is empty");
+  return shift_invert(x->c, b->v, target_energy, num_iter, num_restart, energy);
 }
 
 int sfci_minres(sfci_ctx* x, const sfci_vec* rhs, const sfci_vec* guess, sfci_vec* result, int iters, double tol,

@@ -53,7 +53,8 @@ constexpr unsigned LW_PROBE = 32;                 // probes before a warp table 
 constexpr unsigned LC_PROBE = 128;                // same for the second tier
 constexpr int B_MAX = 30;
 
-enum { M_COUNT = 0, M_SCATTER = 1, M_ENERGY = 2 };
+enum { M_COUNT = 0, M_SCATTER = 1, M_ENERGY = 2, M_PROJECT = 3 };
+constexpr int PROJ_MAX = 64;  // vectors of one projection sweep
 
 template <int W> struct PartIPT;
 template <> struct PartIPT<1> { static constexpr int v = 8; };
@@ -208,16 +209,20 @@ struct GenArgs {
   u64 pass_base;            // SCATTER: basem[bin_lo * G]
   KT* okeys;
   double* oamps;
-  const KT* tkeys;          // ENERGY: support table
+  const KT* tkeys;          // ENERGY / PROJECT: support table
   const double* tvals;
   unsigned tmask;
   double* epart;            // ENERGY: per-CTA partial
+  u64 nmain = ~0ull;        // determinants from nmain on contribute one term, amplitude amps[det]
+  const double* tA;         // PROJECT: [table slot][nv] amplitudes of the projected vectors
+  int nv;
+  double* ppart;            // PROJECT: [CTA][nv] partials
 };
 
 template <class KT>
 __host__ __device__ inline size_t gen_smem_bytes(int mode, unsigned nbp) {
   size_t s = al16(sizeof(DetInfo<KT>)) + al16(2016 * sizeof(unsigned short));
-  if (mode != M_ENERGY) s += al16(sizeof(uint32_t) * nbp);
+  if (mode == M_COUNT || mode == M_SCATTER) s += al16(sizeof(uint32_t) * nbp);
   if (mode == M_SCATTER)
     s += al16(sizeof(uint32_t) * nbp) + 2 * al16(sizeof(u64) * nbp) + 3 * al16(sizeof(unsigned short) * GEN_ROUND);
   return s;
@@ -232,7 +237,7 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
   off += al16(2016 * sizeof(unsigned short));
   const unsigned nbp = (MODE == M_COUNT) ? (1u << g.b1) : (g.bin_hi - g.bin_lo);
   uint32_t* hist = reinterpret_cast<uint32_t*>(smem + off);
-  off += al16(sizeof(uint32_t) * (MODE == M_ENERGY ? 0 : nbp));
+  off += al16(sizeof(uint32_t) * ((MODE == M_COUNT || MODE == M_SCATTER) ? nbp : 0));
   uint32_t* bst = reinterpret_cast<uint32_t*>(smem + off);
   u64* cur = nullptr;            // next output position of each bin
   u64* rbase = nullptr;          // this round: output position of staged item 0's bin run, per bin
@@ -255,12 +260,15 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
   __shared__ unsigned s_nsq;
   __shared__ double s_red[GEN_THREADS / 32];
   __shared__ uint32_t s_scan[GEN_THREADS / 32 + 1];
+  __shared__ double s_pacc[MODE == M_PROJECT ? PROJ_MAX : 1];
 
   const int tid = threadIdx.x, lane = tid & 31;
   const unsigned G = gridDim.x;
   fill_pair_table(pt);
-  if (MODE != M_ENERGY)
+  if (MODE == M_COUNT || MODE == M_SCATTER)
     for (unsigned b = tid; b < nbp; b += GEN_THREADS) hist[b] = 0;
+  if (MODE == M_PROJECT)
+    for (int j = tid; j < g.nv; j += GEN_THREADS) s_pacc[j] = 0.0;
   if (MODE == M_SCATTER)
     for (unsigned b = tid; b < nbp; b += GEN_THREADS)
       cur[b] = g.basem[(u64)(g.bin_lo + b) * G + blockIdx.x] - g.pass_base;
@@ -281,8 +289,9 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
   while (t0 < t1) {
     const u64 dbeg = g.doff[det], dend = g.doff[det + 1];
     if (tid < 32) det_setup_warp(d, g.keys[det], g.coeff * g.amps[det], g.diagE[det], g.lambda, g.h.M);
+    if (tid == 0 && det >= g.nmain) d.h.dterm = g.amps[det];  // a single term, as given
     __syncthreads();
-    det_fill_singles(d, tid, GEN_THREADS);
+    if (det < g.nmain) det_fill_singles(d, tid, GEN_THREADS);  // (term 0 needs no tables)
     __syncthreads();
     const DetHead<KT> dh = d.h;
     const unsigned l0 = (unsigned)(t0 - dbeg);
@@ -381,11 +390,23 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
           if (l < l1) {
             if (MODE == M_COUNT) {
               atomicAdd(&hist[(unsigned)(key_hash(target_key(dh, d, decode(dh, pt, l))) >> shift1)], 1u);
-            } else {
+            } else if (MODE == M_ENERGY) {
               const Exc e = decode(dh, pt, l);
               const KT key = target_key(dh, d, e);
               int s = table_find_global(g.tkeys, g.tmask, key);
               if (s >= 0) eacc += term_amp(dh, d, e, g.h) * __ldcg(g.tvals + s);
+            } else {
+              const Exc e = decode(dh, pt, l);
+              const KT key = target_key(dh, d, e);
+              int s = table_find_global(g.tkeys, g.tmask, key);
+              if (s >= 0) {
+                const double t = term_amp(dh, d, e, g.h);
+                const double* row = g.tA + (u64)s * g.nv;
+                for (int j = 0; j < g.nv; ++j) {
+                  const double x = __ldcg(row + j);
+                  if (x != 0.0) atomicAdd(&s_pacc[j], t * x);
+                }
+              }
             }
           }
         }
@@ -398,6 +419,10 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
   if (MODE == M_COUNT) {
     __syncthreads();
     for (unsigned b = tid; b < nbp; b += GEN_THREADS) g.cntm[(u64)b * G + blockIdx.x] = hist[b];
+  }
+  if (MODE == M_PROJECT) {
+    __syncthreads();
+    for (int j = tid; j < g.nv; j += GEN_THREADS) g.ppart[(u64)blockIdx.x * g.nv + j] = s_pacc[j];
   }
   if (MODE == M_ENERGY) {
     double v = warp_sum(eacc);
@@ -586,6 +611,7 @@ struct LeafArgs {
   double* samps;
   u64* scount;
   double* dpart;       // per-CTA <v|Hv> partials (accumulated across launches)
+  double* qpart;       // nullable: per-CTA sums of squared merged amplitudes (before the cut)
   unsigned* ovf;       // [0] = count, then leaf ids (global)
   unsigned ovf_cap;
   u64* uniq;           // merged distinct determinants (statistics)
@@ -633,11 +659,11 @@ __global__ void __launch_bounds__(LW_WARPS * 32, sizeof(KT) == 8 ? 4 : 3) k_leaf
   extern __shared__ __align__(16) unsigned char smem[];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   WTable<KT> t(smem + (sizeof(KT) + WSLOT_BYTES_EXTRA) * TW_MAX * warp, TW_MAX);
-  __shared__ double s_red[LW_WARPS];
+  __shared__ double s_red[LW_WARPS], s_rq[LW_WARPS];
   __shared__ u64 s_uq[LW_WARPS];
   const KT empty = key_empty<KT>();
   const unsigned lt = (1u << lane) - 1u;
-  double dacc = 0.0;
+  double dacc = 0.0, qacc = 0.0;
   u64 uq = 0;
   for (u64 leaf = (u64)blockIdx.x * LW_WARPS + warp; leaf < a.nleaves; leaf += (u64)gridDim.x * LW_WARPS) {
     const u64 beg = a.loff[leaf], end = a.loff[leaf + 1], n = end - beg;
@@ -709,6 +735,10 @@ __global__ void __launch_bounds__(LW_WARPS * 32, sizeof(KT) == 8 ? 4 : 3) k_leaf
       const bool used = !key_eq(k, empty);
       u64 L = 0, H = 0;
       if (used) t.value(s, L, H);
+      if (a.qpart && used) {
+        const double x = fx_to_double(L, H);
+        qacc += x * x;
+      }
       const bool keep = used && fx_survives_value(L, H, a.cut, v);
       uq += __popc(__ballot_sync(0xffffffffu, used));
       const unsigned m = __ballot_sync(0xffffffffu, keep);
@@ -726,19 +756,23 @@ __global__ void __launch_bounds__(LW_WARPS * 32, sizeof(KT) == 8 ? 4 : 3) k_leaf
     __syncwarp();
   }
   double v = warp_sum(dacc);
+  const double vq = warp_sum(qacc);
   if (lane == 0) {
     s_red[warp] = v;
+    s_rq[warp] = vq;
     s_uq[warp] = uq;
   }
   __syncthreads();
   if (tid == 0) {
-    double s = 0.0;
+    double s = 0.0, sq = 0.0;
     u64 q = 0;
     for (int w = 0; w < LW_WARPS; ++w) {
       s += s_red[w];
+      sq += s_rq[w];
       q += s_uq[w];
     }
     atomicAdd(a.dpart + blockIdx.x, s);  // one adder per slot and launch: the order stays fixed
+    if (a.qpart) atomicAdd(a.qpart + blockIdx.x, sq);
     if (q) atomicAdd(a.uniq, q);
   }
 }
@@ -754,11 +788,11 @@ __global__ void __launch_bounds__(LC_THREADS) k_leafc(LeafArgs<KT> a, const unsi
   STable<KT> t(smem, LC_SLOTS);
   __shared__ unsigned s_nuniq, s_ovf;  // s_nuniq: claimed slots, counted after the inserts
   __shared__ u64 s_sum[LC_THREADS / 32 + 1];
-  __shared__ double s_red[LC_THREADS / 32];
+  __shared__ double s_red[LC_THREADS / 32], s_rq[LC_THREADS / 32];
   __shared__ u64 s_base;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const KT empty = key_empty<KT>();
-  double dacc = 0.0;
+  double dacc = 0.0, qacc = 0.0;
   u64 uq = 0;
   unsigned bad = 0;
   for (unsigned q = blockIdx.x; q < nids; q += gridDim.x) {
@@ -827,6 +861,10 @@ __global__ void __launch_bounds__(LC_THREADS) k_leafc(LeafArgs<KT> a, const unsi
       double v;
       if (!key_eq(t.k[s], empty)) {
         ++cu;
+        if (a.qpart) {
+          const double x = t.amp(s);
+          qacc += x * x;
+        }
         if (fx_survives(t.lo[s], t.hi[s], a.cut, v)) ++c;
       }
     }
@@ -853,12 +891,20 @@ __global__ void __launch_bounds__(LC_THREADS) k_leafc(LeafArgs<KT> a, const unsi
   }
   if (bad) atomicOr(a.bad, 1u);
   double v = warp_sum(dacc);
-  if (lane == 0) s_red[warp] = v;
+  const double vq = warp_sum(qacc);
+  if (lane == 0) {
+    s_red[warp] = v;
+    s_rq[warp] = vq;
+  }
   __syncthreads();
   if (tid == 0) {
-    double s = 0.0;
-    for (int w = 0; w < LC_THREADS / 32; ++w) s += s_red[w];
+    double s = 0.0, sq = 0.0;
+    for (int w = 0; w < LC_THREADS / 32; ++w) {
+      s += s_red[w];
+      sq += s_rq[w];
+    }
     atomicAdd(a.dpart + blockIdx.x, s);
+    if (a.qpart) atomicAdd(a.qpart + blockIdx.x, sq);
     if (uq) atomicAdd(a.uniq, uq);
   }
 }
@@ -881,10 +927,10 @@ __global__ void k_big_insert(const KT* __restrict__ keys, const double* __restri
 template <class KT>
 __global__ void k_big_finish(const KT* tk, const u64* tl, const u64* th, unsigned mask, const KT* in_keys,
                              const double* in_amps, u64 ib, u64 ie, FxCut cut, KT* skeys, double* samps,
-                             u64* scount, double* dsum, u64* uniq) {
+                             u64* scount, double* dsum, u64* uniq, double* qsum) {
   const KT empty = key_empty<KT>();
   u64 gt = (u64)blockIdx.x * blockDim.x + threadIdx.x, gs = (u64)gridDim.x * blockDim.x;
-  double acc = 0.0;
+  double acc = 0.0, qacc = 0.0;
   for (u64 e = ib + gt; e < ie; e += gs) {
     int s = table_find_global(tk, mask, in_keys[e]);
     if (s >= 0) acc += fx_to_double(__ldcg(tl + s), __ldcg(th + s)) * in_amps[e];
@@ -894,6 +940,10 @@ __global__ void k_big_finish(const KT* tk, const u64* tl, const u64* th, unsigne
     KT k = ldcg_key(tk + s);
     if (key_eq(k, empty)) continue;
     atomicAdd(uniq, 1ull);
+    if (qsum) {
+      const double x = fx_to_double(__ldcg(tl + s), __ldcg(th + s));
+      qacc += x * x;
+    }
     double v = 0.0;
     if (fx_survives(__ldcg(tl + s), __ldcg(th + s), cut, v)) {
       u64 p = atomicAdd(scount, 1ull);
@@ -901,6 +951,7 @@ __global__ void k_big_finish(const KT* tk, const u64* tl, const u64* th, unsigne
       samps[p] = v;
     }
   }
+  if (qsum && qacc != 0.0) atomicAdd(qsum, qacc);
 }
 
 template <class KT>
@@ -985,14 +1036,23 @@ static int launch_gen(Ctx& c, const GenArgs<typename KeyOf<W>::T>& g, unsigned g
   return SFCI_OK;
 }
 
+__global__ void k_fill_u64(u64* p, u64 n, u64 v) {
+  for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (u64)gridDim.x * blockDim.x) p[i] = v;
+}
+
+// term counts (one term for determinants from nmain on) -> offsets, and diagonal elements
 template <int W>
-static int prep_dets(Ctx& c, const typename KeyOf<W>::T* keys, u64 n, u64** doff, double** diagE, u64* T) {
+static int prep_dets(Ctx& c, const typename KeyOf<W>::T* keys, u64 n, u64** doff, double** diagE, u64* T,
+                     u64 nmain = ~0ull) {
   u64* off = (u64*)scratch_get(c, "sp_doff", (n + 1) * sizeof(u64));
   double* dg = (double*)scratch_get(c, "sp_diag", (n ? n : 1) * sizeof(double));
   if (!off || !dg) return SFCI_ERR_NOMEM;
   unsigned grid = (unsigned)std::min<u64>((n * 32 + 255) / 256, (u64)c.sm_count * 16);
   if (grid == 0) grid = 1;
   if (n) SFCI_LAUNCH(c, k_det_prep<typename KeyOf<W>::T>, grid, 256, 0, keys, n, ham_view(c), off, dg);
+  if (nmain < n)
+    SFCI_LAUNCH(c, k_fill_u64, std::min<unsigned>((unsigned)((n - nmain + 255) / 256), c.sm_count * 8), 256, 0,
+                off + nmain, n - nmain, (u64)1);
   int st = scan_excl(c, off, off, n);
   if (st) return st;
   if ((st = read_words(c, off + n, sizeof(u64), T))) return st;
@@ -1025,8 +1085,13 @@ static int leaf_smem_config() {
   return SFCI_OK;
 }
 
+__global__ void k_scaled_copy(double* __restrict__ dst, const double* __restrict__ src, double a, u64 n) {
+  for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (u64)gridDim.x * blockDim.x)
+    dst[i] = a * src[i];
+}
+
 template <int W>
-int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, double* diag) {
+int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, double* diag, const SpExtra* ex) {
   typedef typename KeyOf<W>::T KT;
   constexpr int IPT = PartIPT<W>::v;
   for (auto& s : c.stats) s = 0;
@@ -1054,6 +1119,34 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
     ns = m;
   }
   c.stats[0] = ns;
+  // extra single terms (coef * vector entries) join the generation sources
+  // after the input determinants; the <v|Hv> share still covers the input only
+  const KT* gen_k = src_k;
+  const double* gen_a = src_a;
+  u64 ng = ns;
+  if (ex && ex->n > 0) {
+    u64 nx = 0;
+    for (int j = 0; j < ex->n; ++j) nx += ex->vecs[j]->len;
+    if (nx) {
+      KT* xk = (KT*)scratch_get(c, "sp_gen_k", (ns + nx) * sizeof(KT));
+      double* xa = (double*)scratch_get(c, "sp_gen_a", (ns + nx) * sizeof(double));
+      if (!xk || !xa) return SFCI_ERR_NOMEM;
+      SFCI_CUDA(cudaMemcpyAsync(xk, src_k, ns * sizeof(KT), cudaMemcpyDeviceToDevice, c.stream));
+      SFCI_CUDA(cudaMemcpyAsync(xa, src_a, ns * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
+      u64 o = ns;
+      for (int j = 0; j < ex->n; ++j) {
+        const Vec& v = *ex->vecs[j];
+        if (!v.len) continue;
+        SFCI_CUDA(cudaMemcpyAsync(xk + o, v.keys, v.len * sizeof(KT), cudaMemcpyDeviceToDevice, c.stream));
+        SFCI_LAUNCH(c, k_scaled_copy, std::min<unsigned>((unsigned)((v.len + 255) / 256), c.sm_count * 8), 256, 0,
+                    xa + o, (const double*)v.amps, ex->coef[j], v.len);
+        o += v.len;
+      }
+      gen_k = xk;
+      gen_a = xa;
+      ng = ns + nx;
+    }
+  }
   {
     // a merged determinant receives at most one term per input determinant
     // connected to it, i.e. at most the term count of a determinant with its
@@ -1070,7 +1163,7 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
   // 2. term offsets + diagonal elements
   u64 *doff = nullptr, T = 0;
   double* diagE = nullptr;
-  if ((st = prep_dets<W>(c, src_k, ns, &doff, &diagE, &T))) return st;
+  if ((st = prep_dets<W>(c, gen_k, ng, &doff, &diagE, &T, ns))) return st;
   c.stats[1] = T;
   // hash digits: level 1 (generation) d0 bits, then nlev partition levels.
   // 2^b leaves: the fewest (so the fewest partition levels, each a full read
@@ -1095,9 +1188,10 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
   u64* cntm = (u64*)scratch_get(c, "sp_cntm", ((u64)NB1 * G + 1) * sizeof(u64));
   if (!cntm) return SFCI_ERR_NOMEM;
   GenArgs<KT> g{};
-  g.keys = src_k;
-  g.amps = src_a;
-  g.ndet = ns;
+  g.keys = gen_k;
+  g.amps = gen_a;
+  g.ndet = ng;
+  g.nmain = ns;
   g.doff = doff;
   g.diagE = diagE;
   g.coeff = coeff;
@@ -1174,6 +1268,13 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
   if (!scount || !dpart || !ovf || !ovf2) return SFCI_ERR_NOMEM;
   SFCI_CUDA(cudaMemsetAsync(scount, 0, 4 * sizeof(u64), c.stream));
   SFCI_CUDA(cudaMemsetAsync(dpart, 0, (leafgrid + 1) * sizeof(double), c.stream));
+  // optional sum of squared merged amplitudes: per-CTA partials, then the global tier's sum
+  double* qpart = nullptr;
+  if (ex && ex->sumsq) {
+    qpart = (double*)scratch_get(c, "sp_qpart", (leafgrid + 2) * sizeof(double));
+    if (!qpart) return SFCI_ERR_NOMEM;
+    SFCI_CUDA(cudaMemsetAsync(qpart, 0, (leafgrid + 2) * sizeof(double), c.stream));
+  }
 
   // input dets grouped by global leaf (top b bits of the hash)
   const u64 NL = 1ull << b;
@@ -1348,6 +1449,7 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
       la.samps = sa;
       la.scount = scount;
       la.dpart = dpart;
+      la.qpart = qpart;
       la.ovf = ovf;
       la.ovf_cap = OVF_CAP;
       la.uniq = scount + 1;
@@ -1393,7 +1495,7 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
           gr = (unsigned)std::min<u64>((tsz + 255) / 256, (u64)c.sm_count * 8);
           SFCI_LAUNCH(c, k_big_finish<KT>, gr, 256, 0, (const KT*)bk, (const u64*)ba, (const u64*)(ba + tsz),
                       (unsigned)(tsz - 1), (const KT*)ink, (const double*)ina, (u64)ib_ie[0], (u64)ib_ie[1],
-                      la.cut, sk, sa, scount, dbig, scount + 1);
+                      la.cut, sk, sa, scount, dbig, scount + 1, qpart ? qpart + leafgrid + 1 : nullptr);
         }
       }
       if ((st = read_words(c, scount, sizeof(u64), &scount_h))) return st;
@@ -1437,6 +1539,12 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
     if (uq) c.dup_est = (double)T / (double)uq;
   }
   *diag = dl + dbig_h;
+  if (qpart) {
+    SFCI_LAUNCH(c, k_sum_parts, 1, 32, 0, (const double*)qpart, (int)leafgrid, qpart + leafgrid);
+    double q2[2] = {0.0, 0.0};
+    if ((st = read_words(c, qpart + leafgrid, 2 * sizeof(double), q2))) return st;
+    *ex->sumsq = q2[0] + q2[1];
+  }
   return SFCI_OK;
 }
 
@@ -1496,8 +1604,173 @@ int diag_elements_impl(Ctx& c, const typename KeyOf<W>::T* dkeys, u64 n, double*
   return read_words(c, diagE, n * sizeof(double), out_host);
 }
 
-template int spmspv_impl<1>(Ctx&, const Vec&, Vec&, double, double, double*);
-template int spmspv_impl<2>(Ctx&, const Vec&, Vec&, double, double, double*);
+// ---------------------------------------------------------------------------
+// projection and the linear solver's products
+// ---------------------------------------------------------------------------
+// table of the union of several vectors' keys: A[slot * nv + j] = amplitude of vector j
+template <class KT>
+__global__ void k_proj_fill(const KT* __restrict__ keys, const double* __restrict__ amps, u64 n, KT* tk,
+                            unsigned mask, double* A, int nv, int j) {
+  const KT empty = key_empty<KT>();
+  for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (u64)gridDim.x * blockDim.x) {
+    unsigned slot = (unsigned)slot_hash(keys[i]) & mask;
+    for (unsigned probe = 0; probe <= mask; ++probe) {
+      const KT prev = cas_key(&tk[slot], empty, keys[i]);
+      if (key_eq(prev, empty) || key_eq(prev, keys[i])) {
+        A[(u64)slot * nv + j] = amps[i];
+        break;
+      }
+      slot = (slot + 1) & mask;
+    }
+  }
+}
+
+// out[j] = sum over CTAs (in CTA order) of part[cta * nv + j]
+__global__ void k_proj_sum(const double* __restrict__ part, int G, int nv, double* __restrict__ out) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < nv) {
+    double s = 0.0;
+    for (int b = 0; b < G; ++b) s += __ldcg(part + (u64)b * nv + j);
+    out[j] = s;
+  }
+}
+
+// out[j] = <basis_j | (H - lambda) | src> for j < nv, summed term by term: one
+// generation sweep over src (coefficient 1) probing a table of the union of
+// the basis vectors' keys.  Equal to the dots of the merged product with each
+// basis vector (src/functions.cpp:971-978) up to summation order.
+template <int W>
+int project_impl(Ctx& c, const Vec& src, double lambda, const Vec* const* basis, int nv, double* out) {
+  typedef typename KeyOf<W>::T KT;
+  if (nv < 1 || nv > PROJ_MAX) return set_error(SFCI_ERR_ARG, "projection onto 1 to 64 vectors");
+  for (int j = 0; j < nv; ++j) out[j] = 0.0;
+  u64 nt = 0;
+  for (int j = 0; j < nv; ++j) nt += basis[j]->len;
+  if (src.len == 0 || nt == 0) return SFCI_OK;
+  u64 tsz = 64;
+  while (tsz < 2 * nt) tsz <<= 1;
+  if (tsz > (1ull << 31)) return set_error(SFCI_ERR_UNSUPPORTED, "projection table above 2^31 slots");
+  KT* tk = (KT*)scratch_get(c, "pj_tk", tsz * sizeof(KT));
+  double* A = (double*)scratch_get(c, "pj_A", tsz * nv * sizeof(double));
+  if (!tk || !A) return SFCI_ERR_NOMEM;
+  unsigned gr = (unsigned)std::min<u64>((tsz + 255) / 256, (u64)c.sm_count * 8);
+  SFCI_LAUNCH(c, k_fill_empty<KT>, gr, 256, 0, tk, (double*)nullptr, tsz);
+  SFCI_CUDA(cudaMemsetAsync(A, 0, tsz * nv * sizeof(double), c.stream));
+  for (int j = 0; j < nv; ++j) {
+    const u64 l = basis[j]->len;
+    if (!l) continue;
+    gr = (unsigned)std::min<u64>((l + 255) / 256, (u64)c.sm_count * 8);
+    SFCI_LAUNCH(c, k_proj_fill<KT>, gr, 256, 0, (const KT*)basis[j]->keys, (const double*)basis[j]->amps, l, tk,
+                (unsigned)(tsz - 1), A, nv, j);
+  }
+  int st;
+  u64 *doff = nullptr, T = 0;
+  double* diagE = nullptr;
+  if ((st = prep_dets<W>(c, (const KT*)src.keys, src.len, &doff, &diagE, &T))) return st;
+  const unsigned G = gen_grid(c, T);
+  double* part = (double*)scratch_get(c, "pj_part", ((u64)G + 1) * nv * sizeof(double));
+  if (!part) return SFCI_ERR_NOMEM;
+  GenArgs<KT> g{};
+  g.keys = (const KT*)src.keys;
+  g.amps = src.amps;
+  g.ndet = src.len;
+  g.doff = doff;
+  g.diagE = diagE;
+  g.coeff = 1.0;
+  g.lambda = lambda;
+  g.h = ham_view(c);
+  g.T = T;
+  g.b1 = 1;
+  g.tkeys = tk;
+  g.tmask = (unsigned)(tsz - 1);
+  g.tA = A;
+  g.nv = nv;
+  g.ppart = part;
+  if ((st = launch_gen<W, M_PROJECT>(c, g, G, 0))) return st;
+  SFCI_LAUNCH(c, k_proj_sum, 1, 64, 0, (const double*)part, (int)G, nv, part + (u64)G * nv);
+  return read_words(c, part + (u64)G * nv, nv * sizeof(double), out);
+}
+
+// the whole input enters the product (the linear solver's products take no top-Nd slice)
+template <int W>
+static int product_all(Ctx& c, const Vec& in, Vec& out, double lambda, const SpExtra& ex) {
+  const u64 nd = c.opts.Nd;
+  c.opts.Nd = std::max<u64>(nd, in.len);
+  double dg = 0.0;
+  const int st = spmspv_impl<W>(c, in, out, lambda, 1.0, &dg, &ex);
+  c.opts.Nd = nd;
+  return st;
+}
+
+// spmspvm_bucket_linear (src/functions.cpp:858-1094) with current_idx = nb - 1
+template <int W>
+int spmspv_linear_impl(Ctx& c, const Vec& in, Vec& out, double lambda, const Vec* const* basis, int nb, double* hij) {
+  if (in.len == 0) {  // :880-884: empty result, Hij left as it was
+    out.len = 0;
+    return SFCI_OK;
+  }
+  int st = project_impl<W>(c, in, lambda, basis, nb, hij);
+  if (st) return st;
+  SpExtra ex;
+  ex.vecs[0] = basis[nb - 1];
+  ex.coef[0] = -hij[nb - 1];
+  ex.n = 1;
+  if (nb > 1) {
+    ex.vecs[1] = basis[nb - 2];
+    ex.coef[1] = -hij[nb - 2];
+    ex.n = 2;
+  }
+  return product_all<W>(c, in, out, lambda, ex);
+}
+
+// spmspvm_bucket_res_norm (src/functions.cpp:1096-1269)
+template <int W>
+int res_norm_impl(Ctx& c, const Vec& x, Vec& r, const Vec& b, double lambda, double* res) {
+  typedef typename KeyOf<W>::T KT;
+  int st;
+  if (x.len == 0) {
+    // A x = 0: r = -b through the cut and the top-cap, |A x - b| = |b|
+    if ((st = norm_impl(c, b, res))) return st;
+    const u64 n = b.len;
+    KT* tk = (KT*)scratch_get(c, "rn_k", (n ? n : 1) * sizeof(KT));
+    double* na = (double*)scratch_get(c, "rn_n", (n ? n : 1) * sizeof(double));
+    double* ta = (double*)scratch_get(c, "rn_a", (n ? n : 1) * sizeof(double));
+    if (!tk || !na || !ta) return SFCI_ERR_NOMEM;
+    if (n) {
+      SFCI_LAUNCH(c, k_scaled_copy, std::min<unsigned>((unsigned)((n + 255) / 256), c.sm_count * 8), 256, 0, na,
+                  (const double*)b.amps, -1.0, n);
+    }
+    size_t m = 0;
+    if ((st = compact_cut<W>(c, (const KT*)b.keys, na, n, c.opts.coeff_cut, tk, ta, &m))) return st;
+    if (m > r.cap) {
+      size_t m2 = 0;
+      if ((st = top_k_stable<W>(c, tk, ta, m, r.cap, -1.0, tk, ta, &m2))) return st;
+      m = m2;
+    }
+    SFCI_CUDA(cudaMemcpyAsync(r.keys, tk, m * sizeof(KT), cudaMemcpyDeviceToDevice, c.stream));
+    SFCI_CUDA(cudaMemcpyAsync(r.amps, ta, m * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
+    r.len = m;
+    return SFCI_OK;
+  }
+  double q = 0.0;
+  SpExtra ex;
+  ex.vecs[0] = &b;
+  ex.coef[0] = -1.0;
+  ex.n = 1;
+  ex.sumsq = &q;
+  if ((st = product_all<W>(c, x, r, lambda, ex))) return st;
+  *res = std::sqrt(q);
+  return SFCI_OK;
+}
+
+template int spmspv_impl<1>(Ctx&, const Vec&, Vec&, double, double, double*, const SpExtra*);
+template int spmspv_impl<2>(Ctx&, const Vec&, Vec&, double, double, double*, const SpExtra*);
+template int project_impl<1>(Ctx&, const Vec&, double, const Vec* const*, int, double*);
+template int project_impl<2>(Ctx&, const Vec&, double, const Vec* const*, int, double*);
+template int spmspv_linear_impl<1>(Ctx&, const Vec&, Vec&, double, const Vec* const*, int, double*);
+template int spmspv_linear_impl<2>(Ctx&, const Vec&, Vec&, double, const Vec* const*, int, double*);
+template int res_norm_impl<1>(Ctx&, const Vec&, Vec&, const Vec&, double, double*);
+template int res_norm_impl<2>(Ctx&, const Vec&, Vec&, const Vec&, double, double*);
 template int energy_impl<1>(Ctx&, const Vec&, double*);
 template int energy_impl<2>(Ctx&, const Vec&, double*);
 template int diag_elements_impl<1>(Ctx&, const u64*, u64, double*);

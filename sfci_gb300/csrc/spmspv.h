@@ -6,7 +6,24 @@
 
 namespace sfci {
 
-template <int W> int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, double* diag);
+// Extra input of spmspv_impl: each listed vector enters the merge as one term
+// per entry, amplitude coef * amp (before the cut); when sumsq is set it
+// receives the sum over merged determinants of their squared amplitude, before
+// the cut.
+struct SpExtra {
+  const Vec* vecs[2] = {nullptr, nullptr};
+  double coef[2] = {0.0, 0.0};
+  int n = 0;
+  double* sumsq = nullptr;
+};
+
+template <int W> int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, double* diag,
+                                 const SpExtra* ex = nullptr);
+template <int W> int project_impl(Ctx& c, const Vec& src, double lambda, const Vec* const* basis, int nv,
+                                  double* out);
+template <int W> int spmspv_linear_impl(Ctx& c, const Vec& in, Vec& out, double lambda, const Vec* const* basis,
+                                        int nb, double* hij);
+template <int W> int res_norm_impl(Ctx& c, const Vec& x, Vec& r, const Vec& b, double lambda, double* res);
 template <int W> int energy_impl(Ctx& c, const Vec& psi, double* E);
 template <int W> int diag_elements_impl(Ctx& c, const typename KeyOf<W>::T* dkeys, u64 n, double* out_host);
 
@@ -34,5 +51,12 @@ int op_add_three(Ctx& c, Vec& v, const Vec& x, const Vec& y, const Vec& z, doubl
 int op_shrink(Ctx& c, Vec& dst, const Vec& src);
 int op_combine(Ctx& c, Vec& dst, const Vec* const* vs, const double* coef, int n);
 int op_copy(Ctx& c, Vec& dst, const Vec& src);
+int op_spmspv_linear(Ctx& c, const Vec& in, Vec& out, double lambda, const Vec* const* basis, int nb, double* hij);
+int op_res_norm(Ctx& c, const Vec& x, Vec& r, const Vec& b, double lambda, double* res);
+
+// linear Krylov driver (solver.cpp)
+int krylov_linear(Ctx& c, const Vec& b, Vec& result, double target_energy, int num_iter, int num_restart,
+                  double* residues);
+int shift_invert(Ctx& c, Vec& b, double target_energy, int num_iter, int num_restart, double* energy);
 
 }  // namespace sfci

@@ -4,6 +4,7 @@ Run in a checkout that has the reference tree (the x86 development container):
 
     python tests/golden/make_golden.py [REF_ROOT]
     python tests/golden/make_golden.py --subspace [REF_ROOT]
+    python tests/golden/make_golden.py --linear [REF_ROOT]
 
 It (1) runs the reference converter ``util/convert_fcidump.py`` on small
 synthetic FCIDUMPs and stores the resulting ``_IN`` files, and (2) builds the
@@ -13,7 +14,11 @@ SpMVMtply_bucket, calc_energy, dynVec::dot/addTwo/addThree/shrinkFrom and a
 restated Lanczos driver over those primitives.  With ``--subspace`` it writes
 only the ``sub_*.npz`` fixtures: calc_CISD and fci (src/sparse_solver.cpp:15-114,
 src/dense_algo.cpp:77-124) restated by oracle.cisd / oracle.fci over the
-reference's own DiagCal_bit and OffDiagGen_bit_e.  The fixtures pin both the
+reference's own DiagCal_bit and OffDiagGen_bit_e.  With ``--linear`` it writes
+the ``lin_*.npz`` fixtures: the reference's spmspvm_bucket_linear and
+spmspvm_bucket_res_norm (src/functions.cpp:858-1269) on golden vectors, and the
+linear Krylov driver (src/sparse_solver.cpp:561-730) restated by
+oracle.krylov_linear over them.  The fixtures pin both the
 oracle restatement (oracle/sfci_port.cpp) and the GPU path; neither needs the
 reference tree afterwards.
 """
@@ -276,8 +281,60 @@ def subspace():
             shutil.rmtree(tmp)
 
 
+def linear():
+    so = orc.build_ref(REF)
+    if not so:
+        raise SystemExit("reference sources not available under %s" % REF)
+    ref = orc.RefLib(so)
+    # (name, Nd of the products, output cap, Nd of the driver run): the RHF case's
+    # driver runs untruncated (70000 > its 63504 determinants) because spin-mirror
+    # determinants tie exactly in magnitude at a top-Nd edge and the reference
+    # breaks such ties arbitrarily; the UHF case covers the truncating driver
+    for name, Nd, cap, Nd_d in (("c1", 2000, 2000, 70000), ("u8", 1000, 600, 1000)):
+        g = dict(np.load(os.path.join(HERE, name + ".npz")))
+        M, ne, kind, seeds = int(g["M"]), int(g["ne"]), str(g["kind"]), tuple(int(x) for x in g["seeds"])
+        N = 2 * M
+        tmp = tempfile.mkdtemp()
+        try:
+            fpath = os.path.join(tmp, "sys_fcidump")
+            if kind == "rhf":
+                h, q, v, e = fd.synthetic_rhf(M, seeds[0])
+                fd.write_fcidump_rhf(fpath, h, q, v, e, ne)
+                txt = ref_convert(fpath, "-r")
+            else:
+                hs, aa, bb, ab, e = fd.synthetic_uhf(M, seeds[0], seeds[1])
+                fd.write_fcidump_uhf(fpath, hs, aa, bb, ab, e, ne)
+                txt = ref_convert(fpath, "-u")
+            inp = os.path.join(tmp, "sys_IN")
+            open(inp, "w").write(txt)
+            ref.setup(inp, N, ne, Nd, bucket_unit=BUNIT, nthread=os.cpu_count(), num_connected=2000000)
+            v1 = (g["B_in_keys"], g["B_in_amps"])
+            w = (g["w_keys"], g["w_amps"])
+            e0 = float(g["L_final_e"])
+            lam = e0 + 0.3
+            out = {"M": M, "ne": ne, "kind": kind, "seeds": np.array(seeds),
+                   "in_sha256": hashlib.sha256(txt.encode()).hexdigest(), "Nd": Nd, "cap": cap, "lam": lam,
+                   "v1_keys": v1[0], "v1_amps": v1[1], "w_keys": w[0], "w_amps": w[1]}
+            k, a, hh = ref.spmspv_linear([v1], 0, lam, cap)
+            out.update(P0_keys=k, P0_amps=a, P0_hij=hh)
+            k, a, hh = ref.spmspv_linear([v1, w], 1, lam, cap)
+            out.update(P1_keys=k, P1_amps=a, P1_hij=hh)
+            k, a, r = ref.res_norm(w[0], w[1], v1[0], v1[1], lam, cap)
+            out.update(R_keys=k, R_amps=a, R_norm=r)
+            lam_d = e0 - 0.5
+            ref.setup(inp, N, ne, Nd_d, bucket_unit=BUNIT, nthread=os.cpu_count(), num_connected=2000000)
+            xk, xa, rh = orc.krylov_linear(ref, v1, lam_d, 5, 3, Nd_d)
+            out.update(D_Nd=Nd_d, D_lam=lam_d, D_iter=5, D_restarts=3, D_keys=xk, D_amps=xa, D_res=rh)
+            np.savez_compressed(os.path.join(HERE, "lin_%s.npz" % name), **out)
+            print(name, {k: (v.shape if hasattr(v, "shape") else v) for k, v in out.items() if "keys" not in k})
+        finally:
+            shutil.rmtree(tmp)
+
+
 if __name__ == "__main__":
     if "--subspace" in sys.argv[1:]:
         subspace()
+    elif "--linear" in sys.argv[1:]:
+        linear()
     else:
         main()

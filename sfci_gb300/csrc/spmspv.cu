@@ -214,9 +214,9 @@ struct GenArgs {
   unsigned tmask;
   double* epart;            // ENERGY: per-CTA partial
   u64 nmain = ~0ull;        // determinants from nmain on contribute one term, amplitude amps[det]
-  const double* tA;         // PROJECT: [table slot][nv] amplitudes of the projected vectors
-  int nv;
-  double* ppart;            // PROJECT: [CTA][nv] partials
+  u64* plo;                 // PROJECT: exact merged amplitude of each table slot (wide
+  u64* phi;                 //   fixed point, low and high addends)
+  unsigned* pbad;           // PROJECT: a term outside the fixed-point range
 };
 
 template <class KT>
@@ -260,15 +260,12 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
   __shared__ unsigned s_nsq;
   __shared__ double s_red[GEN_THREADS / 32];
   __shared__ uint32_t s_scan[GEN_THREADS / 32 + 1];
-  __shared__ double s_pacc[MODE == M_PROJECT ? PROJ_MAX : 1];
 
   const int tid = threadIdx.x, lane = tid & 31;
   const unsigned G = gridDim.x;
   fill_pair_table(pt);
   if (MODE == M_COUNT || MODE == M_SCATTER)
     for (unsigned b = tid; b < nbp; b += GEN_THREADS) hist[b] = 0;
-  if (MODE == M_PROJECT)
-    for (int j = tid; j < g.nv; j += GEN_THREADS) s_pacc[j] = 0.0;
   if (MODE == M_SCATTER)
     for (unsigned b = tid; b < nbp; b += GEN_THREADS)
       cur[b] = g.basem[(u64)(g.bin_lo + b) * G + blockIdx.x] - g.pass_base;
@@ -284,9 +281,71 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
   }
   __syncthreads();
   double eacc = 0.0;
+  unsigned pbad = 0;
   const int shift1 = 64 - g.b1;
   u64 det = (t0 < t1) ? s_det : 0;
   while (t0 < t1) {
+    if ((MODE == M_COUNT || MODE == M_SCATTER) && det >= g.nmain) {
+      // The rest of the slice belongs to single-term extra sources (they follow
+      // the input determinants): term t is source nmain + (t - doff[nmain]).
+      // Whole rounds of them, with no per-source set-up, so that a slice holding
+      // many of them costs what a slice of ordinary terms does.
+      const u64 Tm = g.doff[g.nmain];
+      for (u64 rb = t0; rb < t1; rb += GEN_ROUND) {
+        if (MODE == M_SCATTER) {
+          unsigned br[GEN_IPT];
+#pragma unroll
+          for (int it = 0; it < GEN_IPT; ++it) {
+            const u64 t = rb + (u64)it * GEN_THREADS + tid;
+            br[it] = ~0u;
+            if (t < t1) {
+              const unsigned bin = (unsigned)(key_hash(g.keys[g.nmain + (t - Tm)]) >> shift1);
+              if (bin >= g.bin_lo && bin < g.bin_hi) {
+                const unsigned lb = bin - g.bin_lo;
+                br[it] = (atomicAdd(&hist[lb], 1u) << 16) | lb;
+              }
+            }
+          }
+          __syncthreads();
+          uint32_t cnt = 0;
+          if (tid < (int)nbp) {
+            cnt = hist[tid];
+            hist[tid] = 0;
+          }
+          uint32_t tot;
+          const uint32_t ex = block_excl_scan<uint32_t, GEN_THREADS>(cnt, &tot, s_scan);
+          if (tid < (int)nbp) {
+            bst[tid] = ex;
+            rbase[tid] = cur[tid] - ex;
+            cur[tid] += cnt;
+          }
+          __syncthreads();
+#pragma unroll
+          for (int it = 0; it < GEN_IPT; ++it) {
+            if (br[it] != ~0u) {
+              const unsigned lb = br[it] & 0xffffu, p = bst[lb] + (br[it] >> 16);
+              sx[p] = (unsigned short)(it * GEN_THREADS + tid);
+              sb[p] = (unsigned short)lb;
+            }
+          }
+          __syncthreads();
+          // (the next round writes rbase, sx and sb only after its first barrier)
+          for (unsigned i = tid; i < tot; i += GEN_THREADS) {
+            const u64 src = g.nmain + (rb + sx[i] - Tm);
+            const u64 pos = rbase[sb[i]] + i;
+            g.okeys[pos] = g.keys[src];
+            g.oamps[pos] = g.amps[src];
+          }
+        } else {
+#pragma unroll
+          for (int it = 0; it < GEN_IPT; ++it) {
+            const u64 t = rb + (u64)it * GEN_THREADS + tid;
+            if (t < t1) atomicAdd(&hist[(unsigned)(key_hash(g.keys[g.nmain + (t - Tm)]) >> shift1)], 1u);
+          }
+        }
+      }
+      break;
+    }
     const u64 dbeg = g.doff[det], dend = g.doff[det + 1];
     if (tid < 32) det_setup_warp(d, g.keys[det], g.coeff * g.amps[det], g.diagE[det], g.lambda, g.h.M);
     if (tid == 0 && det >= g.nmain) d.h.dterm = g.amps[det];  // a single term, as given
@@ -395,18 +454,17 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
               const KT key = target_key(dh, d, e);
               int s = table_find_global(g.tkeys, g.tmask, key);
               if (s >= 0) eacc += term_amp(dh, d, e, g.h) * __ldcg(g.tvals + s);
-            } else {
-              const Exc e = decode(dh, pt, l);
-              const KT key = target_key(dh, d, e);
-              int s = table_find_global(g.tkeys, g.tmask, key);
-              if (s >= 0) {
-                const double t = term_amp(dh, d, e, g.h);
-                const double* row = g.tA + (u64)s * g.nv;
-                for (int j = 0; j < g.nv; ++j) {
-                  const double x = __ldcg(row + j);
-                  if (x != 0.0) atomicAdd(&s_pacc[j], t * x);
-                }
-              }
+            }
+          }
+          if (MODE == M_PROJECT && l < l1) {
+            // a term landing on the projected vectors' support joins that key's
+            // exact merged amplitude
+            const Exc e = decode(dh, pt, l);
+            const int s = table_find_global(g.tkeys, g.tmask, target_key(dh, d, e));
+            if (s >= 0) {
+              u64 xl, xh;
+              fx_addends(term_amp(dh, d, e, g.h), xl, xh, pbad);
+              fx_red(g.plo + s, g.phi + s, xl, xh);
             }
           }
         }
@@ -420,10 +478,7 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
     __syncthreads();
     for (unsigned b = tid; b < nbp; b += GEN_THREADS) g.cntm[(u64)b * G + blockIdx.x] = hist[b];
   }
-  if (MODE == M_PROJECT) {
-    __syncthreads();
-    for (int j = tid; j < g.nv; j += GEN_THREADS) g.ppart[(u64)blockIdx.x * g.nv + j] = s_pacc[j];
-  }
+  if (MODE == M_PROJECT && pbad) atomicOr(g.pbad, 1u);
   if (MODE == M_ENERGY) {
     double v = warp_sum(eacc);
     if (lane == 0) s_red[tid >> 5] = v;
@@ -1028,7 +1083,9 @@ static int launch_gen(Ctx& c, const GenArgs<typename KeyOf<W>::T>& g, unsigned g
   typedef typename KeyOf<W>::T KT;
   size_t sm = gen_smem_bytes<KT>(MODE, nbp);
   static size_t configured = 0;
-  if (sm > 48 * 1024 && sm > configured) {
+  // opt in whenever the size grows: static shared memory (the projection's
+  // per-warp sums) counts against the same 48 KB default
+  if (sm > configured) {
     SFCI_CUDA(cudaFuncSetAttribute(k_gen<KT, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     configured = sm;
   }
@@ -1607,38 +1664,49 @@ int diag_elements_impl(Ctx& c, const typename KeyOf<W>::T* dkeys, u64 n, double*
 // ---------------------------------------------------------------------------
 // projection and the linear solver's products
 // ---------------------------------------------------------------------------
-// table of the union of several vectors' keys: A[slot * nv + j] = amplitude of vector j
+// table of the union of several vectors' keys
 template <class KT>
-__global__ void k_proj_fill(const KT* __restrict__ keys, const double* __restrict__ amps, u64 n, KT* tk,
-                            unsigned mask, double* A, int nv, int j) {
+__global__ void k_key_insert(const KT* __restrict__ keys, u64 n, KT* tk, unsigned mask) {
   const KT empty = key_empty<KT>();
   for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (u64)gridDim.x * blockDim.x) {
     unsigned slot = (unsigned)slot_hash(keys[i]) & mask;
     for (unsigned probe = 0; probe <= mask; ++probe) {
       const KT prev = cas_key(&tk[slot], empty, keys[i]);
-      if (key_eq(prev, empty) || key_eq(prev, keys[i])) {
-        A[(u64)slot * nv + j] = amps[i];
-        break;
-      }
+      if (key_eq(prev, empty) || key_eq(prev, keys[i])) break;
       slot = (slot + 1) & mask;
     }
   }
 }
 
-// out[j] = sum over CTAs (in CTA order) of part[cta * nv + j]
-__global__ void k_proj_sum(const double* __restrict__ part, int G, int nv, double* __restrict__ out) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j < nv) {
+// per-CTA partial of sum_k v[k] * w[k], w the exact merged amplitudes in the table
+template <class KT>
+__global__ void __launch_bounds__(256) k_proj_dot(const KT* __restrict__ keys, const double* __restrict__ amps, u64 n,
+                                                  const KT* tk, unsigned mask, const u64* plo, const u64* phi,
+                                                  double* __restrict__ part) {
+  __shared__ double s_red[8];
+  double acc = 0.0;
+  for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (u64)gridDim.x * blockDim.x) {
+    const int s = table_find_global(tk, mask, keys[i]);
+    if (s >= 0) acc += amps[i] * fx_acc_double(__ldcg(plo + s), __ldcg(phi + s));
+  }
+  acc = block_sum<256>(acc, s_red);
+  if (threadIdx.x == 0) part[blockIdx.x] = acc;
+}
+
+__global__ void k_proj_sum(const double* __restrict__ part, int G, double* __restrict__ out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
     double s = 0.0;
-    for (int b = 0; b < G; ++b) s += __ldcg(part + (u64)b * nv + j);
-    out[j] = s;
+    for (int b = 0; b < G; ++b) s += __ldcg(part + b);
+    *out = s;
   }
 }
 
-// out[j] = <basis_j | (H - lambda) | src> for j < nv, summed term by term: one
-// generation sweep over src (coefficient 1) probing a table of the union of
-// the basis vectors' keys.  Equal to the dots of the merged product with each
-// basis vector (src/functions.cpp:971-978) up to summation order.
+// out[j] = <basis_j | merge((H - lambda) src)> for j < nv (src coefficient 1):
+// one generation sweep over src merges, exactly, every term that lands on the
+// union of the basis vectors' keys into that key's accumulator (the rest of
+// the product is never stored); then each dot is one pass over its vector.
+// These are the dots of the merged product with the basis vectors that
+// src/functions.cpp:971-978 takes, up to the dots' summation order.
 template <int W>
 int project_impl(Ctx& c, const Vec& src, double lambda, const Vec* const* basis, int nv, double* out) {
   typedef typename KeyOf<W>::T KT;
@@ -1651,25 +1719,24 @@ int project_impl(Ctx& c, const Vec& src, double lambda, const Vec* const* basis,
   while (tsz < 2 * nt) tsz <<= 1;
   if (tsz > (1ull << 31)) return set_error(SFCI_ERR_UNSUPPORTED, "projection table above 2^31 slots");
   KT* tk = (KT*)scratch_get(c, "pj_tk", tsz * sizeof(KT));
-  double* A = (double*)scratch_get(c, "pj_A", tsz * nv * sizeof(double));
-  if (!tk || !A) return SFCI_ERR_NOMEM;
+  u64* acc = (u64*)scratch_get(c, "pj_acc", (2 * tsz + 1) * sizeof(u64));
+  if (!tk || !acc) return SFCI_ERR_NOMEM;
+  u64 *plo = acc, *phi = acc + tsz;
+  unsigned* bad = (unsigned*)(acc + 2 * tsz);
   unsigned gr = (unsigned)std::min<u64>((tsz + 255) / 256, (u64)c.sm_count * 8);
   SFCI_LAUNCH(c, k_fill_empty<KT>, gr, 256, 0, tk, (double*)nullptr, tsz);
-  SFCI_CUDA(cudaMemsetAsync(A, 0, tsz * nv * sizeof(double), c.stream));
+  SFCI_CUDA(cudaMemsetAsync(acc, 0, (2 * tsz + 1) * sizeof(u64), c.stream));
   for (int j = 0; j < nv; ++j) {
     const u64 l = basis[j]->len;
     if (!l) continue;
     gr = (unsigned)std::min<u64>((l + 255) / 256, (u64)c.sm_count * 8);
-    SFCI_LAUNCH(c, k_proj_fill<KT>, gr, 256, 0, (const KT*)basis[j]->keys, (const double*)basis[j]->amps, l, tk,
-                (unsigned)(tsz - 1), A, nv, j);
+    SFCI_LAUNCH(c, k_key_insert<KT>, gr, 256, 0, (const KT*)basis[j]->keys, l, tk, (unsigned)(tsz - 1));
   }
   int st;
   u64 *doff = nullptr, T = 0;
   double* diagE = nullptr;
   if ((st = prep_dets<W>(c, (const KT*)src.keys, src.len, &doff, &diagE, &T))) return st;
   const unsigned G = gen_grid(c, T);
-  double* part = (double*)scratch_get(c, "pj_part", ((u64)G + 1) * nv * sizeof(double));
-  if (!part) return SFCI_ERR_NOMEM;
   GenArgs<KT> g{};
   g.keys = (const KT*)src.keys;
   g.amps = src.amps;
@@ -1683,12 +1750,34 @@ int project_impl(Ctx& c, const Vec& src, double lambda, const Vec* const* basis,
   g.b1 = 1;
   g.tkeys = tk;
   g.tmask = (unsigned)(tsz - 1);
-  g.tA = A;
-  g.nv = nv;
-  g.ppart = part;
+  g.plo = plo;
+  g.phi = phi;
+  g.pbad = bad;
   if ((st = launch_gen<W, M_PROJECT>(c, g, G, 0))) return st;
-  SFCI_LAUNCH(c, k_proj_sum, 1, 64, 0, (const double*)part, (int)G, nv, part + (u64)G * nv);
-  return read_words(c, part + (u64)G * nv, nv * sizeof(double), out);
+  unsigned hbad = 0;
+  if ((st = read_words(c, bad, sizeof(unsigned), &hbad))) return st;
+  if (hbad)
+    return set_error(SFCI_ERR_NUMERIC,
+                     "projection term with |amplitude| >= 2^24 or not finite: outside the accumulator's range");
+  const unsigned DG = (unsigned)c.sm_count * 2;
+  double* part = (double*)scratch_get(c, "pj_part", ((u64)DG + 1) * nv * sizeof(double));
+  if (!part) return SFCI_ERR_NOMEM;
+  for (int j = 0; j < nv; ++j) {
+    const u64 l = basis[j]->len;
+    double* pj = part + (u64)j * (DG + 1);
+    if (!l) {
+      SFCI_CUDA(cudaMemsetAsync(pj + DG, 0, sizeof(double), c.stream));
+      continue;
+    }
+    const unsigned dg = (unsigned)std::min<u64>((l + 255) / 256, DG);
+    SFCI_LAUNCH(c, k_proj_dot<KT>, dg, 256, 0, (const KT*)basis[j]->keys, (const double*)basis[j]->amps, l,
+                (const KT*)tk, (unsigned)(tsz - 1), (const u64*)plo, (const u64*)phi, pj);
+    SFCI_LAUNCH(c, k_proj_sum, 1, 32, 0, (const double*)pj, (int)dg, pj + DG);
+  }
+  std::vector<double> all((u64)nv * (DG + 1));
+  if ((st = read_words(c, part, all.size() * sizeof(double), all.data()))) return st;
+  for (int j = 0; j < nv; ++j) out[j] = all[(u64)j * (DG + 1) + DG];
+  return SFCI_OK;
 }
 
 // the whole input enters the product (the linear solver's products take no top-Nd slice)

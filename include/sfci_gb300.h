@@ -49,7 +49,7 @@ typedef struct sfci_opts {
   uint64_t hpsi_cap;       /* capacity of H*v products (default 6e7, src/main.cpp:194) */
   double coeff_cut;        /* post-merge magnitude cut (default 1e-5, src/main.cpp:196) */
   uint64_t bucket_unit;    /* accepted and ignored: sizes come from prefix sums */
-  uint64_t mem_budget;     /* bytes of device scratch the SpMSpV may use (0: 85% of free) */
+  uint64_t mem_budget;     /* bytes of device scratch the SpMSpV may use (0: 90% of free) */
   int verbose;             /* 1: print the reference's progress lines */
   int reserved[7];
 } sfci_opts;

@@ -17,6 +17,7 @@
 #include <memory>
 #include <vector>
 
+#include "hostla.h"
 #include "internal.h"
 #include "spmspv.h"
 
@@ -246,65 +247,6 @@ int lanczos_ground(Ctx& c, Vec& v, int Nl, int restarts, double* energies, doubl
   return SFCI_OK;
 }
 
-// ---- least squares min |A y - e|, A m x n column-major (m >= n) -----------------
-// Householder QR with column pivoting, as Eigen's colPivHouseholderQr: columns
-// whose remaining norm falls below eps * max(m, n) * |R(0,0)| are left out
-// (their y entries are zero).
-static void lstsq_qr(int m, int n, std::vector<double> A, std::vector<double> e, std::vector<double>& y) {
-  auto at = [&](int i, int j) -> double& { return A[(size_t)j * m + i]; };
-  std::vector<int> perm(n);
-  for (int j = 0; j < n; ++j) perm[j] = j;
-  std::vector<double> cn(n, 0.0);
-  for (int j = 0; j < n; ++j)
-    for (int i = 0; i < m; ++i) cn[j] += at(i, j) * at(i, j);
-  int rank = 0;
-  double r00 = 0.0;
-  const int kmax = std::min(m, n);
-  for (int k = 0; k < kmax; ++k) {
-    int p = k;
-    for (int j = k + 1; j < n; ++j)
-      if (cn[j] > cn[p]) p = j;
-    if (p != k) {
-      for (int i = 0; i < m; ++i) std::swap(at(i, k), at(i, p));
-      std::swap(cn[k], cn[p]);
-      std::swap(perm[k], perm[p]);
-    }
-    double nx = 0.0;
-    for (int i = k; i < m; ++i) nx += at(i, k) * at(i, k);
-    nx = std::sqrt(nx);
-    if (k == 0) r00 = nx;
-    if (nx <= std::numeric_limits<double>::epsilon() * std::max(m, n) * r00 || nx == 0.0) break;
-    const double alpha = at(k, k) > 0 ? -nx : nx;
-    std::vector<double> v(m - k);
-    for (int i = k; i < m; ++i) v[i - k] = at(i, k);
-    v[0] -= alpha;
-    double vn = 0.0;
-    for (double t : v) vn += t * t;
-    if (vn > 0.0) {
-      for (int j = k; j < n; ++j) {
-        double d = 0.0;
-        for (int i = k; i < m; ++i) d += v[i - k] * at(i, j);
-        d = 2.0 * d / vn;
-        for (int i = k; i < m; ++i) at(i, j) -= d * v[i - k];
-      }
-      double d = 0.0;
-      for (int i = k; i < m; ++i) d += v[i - k] * e[i];
-      d = 2.0 * d / vn;
-      for (int i = k; i < m; ++i) e[i] -= d * v[i - k];
-    }
-    for (int j = k + 1; j < n; ++j) cn[j] -= at(k, j) * at(k, j);
-    rank = k + 1;
-  }
-  std::vector<double> z(n, 0.0);
-  for (int k = rank - 1; k >= 0; --k) {
-    double s = e[k];
-    for (int j = k + 1; j < rank; ++j) s -= at(k, j) * z[j];
-    z[k] = s / at(k, k);
-  }
-  y.assign(n, 0.0);
-  for (int k = 0; k < n; ++k) y[perm[k]] = z[k];
-}
-
 int krylov_linear(Ctx& c, const Vec& b, Vec& result, double target_energy, int num_iter, int num_restart,
                   double* residues) {
   const bool vb = c.opts.verbose != 0;
@@ -361,7 +303,7 @@ int krylov_linear(Ctx& c, const Vec& b, Vec& result, double target_energy, int n
       }
     }
     std::vector<double> y;
-    lstsq_qr(n1, num_iter, A, e, y);
+    hostla::lstsq_qr(n1, num_iter, A, e, y);
     // x_m += V_m y: merged, no cut (add_bucketed_vec, src/functions.cpp:807-856),
     // then addTwo's top-Nd
     TRY(op_combine(c, sum.v, bp.data(), y.data(), num_iter));

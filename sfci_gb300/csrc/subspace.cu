@@ -27,6 +27,7 @@
 #include "gen.cuh"
 #include "prims.cuh"
 #include "spmspv.h"
+#include "hostla.h"
 #include "table.cuh"
 
 namespace sfci {
@@ -338,121 +339,6 @@ unsigned grid_for(Ctx& c, u64 n, int threads, int per_sm) {
   return (unsigned)(g ? g : 1);
 }
 
-// ---- symmetric tridiagonal T (diagonal a[0..m), off-diagonal b[0..m-1)) ----
-
-// number of eigenvalues of T below x (Sturm sequence of the LDL^T pivots)
-int sturm_below(const std::vector<double>& a, const std::vector<double>& b, int m, double x, double pivmin) {
-  int cnt = 0;
-  double q = a[0] - x;
-  if (std::fabs(q) < pivmin) q = -pivmin;
-  if (q < 0) ++cnt;
-  for (int i = 1; i < m; ++i) {
-    q = a[i] - x - b[i - 1] * b[i - 1] / q;
-    if (std::fabs(q) < pivmin) q = -pivmin;
-    if (q < 0) ++cnt;
-  }
-  return cnt;
-}
-
-// k-th smallest eigenvalue of T by bisection inside the Gershgorin interval
-double tri_eigval(const std::vector<double>& a, const std::vector<double>& b, int m, int k, double pivmin) {
-  double lo = a[0], hi = a[0];
-  for (int i = 0; i < m; ++i) {
-    const double r = (i ? std::fabs(b[i - 1]) : 0.0) + (i + 1 < m ? std::fabs(b[i]) : 0.0);
-    lo = std::min(lo, a[i] - r);
-    hi = std::max(hi, a[i] + r);
-  }
-  const double span = hi - lo;
-  lo -= 1e-12 * span + pivmin;
-  hi += 1e-12 * span + pivmin;
-  for (int it = 0; it < 256; ++it) {
-    const double mid = 0.5 * (lo + hi);
-    if (mid <= lo || mid >= hi) break;
-    if (hi - lo <= 2.0 * DBL_EPSILON * std::max(std::fabs(lo), std::fabs(hi)) + pivmin) break;
-    if (sturm_below(a, b, m, mid, pivmin) > k) hi = mid;
-    else lo = mid;
-  }
-  return 0.5 * (lo + hi);
-}
-
-// eigenvector of T for the eigenvalue theta by inverse iteration: Gaussian
-// elimination with partial pivoting of T - theta I (upper factor with two
-// superdiagonals), three solves, each followed by orthogonalisation against the
-// eigenvectors already found
-void tri_eigvec(const std::vector<double>& a, const std::vector<double>& b, int m, double theta, double tiny,
-                const std::vector<std::vector<double>>& prev, std::vector<double>& y) {
-  std::vector<double> u0(m), u1(m, 0.0), u2(m, 0.0), L(m, 0.0);
-  std::vector<char> sw(m, 0);
-  double cd = a[0] - theta, cu = m > 1 ? b[0] : 0.0;
-  for (int i = 0; i + 1 < m; ++i) {
-    const double bi = b[i], d1 = a[i + 1] - theta, n1 = (i + 2 < m) ? b[i + 1] : 0.0;
-    if (std::fabs(cd) >= std::fabs(bi)) {
-      if (cd == 0.0) cd = tiny;
-      u0[i] = cd;
-      u1[i] = cu;
-      L[i] = bi / cd;
-      cd = d1 - L[i] * cu;
-      cu = n1;
-    } else {
-      sw[i] = 1;
-      u0[i] = bi;
-      u1[i] = d1;
-      u2[i] = n1;
-      L[i] = cd / bi;
-      const double nd = cu - L[i] * d1;
-      cu = -L[i] * n1;
-      cd = nd;
-    }
-  }
-  u0[m - 1] = (std::fabs(cd) < tiny) ? (cd < 0 ? -tiny : tiny) : cd;
-  for (int i = 0; i < m; ++i)
-    if (u0[i] == 0.0) u0[i] = tiny;
-  y.assign(m, 0.0);
-  for (int i = 0; i < m; ++i) y[i] = 1.0 + 0.01 * (double)((i * 7919) % 101) / 101.0;
-  for (int it = 0; it < 3; ++it) {
-    for (int i = 0; i + 1 < m; ++i) {
-      if (sw[i]) std::swap(y[i], y[i + 1]);
-      y[i + 1] -= L[i] * y[i];
-    }
-    for (int i = m - 1; i >= 0; --i) {
-      double s = y[i];
-      if (i + 1 < m) s -= u1[i] * y[i + 1];
-      if (i + 2 < m) s -= u2[i] * y[i + 2];
-      y[i] = s / u0[i];
-    }
-    for (const auto& p : prev) {
-      double dp = 0.0;
-      for (int i = 0; i < m; ++i) dp += p[i] * y[i];
-      for (int i = 0; i < m; ++i) y[i] -= dp * p[i];
-    }
-    double nrm = 0.0;
-    for (int i = 0; i < m; ++i) nrm += y[i] * y[i];
-    nrm = std::sqrt(nrm);
-    if (!(nrm > 0.0)) nrm = 1.0;
-    for (int i = 0; i < m; ++i) y[i] /= nrm;
-  }
-}
-
-// the nev lowest eigenpairs of T_m
-void tri_lowest(const std::vector<double>& a, const std::vector<double>& b, int m, int nev, std::vector<double>& th,
-                std::vector<std::vector<double>>& vecs) {
-  double tn = 0.0, bmax = 0.0;
-  for (int i = 0; i < m; ++i) {
-    tn = std::max(tn, std::fabs(a[i]) + (i ? std::fabs(b[i - 1]) : 0.0) + (i + 1 < m ? std::fabs(b[i]) : 0.0));
-    if (i + 1 < m) bmax = std::max(bmax, b[i] * b[i]);
-  }
-  const double pivmin = DBL_MIN * std::max(1.0, bmax);
-  const double tiny = DBL_EPSILON * std::max(tn, DBL_MIN);
-  th.assign(nev, 0.0);
-  vecs.assign(nev, std::vector<double>());
-  for (int k = 0; k < nev; ++k) th[k] = tri_eigval(a, b, m, k, pivmin);
-  std::vector<std::vector<double>> prev;
-  for (int k = 0; k < nev; ++k) {
-    tri_eigvec(a, b, m, th[k], tiny, prev, vecs[k]);
-    prev.push_back(vecs[k]);
-  }
-}
-
 }  // namespace
 
 // Lowest eigenpairs of H on the block spanned by the sorted, distinct keys
@@ -568,7 +454,7 @@ static int subspace_eigs(Ctx& c, DevArena& A, const typename KeyOf<W>::T* basis,
     const bool ended = (u64)m == n || (u64)m == mcap || beta <= 1e-13 * anorm;
     const int k = std::min(nev, m);
     if (ended || (m >= nev && m % 5 == 0)) {
-      tri_lowest(al, be, m, k, th, sv);
+      hostla::tri_lowest(al, be, m, k, th, sv);
       bool conv = k == nev;
       for (int q = 0; q < k && conv; ++q)
         if (beta * std::fabs(sv[q][m - 1]) > tol * std::max(1.0, std::fabs(th[q]))) conv = false;

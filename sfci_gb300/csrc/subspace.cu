@@ -183,7 +183,9 @@ __global__ void __launch_bounds__(SS_THREADS) k_rows(const KT* __restrict__ basi
   }
 }
 
-// y = H x on the block: one warp per row, lanes striding the row's entries
+// y = H x on the block: one warp per row, lanes striding the row's entries with
+// four independent accumulators (four index loads, gathers and FMAs in flight
+// per lane instead of one dependent chain), combined in a fixed order
 __global__ void k_csr_spmv(const u64* __restrict__ rowptr, const uint32_t* __restrict__ col,
                            const double* __restrict__ val, const double* __restrict__ diag,
                            const double* __restrict__ x, double* __restrict__ y, u64 n) {
@@ -191,9 +193,18 @@ __global__ void k_csr_spmv(const u64* __restrict__ rowptr, const uint32_t* __res
   const u64 nw = ((u64)gridDim.x * blockDim.x) >> 5;
   for (u64 w = ((u64)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n; w += nw) {
     const u64 b = rowptr[w], e = rowptr[w + 1];
-    double s = 0.0;
-    for (u64 p = b + lane; p < e; p += 32) s = fma(val[p], x[col[p]], s);
-    s = warp_sum(s);
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    u64 p = b + lane;
+    for (; p + 96 < e; p += 128) {
+      const uint32_t c0 = col[p], c1 = col[p + 32], c2 = col[p + 64], c3 = col[p + 96];
+      const double v0 = val[p], v1 = val[p + 32], v2 = val[p + 64], v3 = val[p + 96];
+      s0 = fma(v0, x[c0], s0);
+      s1 = fma(v1, x[c1], s1);
+      s2 = fma(v2, x[c2], s2);
+      s3 = fma(v3, x[c3], s3);
+    }
+    for (; p < e; p += 32) s0 = fma(val[p], x[col[p]], s0);
+    const double s = warp_sum((s0 + s1) + (s2 + s3));
     if (lane == 0) y[w] = fma(diag[w], x[w], s);
   }
 }

@@ -46,10 +46,10 @@ REF = _ARGS[0] if _ARGS else os.environ.get("SFCI_REFERENCE_ROOT", "/root/refere
 
 # name, kind, M, ne, seeds, Nd for the Lanczos case (0 = no Lanczos)
 SYSTEMS = [
-    ("c1", "rhf", 10, 10, (0,), 20000, 20, 3),        # configs[0] of the benchmark definition
+    ("c1", "rhf", 10, 10, (0,), 20000, 20, 3),        # the 20-spin-orbital, 10-electron benchmark case
     ("u8", "uhf", 8, 6, (2, 3), 4000, 12, 3),         # small UHF, FCI dim 3136 < Nd
     ("r16", "rhf", 16, 8, (1,), 3000, 10, 2),         # wider virtual space
-    ("r28", "rhf", 28, 14, (1,), 0, 0, 0),            # configs[1] shape (SpMSpV level only)
+    ("r28", "rhf", 28, 14, (1,), 0, 0, 0),            # the 56-spin-orbital, 14-electron benchmark shape (SpMSpV level only)
 ]
 
 

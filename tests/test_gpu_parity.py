@@ -199,8 +199,8 @@ def test_128bit_keys_match_oracle(tmp_path, port):
     assert np.allclose(dd, be.diag(keys[:20]), rtol=1e-13, atol=1e-13)
 
 
-def test_full_size_properties_configs1_shape(golden_in, port):
-    """The configs[1] system (56 spin orbitals, 14 electrons) at a size where the
+def test_full_size_properties_56_orbital_system(golden_in, port):
+    """The benchmark system (56 spin orbitals, 14 electrons) at a size where the
     two-level partition is active: parity with the oracle on the same input."""
     g, path = golden_in("r28")
     rng = np.random.default_rng(9)

@@ -1,5 +1,5 @@
 """The drop-in `sfci` binary on a reference run directory (sfci.input + _IN file)
-for the configs[0] system: its printed E_hf, per-restart "gsaes energy" and
+for the 20-spin-orbital, 10-electron system: its printed E_hf, per-restart "gsaes energy" and
 "final e" lines against the reference driver's golden values (within 1e-8 Eh,
 the Lanczos parity bar)."""
 import os

@@ -31,6 +31,7 @@
 
 #include "gen.cuh"
 #include "prims.cuh"
+#include "plan.h"
 #include "spmspv.h"
 #include "table.cuh"
 
@@ -1286,43 +1287,10 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
   size_t budget = c.opts.mem_budget ? (size_t)c.opts.mem_budget : (size_t)((freeb + held) * 0.90);
   u64 avail = budget / tb;
   const u64 cap = out.cap;
-  // level-2 group capacity C2, survivor capacity SC (x2: a reduction of the
-  // survivors stages through a second buffer of the same size) and level-1
-  // capacity C1 (what is left).  Every generation pass regenerates all terms,
-  // so the plan takes the fewest passes first; among plans with that many, the
-  // largest level-2 groups (fewer, fuller partition and merge launches).
-  auto passes_for = [&](u64 c2, u64& c1, u64& sc) -> int {  // -1: does not fit
-    sc = std::min<u64>(cap, T) + std::min<u64>(c2, T);
-    c1 = T;
-    const u64 l2 = (nlev > 0) ? c2 : 0;
-    if (c1 + l2 + 2 * sc > avail) {
-      if (avail < l2 + 2 * sc + maxbin) return -1;
-      c1 = avail - l2 - 2 * sc;
-    }
-    if (c1 < maxbin || c2 < maxbin) return -1;
-    int np = 0;
-    for (unsigned lo = 0; lo < NB1; ++np) {
-      unsigned hi = lo + 1;
-      while (hi < NB1 && binoff[hi + 1] - binoff[lo] <= c1) ++hi;
-      lo = hi;
-    }
-    return np;
-  };
-  u64 C2 = 0, C1 = 0, SC = 0;
-  int np_best = -1;
-  for (const int div : {6, 16, 24, 32, 48, 64}) {
-    if ((nlev == 0) != (div == 6)) continue;  // no partition levels: one large group buffer
-    const u64 c2 = std::max<u64>(maxbin, std::min<u64>(T, std::max<u64>(avail / div, 1u << 20)));
-    u64 c1 = 0, sc = 0;
-    const int np = passes_for(c2, c1, sc);
-    if (np > 0 && (np_best < 0 || np < np_best)) {
-      np_best = np;
-      C2 = c2;
-      C1 = c1;
-      SC = sc;
-    }
-  }
-  if (np_best < 0) return set_error(SFCI_ERR_NOMEM, "SpMSpV device-memory budget too small");
+  MemPlan mp;
+  if (!plan_memory(binoff, NB1, T, avail, std::min<u64>(cap, T), maxbin, nlev > 0, mp))
+    return set_error(SFCI_ERR_NOMEM, "SpMSpV device-memory budget too small");
+  const u64 C2 = mp.C2, C1 = mp.C1, SC = mp.SC;
   KT* l1k = (KT*)scratch_get(c, "sp_l1k", C1 * sizeof(KT));
   double* l1a = (double*)scratch_get(c, "sp_l1a", C1 * sizeof(double));
   KT* l2k = nlev ? (KT*)scratch_get(c, "sp_l2k", C2 * sizeof(KT)) : nullptr;

@@ -91,3 +91,18 @@ def test_keys_roundtrip_helpers():
     ints = [0, 1, (1 << 64) + 5, (1 << 127) | 3]
     k = sg.keys_from_ints(ints, 2)
     assert sg.ints_from_keys(k) == ints
+
+
+def test_solver_entry_points_reject_null_arguments():
+    """Argument checks of the linear-solver and subspace entry points run before
+    any device call."""
+    L = sg.load_library()
+    name = lambda st: L.sfci_status_name(st).decode()
+    d = C.c_double()
+    n = C.c_uint64()
+    assert name(L.sfci_spmspv_linear(None, None, None, 0.0, None, 1, None)) == "SFCI_ERR_ARG"
+    assert name(L.sfci_res_norm(None, None, None, None, 0.0, C.byref(d))) == "SFCI_ERR_ARG"
+    assert name(L.sfci_krylov_linear(None, None, None, 0.0, 5, 1, None)) == "SFCI_ERR_ARG"
+    assert name(L.sfci_shift_invert(None, None, 0.0, 5, 1, C.byref(d))) == "SFCI_ERR_ARG"
+    assert name(L.sfci_cisd(None, None, 0, 1, None, None, None, C.byref(n))) == "SFCI_ERR_ARG"
+    assert name(L.sfci_fci(None, 1, None, None, None, C.byref(n))) == "SFCI_ERR_ARG"

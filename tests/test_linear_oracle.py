@@ -62,3 +62,15 @@ def test_linear_driver_reduces_the_residual():
     for name in NAMES:
         r = load_golden("lin_" + name)["D_res"]
         assert r[-1] < r[0]
+
+
+def test_port_linear_driver_two_word_keys(port, golden_in):
+    """The restated driver over the port's 128-bit backend gives the one-word
+    fixture's run on a 64-bit system."""
+    g, path = golden_in("lin_u8")
+    be = port.PortLib(words=2)
+    be.setup(path, 2 * int(g["M"]), int(g["ne"]), int(g["D_Nd"]), nthread=8)
+    xk, xa, rh = port.krylov_linear(be, (_wide(g["v1_keys"]), g["v1_amps"]), float(g["D_lam"]), int(g["D_iter"]),
+                                    int(g["D_restarts"]), int(g["D_Nd"]))
+    assert np.allclose(rh, g["D_res"], rtol=1e-8, atol=0)
+    compare_vectors(_wide(g["D_keys"]), g["D_amps"], xk, xa, capped=True, rtol=1e-8, atol=1e-11, edge_rtol=1e-6)

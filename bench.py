@@ -3,20 +3,28 @@
 
 Workload: synthetic RHF integrals, 28 spatial / 56 spin orbitals, 14 electrons,
 seed 1 (FP64, 8-fold symmetric, distributions of sfci_gb300.fcidump), Nd = 1e6.
-The input vector is a power-iteration Krylov vector: v_{k+1} = top-Nd(H v_k)
-(normalised) from |HF>, iterated on the device until it holds Nd determinants.
+The input vector is a second Krylov vector built identically by both arms:
+v1 = H|HF> (all 30,724 connected determinants), normalised; v2 = top-Nd of
+H v1 by |amplitude| (products without the 1e-5 cut), normalised.  The GPU arm
+builds it with its own product on the device, the reference arm with the CPU
+restatement; the two agree to rounding (RHF spin-mirror twins that tie exactly
+at the top-Nd edge may be swapped, which changes no work).
 value   = merged terms/s = Nd * C / t, C = connected determinants per source
           determinant (30723 here: singles + same- and opposite-spin doubles);
 e2e     = the same through the C ABI from pinned host buffers: host->device copy
           of the input, SpMSpV, device->host copy of the result, every step;
 roofline= dominant kernel of the step, algorithmic bytes per launch / its mean
           launch time (CUDA events on the library's stream), against the
-          measured HBM copy bandwidth.
+          measured HBM copy bandwidth; product_roofline = the whole product's
+          bytes under the materialise-once model (Nd + 2 T_conn + U)(K + 8)
+          over the step time;
+parity  = the GPU product of the exact top-n slice that cpu_baseline times,
+          against the CPU restatement's product of it (key sets, amplitudes).
 
 --impl reference times the CPU implementation of the same path (the oracle
-restatement of the reference algorithm, all host threads) on a bounded sample
-of the same workload.  Multi-GPU (torchrun) runs independent replicas, one per
-rank (weak scaling); rank 0 prints one JSON line.
+restatement of the reference algorithm, all host threads) on a bounded top-n
+slice of the same input vector.  Multi-GPU (torchrun) runs independent
+replicas, one per rank (weak scaling); rank 0 prints one JSON line.
 """
 from __future__ import annotations
 
@@ -88,6 +96,55 @@ def hf_key(sysd):
     return np.array([[hf & (2 ** 64 - 1), hf >> 64]], np.uint64)
 
 
+INPUT_TEXT = ("top-Nd of H (H|HF>) by |amplitude|, normalised (both products without the 1e-5 cut; "
+              "H|HF> holds every connected determinant)")
+
+
+def bench_config(sysd, nd, input_dets):
+    """The workload description both arms print (the reference arm adds only sample_dets)."""
+    return {"workload": "SpMSpV of a Krylov vector, " + sysd["text"], "input": INPUT_TEXT,
+            "num_orb": 2 * sysd["M"], "num_e": sysd["ne"], "Nd": nd, "input_dets": int(input_dets),
+            "l2": "inputs larger than L2: the terms of one product are hundreds of GB against 129 MB of L2"}
+
+
+def input_on_gpu(sg, path, sysd, nd):
+    """v2 = top-Nd(H v1), v1 = H|HF>, both normalised, built by the device product
+    on a construction context whose post-merge cut keeps every term."""
+    c0 = sg.Context(path, 2 * sysd["M"], sysd["ne"], Nd=nd, coeff_cut=-1.0)
+    hf = c0.vec(1)
+    hf.upload(hf_key(sysd), np.array([1.0]))
+    C1 = connected_per_det(sysd["M"], sysd["ne"] // 2, sysd["ne"] // 2) + 1
+    v1 = c0.vec(C1)
+    c0.SpMVMtply_bucket(hf, v1, 0.0, 1.0)
+    v1.normalize()
+    v2 = c0.vec(nd)
+    c0.SpMVMtply_bucket(v1, v2, 0.0, 1.0)
+    v2.normalize()
+    k, a = v2.download()
+    del v1, v2, hf, c0
+    return k, a
+
+
+def input_on_cpu(be, sysd, nd):
+    """The same construction with the CPU restatement (cut switched off, then restored)."""
+    C1 = connected_per_det(sysd["M"], sysd["ne"] // 2, sysd["ne"] // 2) + 1
+    be.set_cut(-1.0)
+    try:
+        k1, a1, _ = be.spmspv(hf_key(sysd), np.array([1.0]), C1, 0.0, 1.0)
+        a1 = a1 / np.linalg.norm(a1)
+        k2, a2, _ = be.spmspv(k1, a1, nd, 0.0, 1.0)
+    finally:
+        be.set_cut(1e-5)
+    return k2, a2 / np.linalg.norm(a2)
+
+
+def top_slice(keys, amps, n):
+    """The n largest |amplitude| entries (stable: ties keep the higher key), in key order."""
+    order = np.argsort(-np.abs(amps), kind="stable")
+    sel = np.sort(order[:n])
+    return keys[sel], amps[sel]
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled every 200 ms in the background."""
 
@@ -153,25 +210,61 @@ def peaks():
 # CPU baseline (oracle restatement of the reference algorithm)
 # ---------------------------------------------------------------------------
 
-def cpu_baseline(sysd, path, sample_keys, sample_amps_fn, target_s=15.0, threads=None):
+def calibrate_sample(be, keys, amps, target_s, n0=100):
+    """Largest top-n slice whose CPU product takes about target_s (at most the whole vector)."""
+    n = n0
+    while True:
+        k, a = top_slice(keys, amps, n)
+        t = time.perf_counter()
+        be.spmspv(k, a, 10 ** 7, 0.0, 1.0)
+        dt = time.perf_counter() - t
+        if dt > target_s / 4 or n >= len(amps):
+            return n, dt
+        n = min(len(amps), int(n * min(8.0, max(2.0, target_s / max(dt, 1e-3) / 2))))
+
+
+def cpu_baseline(sysd, path, keys, amps, target_s=15.0, threads=None):
+    """The CPU restatement on all host threads, one product of a top-n slice of the
+    GPU arm's input sized to ~target_s; returns the baseline and its product."""
     from oracle import oracle as orc
     orc.build_port()
     threads = threads or os.cpu_count() or 1
     be = orc.PortLib(words=key_words(sysd))
     be.setup(path, 2 * sysd["M"], sysd["ne"], 10 ** 7, nthread=threads)
     C = connected_per_det(sysd["M"], sysd["ne"] // 2, sysd["ne"] // 2)
-    n = 100
-    while True:
-        k, a = sample_keys[:n], sample_amps_fn(n)
-        t = time.perf_counter()
-        be.spmspv(k, a, 10 ** 7, 0.0, 1.0)
-        dt = time.perf_counter() - t
-        if dt > target_s / 4 or n >= len(sample_keys):
-            break
-        n = min(len(sample_keys), int(n * min(8.0, max(2.0, target_s / max(dt, 1e-3) / 2))))
-    return {"value": n * C / dt, "unit": UNIT, "cores": threads, "kind": "port",
+    n, _ = calibrate_sample(be, keys, amps, target_s)
+    k, a = top_slice(keys, amps, n)
+    t = time.perf_counter()
+    rk, ra, rd = be.spmspv(k, a, 10 ** 7, 0.0, 1.0)
+    dt = time.perf_counter() - t
+    base = {"value": n * C / dt, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": "top-%d determinants of the same input vector, one SpMSpV, %.1f s" % (n, dt),
             "seconds": dt, "dets": n}
+    return base, (k, a), (rk, ra, rd)
+
+
+def parity_report(ctx, sample, ref_out, cut=1e-5):
+    """The GPU product of the slice cpu_baseline timed, against the CPU product."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from parity import compare_vectors
+    k, a = sample
+    rk, ra, rd = ref_out
+    vin = ctx.vec_from(k, a)
+    out = ctx.vec(10 ** 7)
+    d = ctx.SpMVMtply_bucket(vin, out, 0.0, 1.0)
+    gk, ga = out.download()
+    rep = {"sample_dets": int(len(a)), "against": "CPU restatement (oracle) product of the same slice",
+           "diag_rel_diff": abs(d - rd) / max(abs(rd), 1e-300)}
+    try:
+        r = compare_vectors(rk, ra, gk, ga, cut=cut, capped=len(ra) == 10 ** 7)
+        rep.update(ok=True, max_rel_diff=r["max_rel"], common_keys=r["common"],
+                   edge_keys_only_cpu=r["edge_only_ref"], edge_keys_only_gpu=r["edge_only_got"],
+                   tolerance="keys bit-exact off the 1e-5 cut edge; amplitudes 1e-12 relative, 1e-14 absolute")
+    except AssertionError as e:
+        rep.update(ok=False, error=str(e)[:300])
+    rep["ok"] = bool(rep["ok"] and rep["diag_rel_diff"] <= 1e-12)
+    del vin, out
+    return rep
 
 
 # ---------------------------------------------------------------------------
@@ -216,21 +309,12 @@ def run_reference(args, rank, ws, dist):
     orc.build_port()
     be = orc.PortLib(words=key_words(sysd))
     be.setup(path, 2 * sysd["M"], sysd["ne"], args.nd, nthread=threads)
-    k1, a1, _ = be.spmspv(hf_key(sysd), np.array([1.0]), 10 ** 7, 0.0, 1.0)
-    order = np.argsort(-np.abs(a1), kind="stable")
+    keys, amps = input_on_cpu(be, sysd, args.nd)
+    be.set_nd(10 ** 7)
     C = connected_per_det(sysd["M"], sysd["ne"] // 2, sysd["ne"] // 2)
-    # size each step for ~args.ref_step_s seconds of CPU work
-    n = 200
-    for _ in range(6):
-        sel = np.sort(order[:n])
-        t = time.perf_counter()
-        be.spmspv(k1[sel], a1[sel], 10 ** 7, 0.0, 1.0)
-        dt = time.perf_counter() - t
-        if dt >= args.ref_step_s / 2 or n >= len(order):
-            break
-        n = min(len(order), int(n * min(8.0, args.ref_step_s / max(dt, 1e-3))))
-    sel = np.sort(order[:n])
-    ks, as_ = k1[sel], a1[sel] / np.linalg.norm(a1[sel])
+    # each step: one product of the top-n slice, n sized for ~args.ref_step_s
+    n, _ = calibrate_sample(be, keys, amps, args.ref_step_s, n0=200)
+    ks, as_ = top_slice(keys, amps, n)
     for _ in range(args.warmup):
         be.spmspv(ks, as_, 10 ** 7, 0.0, 1.0)
     t0 = time.perf_counter()
@@ -238,14 +322,14 @@ def run_reference(args, rank, ws, dist):
         be.spmspv(ks, as_, 10 ** 7, 0.0, 1.0)
     dt = (time.perf_counter() - t0) / args.steps
     val = n * C / dt
+    cfg = bench_config(sysd, args.nd, len(amps))
+    cfg["sample_dets"] = n
     out = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": "SpMSpV of a Krylov vector, " + sysd["text"],
-                      "num_orb": 2 * sysd["M"], "num_e": sysd["ne"], "Nd": args.nd, "sample_dets": n,
-                      "parallelism": "CPU, %d threads" % threads},
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
+           "parallelism": "CPU, %d threads" % threads,
            "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
-                            "sample": "top-%d determinants of H|HF>, one SpMSpV per step" % n},
+                            "sample": "top-%d determinants of the input vector, one SpMSpV per step" % n},
            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 
@@ -257,20 +341,10 @@ def run_gpu(args, rank, ws, local, dist):
     path = workload_in(sysd)
     nd = args.nd
     M, NE, W = sysd["M"], sysd["ne"], key_words(sysd)
+    in_k, in_a = input_on_gpu(sg, path, sysd, nd)
     ctx = sg.Context(path, 2 * M, NE, Nd=nd, hpsi_cap=HPSI_CAP, mem_budget=args.mem_budget)
-    # input: v_{k+1} = top-Nd(H v_k) normalised, from |HF>, until it holds Nd dets
-    hf = hf_key(sysd)
-    vin = ctx.vec(nd)
-    vin.upload(hf, np.array([1.0]))
-    tmp = ctx.vec(HPSI_CAP)
-    steps_in = 0
-    while vin.len < nd and steps_in < 8:
-        ctx.SpMVMtply_bucket(vin, tmp, 0.0, 1.0)
-        vin.shrinkFrom(tmp)
-        vin.normalize()
-        steps_in += 1
+    vin = ctx.vec_from(in_k, in_a, cap=nd)
     n_in = vin.len
-    del tmp
     out = ctx.vec(HPSI_CAP)
     C = connected_per_det(M, NE // 2, NE // 2)
     T_conn = n_in * C
@@ -298,7 +372,7 @@ def run_gpu(args, rank, ws, local, dist):
     out_len = out.len
     ms_max = reduce_max(dist, ms, local)
     # ---- end to end from pinned host buffers
-    keys_h, amps_h = vin.download()
+    keys_h, amps_h = in_k, in_a
     e2e_ms = None
     h2d = d2h = 0
     try:
@@ -369,22 +443,28 @@ def run_gpu(args, rank, ws, local, dist):
         else None  # measured for one-word keys
     value = T_conn * ws / (ms_max * 1e-3)
     e2e_val = T_conn * ws / e2e_s
+    # the whole product under the materialise-once model: read the input, write
+    # and read every connected term once, write the merged determinants once
+    B = (n_in + 2 * T_conn + stats["unique"]) * tbytes
+    prod_ach = B / (ms_max * 1e-3) / 1e9
     res = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_max, "s_per_iter": ms_max / 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "SpMSpV of a Krylov vector (top-Nd of H^k|HF>, k=%d), %s" % (steps_in, sysd["text"]),
-                   "num_orb": 2 * M, "num_e": NE, "Nd": nd, "input_dets": n_in,
-                   "connected_per_det": C, "emitted_per_det_reference": emitted_per_det(M, NE // 2, NE // 2),
-                   "generated_terms_per_step": T, "merged_unique_per_step": stats["unique"],
-                   "survivors_per_step": surv, "output_dets": out_len,
-                   "passes": stats["passes"], "leaves": stats["leaves"], "partition_levels": levels,
-                   "l2": "inputs larger than L2: %.0f GB of terms per step vs 129 MB" % (tbytes * T / 1e9),
-                   "parallelism": "replicas" if ws > 1 else "1 GPU"},
+        "config": bench_config(sysd, nd, n_in),
+        "parallelism": "replicas" if ws > 1 else "1 GPU",
+        "stats": {"connected_per_det": C, "emitted_per_det_reference": emitted_per_det(M, NE // 2, NE // 2),
+                  "generated_terms_per_step": T, "merged_unique_per_step": stats["unique"],
+                  "survivors_per_step": surv, "output_dets": out_len, "passes": stats["passes"],
+                  "leaves": stats["leaves"], "partition_levels": levels,
+                  "terms_gb_per_step": tbytes * T / 1e9},
         "roofline": {"bound": "hbm", "kernel": kernels[dom], "phase": dom, "achieved": achieved, "peak": hbm,
                      "unit": "GB/s", "frac": achieved / hbm, "peak_source": how, "traffic": traffic,
                      "traffic_unit": "bytes per launch", "algorithmic_bytes_per_launch": per_launch_bytes,
                      "launches": dl, "ms_per_launch": per_launch_ms},
+        "product_roofline": {"bytes_model": "(Nd + 2*T_conn + U) * (K + 8)", "bytes_per_step": B,
+                             "achieved": prod_ach, "peak": hbm, "unit": "GB/s", "frac": prod_ach / hbm,
+                             "peak_source": how},
         "phases_ms_per_step": {k: v[0] / args.steps for k, v in prof.items()},
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": e2e_s * 1e3},
@@ -393,13 +473,133 @@ def run_gpu(args, rank, ws, local, dist):
         "diag": diag,
     }
     if not args.no_cpu_baseline:
-        keys_sorted = keys_h[np.argsort(-np.abs(amps_h), kind="stable")]
-        amps_sorted = amps_h[np.argsort(-np.abs(amps_h), kind="stable")]
-        res["cpu_baseline"] = cpu_baseline(sysd, path, keys_sorted,
-                                           lambda n: amps_sorted[:n] / np.linalg.norm(amps_sorted[:n]),
-                                           target_s=args.cpu_seconds)
+        base, sample, ref_out = cpu_baseline(sysd, path, keys_h, amps_h, target_s=args.cpu_seconds)
+        res["cpu_baseline"] = base
+        res["parity"] = parity_report(ctx, sample, ref_out)
     print(json.dumps(res), flush=True)
     barrier(dist)
+
+
+# ---------------------------------------------------------------------------
+# learned excitation screen: train on logged labels, then plain vs screened
+# ---------------------------------------------------------------------------
+
+def _krylov_input(sg, ctx, sysd, nd):
+    """top-nd of H (H|HF>) with the product's own cut, normalised (the sources a
+    Lanczos step would multiply)."""
+    hf = ctx.vec(1)
+    hf.upload(hf_key(sysd), np.array([1.0]))
+    v1 = ctx.vec(HPSI_CAP)
+    ctx.SpMVMtply_bucket(hf, v1, 0.0, 1.0)
+    v1.normalize()
+    w = ctx.vec(HPSI_CAP)
+    ctx.SpMVMtply_bucket(v1, w, 0.0, 1.0)
+    v2 = ctx.vec(nd)
+    v2.shrinkFrom(w)
+    v2.normalize()
+    return v2
+
+
+def run_screen(args):
+    """Screen study: labels from plain products on 112-spin-orbital, 18-electron
+    synthetic RHF systems of seeds 6-9, Adam training of the MLP on them, then the
+    truncated Lanczos driver on the seed-5 system with and without the screen.
+    The energy of every run is judged by the unscreened calc_energy of its final
+    vector; the screened run is accepted when it is within tol of the plain one."""
+    import sfci_gb300 as sg
+    sg.load_library()
+    M, NE = 56, 18
+    train_seeds = [6, 7, 8, 9]
+    res = {"metric": METRIC, "unit": "s (time to energy)", "higher_is_better": False, "mode": "learned screen",
+           "dtype": "f64 products, bf16 MLP (fp32 accumulate)", "data": "synthetic"}
+    t0 = time.perf_counter()
+    tr = {"systems": [], "examples": 0, "positives": 0}
+    scr = None
+    ctxs = []
+    for sd in train_seeds:
+        sysd = dict(M=M, ne=NE, seeds=(sd,), text="")
+        path = workload_in(sysd)
+        ctx = sg.Context(path, 2 * M, NE, Nd=args.screen_log_nd, hpsi_cap=HPSI_CAP)
+        ctxs.append(ctx)
+        if scr is None:
+            scr = sg.Screen(ctx, seed=1)
+        vin = _krylov_input(sg, ctx, sysd, args.screen_log_nd)
+        out = ctx.vec(HPSI_CAP)
+        ctx.SpMVMtply_bucket(vin, out, 0.0, 1.0)
+        # the screen lives on the first context; each system logs from its own
+        ne, npos = scr.log(vin, out)
+        tr["systems"].append({"seed": sd, "sources": vin.len, "examples": ne, "positives": npos})
+        tr["examples"] += ne
+        tr["positives"] += npos
+        del vin, out
+        ctx.trim()
+        if len(ctxs) > 1:
+            ctxs.pop()
+            del ctx
+    pos_frac = tr["positives"] / max(tr["examples"], 1)
+    pw = min(20.0, max(1.0, 0.25 * (1 - pos_frac) / max(pos_frac, 1e-9)))
+    t1 = time.perf_counter()
+    losses = []
+    steps_done = 0
+    while steps_done < args.screen_steps:
+        n = min(500, args.screen_steps - steps_done)
+        losses.append(scr.train(n, batch_tiles=64, lr=args.screen_lr, pos_weight=pw))
+        steps_done += n
+    t2 = time.perf_counter()
+    tr.update(positive_fraction=pos_frac, pos_weight=pw, steps=steps_done, batch=64 * 128,
+              loss_curve=losses, log_seconds=t1 - t0, train_seconds=t2 - t1)
+    res["training"] = tr
+    # evaluation system: seed 5; the screen's weights are moved to a context on it
+    sysd = dict(M=M, ne=NE, seeds=(args.screen_seed,), text="")
+    path = workload_in(sysd)
+    params = scr.params()
+    del scr
+    ctxs.clear()
+    ev = sg.Context(path, 2 * M, NE, Nd=args.screen_nd, hpsi_cap=HPSI_CAP)
+    scr_e = sg.Screen(ev, seed=1)
+    scr_e.set_params(params)
+    runs = []
+
+    def lanczos(thr):
+        ev.set_screen(None if thr is None else scr_e, 0.0 if thr is None else thr)
+        st0 = ev.screen_stats()
+        v = ev.vec(args.screen_nd)
+        v.upload(hf_key(sysd), np.array([1.0]))
+        ev.profile(False)
+        ta = time.perf_counter()
+        en, fe = ev.sparse_krylov_solve_eigenval(v, args.screen_nl, 1)
+        tb = time.perf_counter()
+        st1 = ev.screen_stats()
+        d = {k: st1[k] - st0[k] for k in st1}
+        return {"threshold": thr, "seconds": tb - ta, "gsaes_energy": float(en[0]), "energy": fe,
+                "kept_group_fraction": d["kept_groups"] / d["groups"] if d["groups"] else 1.0,
+                "products": d["products"], "kept_terms": d["kept_terms"]}
+
+    lanczos(None)  # warm-up (scratch allocation)
+    plain = lanczos(None)
+    C = connected_per_det(M, NE // 2, NE // 2)
+    runs.append(plain)
+    best = None
+    for thr in args.screen_thresholds:
+        r = lanczos(thr)
+        r["dE"] = r["energy"] - plain["energy"]
+        # skipped fraction of the doubles' terms, over the screened products
+        r["skipped_term_fraction"] = None
+        runs.append(r)
+        if abs(r["dE"]) <= args.screen_tol and (best is None or r["seconds"] < best["seconds"]):
+            best = r
+    res["config"] = {"workload": "truncated Lanczos, 112 spin orbitals, 18 electrons, synthetic RHF seed %d"
+                                 % args.screen_seed, "num_orb": 2 * M, "num_e": NE, "Nd": args.screen_nd,
+                     "Nl": args.screen_nl, "restarts": 1, "train_seeds": train_seeds,
+                     "log_Nd": args.screen_log_nd, "tol_Eh": args.screen_tol}
+    res["runs"] = runs
+    res["plain_seconds"] = plain["seconds"]
+    res["chosen"] = best
+    res["value"] = best["seconds"] if best else plain["seconds"]
+    res["speedup_vs_plain"] = plain["seconds"] / best["seconds"] if best else 1.0
+    res["fallback"] = best is None
+    res["connected_per_det"] = C
+    print(json.dumps(res), flush=True)
 
 
 def main():
@@ -418,7 +618,20 @@ def main():
     ap.add_argument("--mem-budget", type=int, default=0,
                     help="device bytes the SpMSpV may use (0: 80%% of free); a small budget forces several "
                          "generation passes on a small case, e.g. for profiling")
+    ap.add_argument("--screen", action="store_true",
+                    help="learned-screen study (112 spin orbitals): train, then plain vs screened Lanczos")
+    ap.add_argument("--screen-nd", type=int, default=200000)
+    ap.add_argument("--screen-nl", type=int, default=8)
+    ap.add_argument("--screen-log-nd", type=int, default=1800)
+    ap.add_argument("--screen-steps", type=int, default=4000)
+    ap.add_argument("--screen-lr", type=float, default=1e-3)
+    ap.add_argument("--screen-seed", type=int, default=5)
+    ap.add_argument("--screen-tol", type=float, default=1e-5)
+    ap.add_argument("--screen-thresholds", type=float, nargs="+", default=[0.02, 0.05, 0.1, 0.2, 0.35])
     args = ap.parse_args()
+    if args.screen:
+        run_screen(args)
+        return
     rank, ws, local, dist = dist_init()
     try:
         if args.impl == "reference":

@@ -68,6 +68,9 @@ int sfci_key_words(const sfci_ctx* ctx);
 /* CUDA stream (cudaStream_t) all of the context's work is queued on. */
 int sfci_ctx_stream(const sfci_ctx* ctx, void** stream);
 int sfci_ctx_set_nd(sfci_ctx* ctx, uint64_t Nd);
+/* Frees the device scratch the context's products keep between calls (it grows
+ * to most of the free device memory); the next product allocates it again. */
+int sfci_ctx_trim(sfci_ctx* ctx);
 /* Kernel launches issued by this context so far (monotone counter). */
 int sfci_ctx_launch_count(const sfci_ctx* ctx, uint64_t* n);
 /* Timing probe: record CUDA event `slot` (0..15) on the context stream, and
@@ -117,8 +120,10 @@ int sfci_vec_clear(sfci_vec* v);                                   /* setZeroVec
  *   out = top_cap( { k : |a_k| > coeff_cut } of merge( coeff * (H - lambda) * top_Nd(in) ) )
  * sorted by key, with *diag = coeff * <top_Nd(in)| (H - lambda) |top_Nd(in)>
  * evaluated before the cut.  An empty input leaves *diag untouched and
- * empties out, as the reference does (:529-533).  Merged amplitudes are exact
- * sums rounded once; a term with |amplitude| >= 2^24 (or not finite) gives
+ * empties out, as the reference does (:529-533).  Each term is rounded to the
+ * nearest multiple of 2^-64 (an unbiased error of at most 2.7e-20), the rounded
+ * terms of a determinant are summed exactly, whatever their order, and the sum
+ * is rounded once to double; a term with |amplitude| >= 2^24 (or not finite) gives
  * SFCI_ERR_NUMERIC, and determinants connected to more than 2^19 others give
  * SFCI_ERR_UNSUPPORTED. */
 int sfci_spmspv(sfci_ctx* ctx, const sfci_vec* in, sfci_vec* out, double lambda, double coeff,
@@ -211,10 +216,65 @@ int sfci_fci(sfci_ctx* ctx, int n_evals, double* evals, sfci_vec* ground, double
  * 16,777,216 entries, otherwise SFCI_ERR_ARG before any launch.  All calls share
  * the array, so calls whose kernels overlap on the GPU race; order them on one
  * stream.  The first call on a device looks up the array's address with that
- * device current (cudaGetSymbolAddress); make that first call before any stream
- * capture begins. */
+ * device current (cudaGetSymbolAddress) and keeps it for the life of the
+ * process; make that first call before any stream capture begins.  A
+ * cudaDeviceReset (or a release and re-creation of the device's primary
+ * context) reloads the module and leaves that cached address stale: calls on a
+ * device after such a reset are not supported. */
 int sfci_dot_noalloc(const uint64_t* x_keys, const double* x_amps, uint64_t nx, const uint64_t* y_keys,
                      const double* y_amps, uint64_t ny, int key_words, double* d_out, void* stream);
+
+/* ---- learned excitation screen (no counterpart in the reference) ---------------
+ * A BF16 MLP (3 layers, hidden width 256, FP32 accumulation, sigmoid output),
+ * trained and run on the tensor cores, that predicts for each term group of a
+ * source determinant whether any of its terms lands on a determinant that
+ * survives the product's cut and cap.  A group is a source determinant's
+ * excitations sharing one prefix: same-spin doubles with a given occupied pair
+ * and larger hole, or opposite-spin doubles with a given spin-0 single and spin-1
+ * occupied orbital; the diagonal and singles are never screened.  Features: the
+ * source's occupancy bits, one-hot (p, q, r) of the prefix and its class,
+ * log10 |c_j| and log10 of a bound on the group's two-body elements.  With a
+ * screen attached (sfci_ctx_set_screen), sfci_spmspv and the drivers built on
+ * it skip the groups predicted dead (probability below the threshold): the
+ * generator of OffDiagGen_bit (src/bitstr.cpp:162-302) restricted to the kept
+ * groups.  Threshold 0 keeps every group and gives the plain product exactly;
+ * products with extra sources (sfci_spmspv_linear, sfci_res_norm) and
+ * sfci_energy are never screened, so calc_energy stays the judge of a screened
+ * run's energy. */
+typedef struct sfci_screen sfci_screen;
+int sfci_screen_create(sfci_ctx* ctx, uint64_t seed, sfci_screen** out);
+int sfci_screen_destroy(sfci_screen* s);
+/* Appends labelled examples: every term group of the determinants of `in` (at
+ * most Nd of them: the sources of a product), alive when one of its terms lands
+ * on a key of `out`, the product's output.  `in` and `out` may belong to another
+ * context with the same number of orbitals (another Hamiltonian, up to 64 of
+ * them per screen); the screen keeps that Hamiltonian's integral bounds for the
+ * examples' features. */
+int sfci_screen_log(sfci_screen* s, const sfci_vec* in, const sfci_vec* out, uint64_t* examples,
+                    uint64_t* positives);
+/* `steps` Adam steps on batches of batch_tiles x 128 logged examples (random
+ * windows, or consecutive from the first example when `sequential`), binary
+ * cross-entropy with positives weighted by pos_weight; lr 0 computes the
+ * gradients of one batch without updating.  *loss: the last batch's mean. */
+int sfci_screen_train(sfci_screen* s, int steps, int batch_tiles, double lr, double pos_weight, int sequential,
+                      double* loss);
+int sfci_screen_stats(const sfci_screen* s, uint64_t* sources, uint64_t* examples, uint64_t* positives,
+                      uint64_t* steps);
+/* Runs the MLP on the groups of the determinants of `in`: counts of groups, of
+ * groups with probability >= threshold and of their terms; prob_host (nullable,
+ * prob_cap entries) receives each group's probability, source by source. */
+int sfci_screen_predict(sfci_screen* s, const sfci_vec* in, double threshold, uint64_t* groups,
+                        uint64_t* kept_groups, uint64_t* kept_terms, float* prob_host, uint64_t prob_cap);
+/* FP32 parameters (sfci_screen_param_count floats: W1[576][256] by input row,
+ * b1, W2[256 out][256 in], b2, w3, b3, padding); get and/or set (nullable). */
+uint64_t sfci_screen_param_count(void);
+int sfci_screen_params(sfci_screen* s, float* get, const float* set, uint64_t n);
+/* the gradients of the last training step (same layout) */
+int sfci_screen_grads(sfci_screen* s, float* get, uint64_t n);
+/* Attach (s non-null) or detach the screen of the context's products. */
+int sfci_ctx_set_screen(sfci_ctx* ctx, sfci_screen* s, double threshold);
+/* groups seen, groups kept, terms kept, screened products since the context was made */
+int sfci_ctx_screen_stats(const sfci_ctx* ctx, uint64_t* out4);
 
 /* Generalised symmetric eigensolve K c = E S c (Eigen GSAES as used at
  * src/sparse_solver.cpp:450), FP64 on the host: eigenvalues ascending,

@@ -4,9 +4,11 @@
 # oracle/_ref/libsfci_ref.so.  Only the three translation units of the SpMSpV path
 # are built (functions.cpp, bitstr.cpp, introsort.cpp); Eigen is replaced by the
 # name-only stub under oracle/ref_stub.  Usage: oracle/build_ref.sh [REF_ROOT]
+# REF_ROOT defaults to $SFCI_REFERENCE_ROOT, else a checkout named "reference"
+# beside this repository.
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF="${1:-${SFCI_REFERENCE_ROOT:-/root/reference}}"
+REF="${1:-${SFCI_REFERENCE_ROOT:-$(dirname "$HERE")/../reference}}"
 SRC="$REF/src"
 if [ ! -f "$SRC/functions.cpp" ]; then
   echo "reference sources not found under $SRC; oracle/_ref not built" >&2

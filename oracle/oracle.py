@@ -234,6 +234,17 @@ class PortLib(_Backend):
         self.prefix = "port%d_" % (64 * words)
         super().__init__(so)
 
+    def set_nd(self, Nd):
+        """Change the global Nd without re-reading the integral file."""
+        self.f("set_nd").argtypes = [_ui]
+        self.f("set_nd")(int(Nd))
+        self.Nd = int(Nd)
+
+    def set_cut(self, cut):
+        """The post-merge cut |a| > cut of spmspv (1e-5 by default; negative keeps every term)."""
+        self.f("set_cut").argtypes = [C.c_double]
+        self.f("set_cut")(float(cut))
+
 
 # ---------------------------------------------------------------------------
 # drivers restated on top of a backend

@@ -48,7 +48,7 @@ struct Ham {
 Ham H;
 unsigned g_Nd = 200000;
 int g_threads = 1;
-const double kCut = 1e-5;  // SpMSpVFinalResCut, src/main.cpp:196
+double kCut = 1e-5;  // SpMSpVFinalResCut, src/main.cpp:196 (settable: a negative cut keeps every merged term)
 
 // ReadElements, src/functions.cpp:297-395
 bool read_elements(const char* path) {
@@ -515,6 +515,8 @@ int setup(const char* path, unsigned norb, unsigned ne, unsigned nd, unsigned nt
                                  unsigned) {                                                                     \
     return setup(p, norb, ne, nd, nt);                                                                           \
   }                                                                                                              \
+  extern "C" void port##W##_set_nd(unsigned nd) { g_Nd = nd; }                                                   \
+  extern "C" void port##W##_set_cut(double cut) { kCut = cut; }                                                  \
   extern "C" void port##W##_spmspv(const u64* ik, const double* ia, unsigned il, unsigned, unsigned ocap,      \
                                    double lam, double coeff, u64* ok, double* oa, unsigned* ol, double* dg) {   \
     std::vector<Term<D>> out;                                                                                    \

@@ -57,6 +57,7 @@ def _sigs(L):
     L.sfci_key_words.argtypes = [_vp]
     L.sfci_ctx_stream.argtypes = [_vp, C.POINTER(_vp)]
     L.sfci_ctx_set_nd.argtypes = [_vp, C.c_uint64]
+    L.sfci_ctx_trim.argtypes = [_vp]
     L.sfci_ctx_launch_count.argtypes = [_vp, C.POINTER(C.c_uint64)]
     L.sfci_ctx_event_record.argtypes = [_vp, C.c_int]
     L.sfci_ctx_event_elapsed.argtypes = [_vp, C.c_int, C.c_int, C.POINTER(C.c_float)]
@@ -96,6 +97,18 @@ def _sigs(L):
     L.sfci_res_norm.argtypes = [_vp, _vp, _vp, _vp, C.c_double, C.POINTER(C.c_double)]
     L.sfci_krylov_linear.argtypes = [_vp, _vp, _vp, C.c_double, C.c_int, C.c_int, _vp]
     L.sfci_shift_invert.argtypes = [_vp, _vp, C.c_double, C.c_int, C.c_int, C.POINTER(C.c_double)]
+    _u64p = C.POINTER(C.c_uint64)
+    L.sfci_screen_create.argtypes = [_vp, C.c_uint64, C.POINTER(_vp)]
+    L.sfci_screen_destroy.argtypes = [_vp]
+    L.sfci_screen_log.argtypes = [_vp, _vp, _vp, _u64p, _u64p]
+    L.sfci_screen_train.argtypes = [_vp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, C.POINTER(C.c_double)]
+    L.sfci_screen_stats.argtypes = [_vp, _u64p, _u64p, _u64p, _u64p]
+    L.sfci_screen_predict.argtypes = [_vp, _vp, C.c_double, _u64p, _u64p, _u64p, _vp, C.c_uint64]
+    L.sfci_screen_param_count.restype = C.c_uint64
+    L.sfci_screen_params.argtypes = [_vp, _vp, _vp, C.c_uint64]
+    L.sfci_screen_grads.argtypes = [_vp, _vp, C.c_uint64]
+    L.sfci_ctx_set_screen.argtypes = [_vp, _vp, C.c_double]
+    L.sfci_ctx_screen_stats.argtypes = [_vp, _u64p]
     return L
 
 
@@ -118,7 +131,8 @@ def load_library(path: str | None = None, build: bool = True):
                "sfci_diag_elements", "sfci_energy", "sfci_dot", "sfci_norm", "sfci_scale", "sfci_normalize",
                "sfci_add_two", "sfci_add_three", "sfci_shrink_from", "sfci_combine", "sfci_lanczos_ground",
                "sfci_minres", "sfci_gsaes", "sfci_cisd", "sfci_fci", "sfci_spmspv_linear", "sfci_res_norm",
-               "sfci_krylov_linear", "sfci_shift_invert"):
+               "sfci_krylov_linear", "sfci_shift_invert", "sfci_screen_create", "sfci_screen_train",
+               "sfci_ctx_set_screen"):
         getattr(L, fn)
     _LIB = _sigs(L)
     return _LIB
@@ -237,6 +251,10 @@ class Context:
         v = SpVec(self, cap if cap is not None else max(1, len(amps)))
         v.upload(keys, amps)
         return v
+
+    def trim(self):
+        """Free the device scratch this context's products keep between calls."""
+        _check(self.L.sfci_ctx_trim(self.h))
 
     def set_Nd(self, Nd: int):
         _check(self.L.sfci_ctx_set_nd(self.h, int(Nd)))
@@ -383,6 +401,89 @@ class Context:
         _check(self.L.sfci_ctx_last_stats(self.h, a))
         names = ["input_dets", "terms", "unique", "survivors", "out_len", "passes", "leaves", "big_leaves"]
         return dict(zip(names, [int(x) for x in a]))
+
+    # learned excitation screen
+    def set_screen(self, screen: "Screen | None", threshold: float = 0.5):
+        """Screen this context's products (None: plain products)."""
+        _check(self.L.sfci_ctx_set_screen(self.h, screen.h if screen is not None else None, float(threshold)))
+        self._screen = screen
+
+    def screen_stats(self) -> dict:
+        a = (C.c_uint64 * 4)()
+        _check(self.L.sfci_ctx_screen_stats(self.h, a))
+        return dict(zip(["groups", "kept_groups", "kept_terms", "products"], [int(x) for x in a]))
+
+
+class Screen:
+    """Learned excitation screen: a BF16 MLP on the tensor cores predicting which
+    term groups of a product survive its cut (see include/sfci_gb300.h)."""
+
+    def __init__(self, ctx: Context, seed: int = 1):
+        self.ctx = ctx
+        self.L = ctx.L
+        h = _vp()
+        _check(self.L.sfci_screen_create(ctx.h, int(seed), C.byref(h)))
+        self.h = h
+        self.nparam = int(self.L.sfci_screen_param_count())
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                self.L.sfci_screen_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+    def log(self, vin: "SpVec", vout: "SpVec"):
+        """Label the groups of vin's determinants by vout (the product of vin)."""
+        ne, npos = C.c_uint64(), C.c_uint64()
+        _check(self.L.sfci_screen_log(self.h, vin.h, vout.h, C.byref(ne), C.byref(npos)))
+        return ne.value, npos.value
+
+    def train(self, steps: int, batch_tiles: int = 64, lr: float = 1e-3, pos_weight: float = 1.0,
+              sequential: bool = False) -> float:
+        loss = C.c_double()
+        _check(self.L.sfci_screen_train(self.h, int(steps), int(batch_tiles), float(lr), float(pos_weight),
+                                        1 if sequential else 0, C.byref(loss)))
+        return loss.value
+
+    def stats(self) -> dict:
+        a = [C.c_uint64() for _ in range(4)]
+        _check(self.L.sfci_screen_stats(self.h, *[C.byref(x) for x in a]))
+        return dict(zip(["sources", "examples", "positives", "steps"], [x.value for x in a]))
+
+    def predict(self, vin: "SpVec", threshold: float = 0.5, probs: bool = False):
+        g, kg, kt = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        buf = None
+        cap = 0
+        if probs:
+            cap = self.groups_of(vin)
+            buf = np.zeros(max(cap, 1), np.float32)
+        _check(self.L.sfci_screen_predict(self.h, vin.h, float(threshold), C.byref(g), C.byref(kg), C.byref(kt),
+                                          _ptr(buf) if probs else None, cap))
+        out = {"groups": g.value, "kept_groups": kg.value, "kept_terms": kt.value}
+        if probs:
+            out["prob"] = buf[: g.value]
+        return out
+
+    def groups_of(self, vin: "SpVec") -> int:
+        g, kg, kt = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        _check(self.L.sfci_screen_predict(self.h, vin.h, 0.5, C.byref(g), C.byref(kg), C.byref(kt), None, 0))
+        return g.value
+
+    def params(self) -> np.ndarray:
+        a = np.zeros(self.nparam, np.float32)
+        _check(self.L.sfci_screen_params(self.h, _ptr(a), None, self.nparam))
+        return a
+
+    def set_params(self, a):
+        a = np.ascontiguousarray(a, np.float32)
+        _check(self.L.sfci_screen_params(self.h, None, _ptr(a), self.nparam))
+
+    def grads(self) -> np.ndarray:
+        a = np.zeros(self.nparam, np.float32)
+        _check(self.L.sfci_screen_grads(self.h, _ptr(a), self.nparam))
+        return a
 
 
 class SpVec:

@@ -20,7 +20,7 @@ LIB = os.path.join(BUILD, "libsfci_gb300.so")
 EXE = os.path.join(BUILD, "sfci")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_UNITS = ["prims.cu", "spmspv.cu", "vecops.cu", "noalloc.cu", "subspace.cu"]
+CU_UNITS = ["prims.cu", "spmspv.cu", "vecops.cu", "noalloc.cu", "subspace.cu", "mlp.cu"]
 CXX_UNITS = ["abi.cpp", "solver.cpp", "ham.cpp", "vecio.cpp"]
 
 

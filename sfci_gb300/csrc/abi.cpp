@@ -292,6 +292,13 @@ int sfci_ctx_set_nd(sfci_ctx* x, uint64_t Nd) {
   return SFCI_OK;
 }
 
+int sfci_ctx_trim(sfci_ctx* x) {
+  if (!x) return set_error(SFCI_ERR_ARG, "null context");
+  SFCI_CUDA(cudaStreamSynchronize(x->c.stream));
+  scratch_free_all(x->c);
+  return SFCI_OK;
+}
+
 int sfci_ctx_launch_count(const sfci_ctx* x, uint64_t* n) {
   if (!x || !n) return set_error(SFCI_ERR_ARG, "null argument");
   *n = x->c.launches;

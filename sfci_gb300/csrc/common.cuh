@@ -154,11 +154,14 @@ SFCI_HD u64 abs_bits(double x) {
 // double atomicAdd to shared memory is a compare-and-swap loop around an FP64
 // add.  The merge therefore sums amplitudes as integers in units of
 // 2^-FX_FRAC, with integer reductions only, so a merged amplitude does not
-// depend on the order in which its terms arrive and the only rounding is the
-// final conversion back to double (round to nearest, ties to even).
+// depend on the order in which its terms arrive: each term is rounded once to
+// the 2^-FX_FRAC grid, the sum of the rounded terms is exact, and the sum is
+// rounded once back to double (round to nearest, ties to even).
 //
-// A term x becomes F = x * 2^FX_FRAC truncated toward zero (terms below
-// 2^-FX_FRAC = 5.4e-20 vanish; |x| must stay below 2^FX_MAX_EXP), split into
+// A term x becomes F = x * 2^FX_FRAC rounded to the nearest integer, ties to
+// even (an error of at most 2^-(FX_FRAC+1) = 2.7e-20 per term, unbiased, so k
+// terms of one key drift by about sqrt(k) * 1.6e-20, not k * 5.4e-20 as a
+// truncation toward zero would; |x| must stay below 2^FX_MAX_EXP), split into
 // two addends: lo = F mod 2^FX_SPLIT (unsigned) and hi = F >> FX_SPLIT
 // (signed).  An accumulator is two 64-bit words that add the lo and hi addends
 // independently, without carries between them, so each add is a plain
@@ -191,6 +194,12 @@ SFCI_HD int clz64(u64 x) {  // x != 0
 #endif
 }
 
+// m * 2^-k rounded to the nearest integer, ties to even (m < 2^53, 1 <= k <= 53)
+SFCI_HD u64 shr_round(u64 m, int k) {
+  const u64 q = m >> k, r = m & ((1ull << k) - 1ull), half = 1ull << (k - 1);
+  return q + ((r > half || (r == half && (q & 1ull))) ? 1ull : 0ull);
+}
+
 // the two addends of x; sets *bad for |x| >= 2^FX_MAX_EXP, infinities and NaNs
 // (which then add nothing)
 SFCI_HD void fx_addends(double x, u64& lo, u64& hi, unsigned& bad) {
@@ -204,10 +213,10 @@ SFCI_HD void fx_addends(double x, u64& lo, u64& hi, unsigned& bad) {
     bad = 1u;
     return;
   }
-  if (e == 0 || s <= -53) return;  // zero, subnormal or below the resolution
-  u64 l, h;                        // F as a 128-bit two's-complement (h:l), |F| < 2^(FX_MAX_EXP+FX_FRAC)
+  if (e == 0 || s < -53) return;  // zero, subnormal, or |F| < 1/2 (rounds to 0)
+  u64 l, h;                       // F as a 128-bit two's-complement (h:l), |F| < 2^(FX_MAX_EXP+FX_FRAC)
   if (s < 0) {
-    l = m >> -s;
+    l = shr_round(m, -s);
     h = 0;
   } else {
     l = m << s;
@@ -246,9 +255,9 @@ SFCI_HD void fx32_digits(double x, int dg[4], unsigned& big) {
     return;
   }
   const u64 m = (b & 0xfffffffffffffull) | (1ull << 52);
-  const int s = e - (1075 - FX_FRAC);  // |F| = m * 2^s < 2^(FX_FRAC + FX32_MAX_EXP)
-  if (e == 0 || s <= -53) return;
-  __int128 f = s < 0 ? (__int128)(m >> -s) : ((__int128)m << s);
+  const int s = e - (1075 - FX_FRAC);  // |F| = m * 2^s < 2^(FX_FRAC + FX32_MAX_EXP), rounded as in fx_addends
+  if (e == 0 || s < -53) return;
+  __int128 f = s < 0 ? (__int128)shr_round(m, -s) : ((__int128)m << s);
   if (b >> 63) f = -f;
   for (int k = 0; k < 3; ++k) {
     const long long d = (long long)(((unsigned long long)f + (1ull << (FX32_DIG - 1))) & ((1ull << FX32_DIG) - 1)) -

@@ -62,6 +62,10 @@ struct Ctx {
   // pinned host staging for small readbacks
   u64* h_pin = nullptr;
   size_t h_pin_words = 0;
+  // learned excitation screen applied by the products (nullptr: plain products)
+  struct Screen* screen = nullptr;
+  double screen_thr = 0.5;
+  uint64_t screen_stats[4] = {};  // groups, kept groups, kept terms, screened products
 };
 
 struct Vec {

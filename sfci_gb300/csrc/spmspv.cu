@@ -32,6 +32,7 @@
 #include "gen.cuh"
 #include "prims.cuh"
 #include "plan.h"
+#include "screen.cuh"
 #include "spmspv.h"
 #include "table.cuh"
 
@@ -54,7 +55,7 @@ constexpr unsigned LW_PROBE = 32;                 // probes before a warp table 
 constexpr unsigned LC_PROBE = 128;                // same for the second tier
 constexpr int B_MAX = 30;
 
-enum { M_COUNT = 0, M_SCATTER = 1, M_ENERGY = 2, M_PROJECT = 3 };
+enum { M_COUNT = 0, M_SCATTER = 1, M_ENERGY = 2, M_PROJECT = 3, M_LABEL = 4 };
 constexpr int PROJ_MAX = 64;  // vectors of one projection sweep
 
 template <int W> struct PartIPT;
@@ -218,14 +219,24 @@ struct GenArgs {
   u64* plo;                 // PROJECT: exact merged amplitude of each table slot (wide
   u64* phi;                 //   fixed point, low and high addends)
   unsigned* pbad;           // PROJECT: a term outside the fixed-point range
+  // learned screen (COUNT / SCATTER): the term index space of determinant j is
+  // the screened one, group 0 ([0, c[2])) followed by the kept groups listed at
+  // kl_off[j] .. kl_off[j+1] (first full index, first screened index)
+  const uint32_t* kl_start = nullptr;
+  const uint32_t* kl_pre = nullptr;
+  const u64* kl_off = nullptr;
+  unsigned kl_cap = 0;      // shared-memory entries (the longest list)
+  const u64* goff = nullptr;  // LABEL: first example of each source
+  uint32_t* labels = nullptr; // LABEL: one bit per (source, group >= 1)
 };
 
 template <class KT>
-__host__ __device__ inline size_t gen_smem_bytes(int mode, unsigned nbp) {
+__host__ __device__ inline size_t gen_smem_bytes(int mode, unsigned nbp, unsigned kl_cap = 0) {
   size_t s = al16(sizeof(DetInfo<KT>)) + al16(2016 * sizeof(unsigned short));
   if (mode == M_COUNT || mode == M_SCATTER) s += al16(sizeof(uint32_t) * nbp);
   if (mode == M_SCATTER)
     s += al16(sizeof(uint32_t) * nbp) + 2 * al16(sizeof(u64) * nbp) + 3 * al16(sizeof(unsigned short) * GEN_ROUND);
+  s += 2 * al16(sizeof(uint32_t) * kl_cap);
   return s;
 }
 
@@ -256,7 +267,11 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
     sb = reinterpret_cast<unsigned short*>(smem + off);
     off += al16(sizeof(unsigned short) * GEN_ROUND);
     sq = reinterpret_cast<unsigned short*>(smem + off);
+    off += al16(sizeof(unsigned short) * GEN_ROUND);
   }
+  uint32_t* kst = reinterpret_cast<uint32_t*>(smem + off);  // kept groups of the current determinant
+  uint32_t* kpr = kst + (al16(sizeof(uint32_t) * g.kl_cap) / sizeof(uint32_t));
+  __shared__ unsigned s_nk;
   __shared__ u64 s_det;
   __shared__ unsigned s_nsq;
   __shared__ double s_red[GEN_THREADS / 32];
@@ -350,10 +365,31 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
     const u64 dbeg = g.doff[det], dend = g.doff[det + 1];
     if (tid < 32) det_setup_warp(d, g.keys[det], g.coeff * g.amps[det], g.diagE[det], g.lambda, g.h.M);
     if (tid == 0 && det >= g.nmain) d.h.dterm = g.amps[det];  // a single term, as given
+    const bool screened = (MODE == M_COUNT || MODE == M_SCATTER) && g.kl_start && det < g.nmain;
+    if (screened) {
+      const u64 k0 = g.kl_off[det], nk = g.kl_off[det + 1] - k0;
+      for (unsigned i = tid; i < nk; i += GEN_THREADS) {
+        kst[i] = g.kl_start[k0 + i];
+        kpr[i] = g.kl_pre[k0 + i];
+      }
+      if (tid == 0) s_nk = (unsigned)nk;
+    }
     __syncthreads();
     if (det < g.nmain) det_fill_singles(d, tid, GEN_THREADS);  // (term 0 needs no tables)
     __syncthreads();
     const DetHead<KT> dh = d.h;
+    const unsigned nk = screened ? s_nk : 0u;
+    // screened term index -> full term index: group 0 maps to itself, then a
+    // binary search over the kept groups' screened starts
+    auto remap = [&](unsigned l) -> unsigned {
+      if (!screened || l < dh.c[2]) return l;
+      unsigned lo = 0, hi = nk;
+      while (hi - lo > 1) {
+        const unsigned mid = (lo + hi) >> 1;
+        if (kpr[mid] <= l) lo = mid; else hi = mid;
+      }
+      return kst[lo] + (l - kpr[lo]);
+    };
     const unsigned l0 = (unsigned)(t0 - dbeg);
     const unsigned l1 = (unsigned)((t1 < dend ? t1 : dend) - dbeg);
     for (unsigned rb = l0; rb < l1; rb += GEN_ROUND) {
@@ -368,7 +404,7 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
           unsigned l = rb + it * GEN_THREADS + tid;
           br[it] = ~0u;
           if (l < l1) {
-            const unsigned bin = (unsigned)(key_hash(target_key(dh, d, decode(dh, pt, l))) >> shift1);
+            const unsigned bin = (unsigned)(key_hash(target_key(dh, d, decode(dh, pt, remap(l)))) >> shift1);
             if (bin >= g.bin_lo && bin < g.bin_hi) {
               unsigned lb = bin - g.bin_lo;
               unsigned r = atomicAdd(&hist[lb], 1u);
@@ -422,7 +458,7 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
             key = dh.key;
             amp = dh.dterm;
           } else {
-            amp = double_term(dh, d, pt, g.h, l, key);
+            amp = double_term(dh, d, pt, g.h, remap(l), key);
           }
           g.okeys[pos] = key;
           g.oamps[pos] = amp;
@@ -449,7 +485,17 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
           unsigned l = rb + it * GEN_THREADS + tid;
           if (l < l1) {
             if (MODE == M_COUNT) {
-              atomicAdd(&hist[(unsigned)(key_hash(target_key(dh, d, decode(dh, pt, l))) >> shift1)], 1u);
+              atomicAdd(&hist[(unsigned)(key_hash(target_key(dh, d, decode(dh, pt, remap(l)))) >> shift1)], 1u);
+            } else if (MODE == M_LABEL) {
+              // a group is alive when one of its terms lands on the product's output
+              if (table_find_global(g.tkeys, g.tmask, target_key(dh, d, decode(dh, pt, l))) >= 0) {
+                const GroupCounts gc = group_counts(dh.na[0], dh.nv[0], dh.na[1], dh.nv[1]);
+                const unsigned gi = group_of_term(gc, dh.c, l);
+                if (gi) {
+                  const u64 ex = g.goff[det] + gi - 1;
+                  atomicOr(g.labels + (ex >> 5), 1u << (ex & 31));
+                }
+              }
             } else if (MODE == M_ENERGY) {
               const Exc e = decode(dh, pt, l);
               const KT key = target_key(dh, d, e);
@@ -1082,7 +1128,7 @@ static HamView ham_view(Ctx& c) {
 template <int W, int MODE>
 static int launch_gen(Ctx& c, const GenArgs<typename KeyOf<W>::T>& g, unsigned grid, unsigned nbp) {
   typedef typename KeyOf<W>::T KT;
-  size_t sm = gen_smem_bytes<KT>(MODE, nbp);
+  size_t sm = gen_smem_bytes<KT>(MODE, nbp, g.kl_cap);
   static size_t configured = 0;
   // opt in whenever the size grows: static shared memory (the projection's
   // per-warp sums) counts against the same 48 KB default
@@ -1098,16 +1144,31 @@ __global__ void k_fill_u64(u64* p, u64 n, u64 v) {
   for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (u64)gridDim.x * blockDim.x) p[i] = v;
 }
 
-// term counts (one term for determinants from nmain on) -> offsets, and diagonal elements
+// screened term count of a source: group 0 (diagonal and singles) plus its kept groups' terms
+template <class KT>
+__global__ void k_screen_counts(const KT* __restrict__ keys, u64 n, int N, int M, const u64* __restrict__ kept,
+                                u64* __restrict__ cnt) {
+  for (u64 j = (u64)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (u64)gridDim.x * blockDim.x) {
+    unsigned a0, a1;
+    spin_counts(keys[j], N, a0, a1);
+    cnt[j] = 1ull + (u64)a0 * (M - a0) + (u64)a1 * (M - a1) + kept[j];
+  }
+}
+
+// term counts (one term for determinants from nmain on) -> offsets, and diagonal elements;
+// with `kept` (the screen's kept terms per source) the counts are the screened ones
 template <int W>
 static int prep_dets(Ctx& c, const typename KeyOf<W>::T* keys, u64 n, u64** doff, double** diagE, u64* T,
-                     u64 nmain = ~0ull) {
+                     u64 nmain = ~0ull, const u64* kept = nullptr) {
   u64* off = (u64*)scratch_get(c, "sp_doff", (n + 1) * sizeof(u64));
   double* dg = (double*)scratch_get(c, "sp_diag", (n ? n : 1) * sizeof(double));
   if (!off || !dg) return SFCI_ERR_NOMEM;
   unsigned grid = (unsigned)std::min<u64>((n * 32 + 255) / 256, (u64)c.sm_count * 16);
   if (grid == 0) grid = 1;
   if (n) SFCI_LAUNCH(c, k_det_prep<typename KeyOf<W>::T>, grid, 256, 0, keys, n, ham_view(c), off, dg);
+  if (n && kept)
+    SFCI_LAUNCH(c, k_screen_counts<typename KeyOf<W>::T>, std::min<unsigned>((unsigned)((n + 255) / 256), c.sm_count * 8),
+                256, 0, keys, std::min<u64>(n, nmain), c.N, c.M, kept, off);
   if (nmain < n)
     SFCI_LAUNCH(c, k_fill_u64, std::min<unsigned>((unsigned)((n - nmain + 255) / 256), c.sm_count * 8), 256, 0,
                 off + nmain, n - nmain, (u64)1);
@@ -1218,10 +1279,20 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
     if (std::min<u64>(conn, ns) > FX_MAX_TERMS)
       return set_error(SFCI_ERR_UNSUPPORTED, "SpMSpV: determinants connect to more than 2^19 others");
   }
+  // learned screen: the kept term groups of each source.  Products with extra
+  // single-term sources (the linear solver's) stay unscreened.
+  ScreenList sl;
+  const u64* kept = nullptr;
+  if (c.screen && ng == ns) {
+    tok = phase_begin(c, PH_OTHER);
+    if ((st = screen_select(c, src_k, src_a, ns, &sl))) return st;
+    kept = sl.kept_terms;
+    phase_end(c, tok);
+  }
   // 2. term offsets + diagonal elements
   u64 *doff = nullptr, T = 0;
   double* diagE = nullptr;
-  if ((st = prep_dets<W>(c, gen_k, ng, &doff, &diagE, &T, ns))) return st;
+  if ((st = prep_dets<W>(c, gen_k, ng, &doff, &diagE, &T, ns, kept))) return st;
   c.stats[1] = T;
   // hash digits: level 1 (generation) d0 bits, then nlev partition levels.
   // 2^b leaves: the fewest (so the fewest partition levels, each a full read
@@ -1258,6 +1329,12 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
   g.T = T;
   g.b1 = d0;
   g.cntm = cntm;
+  if (kept) {
+    g.kl_start = sl.start;
+    g.kl_pre = sl.pre;
+    g.kl_off = sl.off;
+    g.kl_cap = std::max(sl.gmax, 1u);
+  }
   if ((st = launch_gen<W, M_COUNT>(c, g, G, NB1))) return st;
   if ((st = scan_excl(c, cntm, cntm, (u64)NB1 * G))) return st;
   std::vector<u64> binoff(NB1 + 1);
@@ -1844,6 +1921,70 @@ int res_norm_impl(Ctx& c, const Vec& x, Vec& r, const Vec& b, double lambda, dou
   *res = std::sqrt(q);
   return SFCI_OK;
 }
+
+// ---------------------------------------------------------------------------
+// learned screen: group offsets and label logging
+// ---------------------------------------------------------------------------
+template <class KT>
+__global__ void k_group_count(const KT* __restrict__ keys, u64 n, int N, int M, u64* __restrict__ cnt) {
+  for (u64 j = (u64)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (u64)gridDim.x * blockDim.x) {
+    unsigned a0, a1;
+    spin_counts(keys[j], N, a0, a1);
+    cnt[j] = det_groups(a0, M - a0, a1, M - a1) - 1;
+  }
+}
+
+template <int W>
+int group_offsets_impl(Ctx& c, const typename KeyOf<W>::T* keys, u64 n, u64* goff) {
+  typedef typename KeyOf<W>::T KT;
+  if (n)
+    SFCI_LAUNCH(c, k_group_count<KT>, std::min<unsigned>((unsigned)((n + 255) / 256), c.sm_count * 8), 256, 0, keys, n,
+                c.N, c.M, goff);
+  return scan_excl(c, goff, goff, n);
+}
+
+template <int W>
+int label_impl(Ctx& c, const typename KeyOf<W>::T* keys, const double* amps, u64 n, const u64* goff, const Vec& out,
+               uint32_t* labels) {
+  typedef typename KeyOf<W>::T KT;
+  if (n == 0 || out.len == 0) return SFCI_OK;
+  int st;
+  u64 *doff = nullptr, T = 0;
+  double* diagE = nullptr;
+  if ((st = prep_dets<W>(c, keys, n, &doff, &diagE, &T))) return st;
+  u64 tsz = 1;
+  while (tsz < 2 * out.len) tsz <<= 1;
+  if (tsz > (1ull << 31)) return set_error(SFCI_ERR_UNSUPPORTED, "label table too large");
+  KT* tk = (KT*)scratch_get(c, "lb_tk", tsz * sizeof(KT));
+  double* ta = (double*)scratch_get(c, "lb_ta", tsz * sizeof(double));
+  if (!tk || !ta) return SFCI_ERR_NOMEM;
+  unsigned gr = (unsigned)std::min<u64>((tsz + 255) / 256, (u64)c.sm_count * 8);
+  SFCI_LAUNCH(c, k_fill_empty<KT>, gr, 256, 0, tk, ta, tsz);
+  gr = (unsigned)std::min<u64>((out.len + 255) / 256, (u64)c.sm_count * 8);
+  SFCI_LAUNCH(c, k_table_build<KT>, gr, 256, 0, (const KT*)out.keys, out.amps, out.len, tk, ta, (unsigned)(tsz - 1));
+  GenArgs<KT> g{};
+  g.keys = keys;
+  g.amps = amps;
+  g.ndet = n;
+  g.doff = doff;
+  g.diagE = diagE;
+  g.coeff = 1.0;
+  g.lambda = 0.0;
+  g.h = ham_view(c);
+  g.T = T;
+  g.b1 = 1;
+  g.tkeys = tk;
+  g.tvals = ta;
+  g.tmask = (unsigned)(tsz - 1);
+  g.goff = goff;
+  g.labels = labels;
+  return launch_gen<W, M_LABEL>(c, g, gen_grid(c, T), 0);
+}
+
+template int group_offsets_impl<1>(Ctx&, const u64*, u64, u64*);
+template int group_offsets_impl<2>(Ctx&, const K128*, u64, u64*);
+template int label_impl<1>(Ctx&, const u64*, const double*, u64, const u64*, const Vec&, uint32_t*);
+template int label_impl<2>(Ctx&, const K128*, const double*, u64, const u64*, const Vec&, uint32_t*);
 
 template int spmspv_impl<1>(Ctx&, const Vec&, Vec&, double, double, double*, const SpExtra*);
 template int spmspv_impl<2>(Ctx&, const Vec&, Vec&, double, double, double*, const SpExtra*);

@@ -42,6 +42,25 @@ template <int W> int cisd_impl(Ctx& c, const u64* ref_key, int state_idx, int n_
 template <int W> int fci_impl(Ctx& c, int n_evals, double* evals, Vec* ground, double* resid, u64* dim);
 int norm_impl(Ctx& c, const Vec& v, double* out);
 
+// learned excitation screen (mlp.cu, screen.cuh): the kept term groups of each
+// source determinant of a product, in the screened term index space
+struct ScreenList {
+  const uint32_t* start = nullptr;  // full term index of each kept group's first term
+  const uint32_t* pre = nullptr;    // screened term index of each kept group's first term
+  const u64* off = nullptr;         // [n + 1] exclusive prefix of kept groups per source
+  const u64* kept_terms = nullptr;  // per source: terms of its kept groups (group 0 not counted)
+  unsigned gmax = 0;                // most kept groups of one source
+  u64 groups = 0, kept_groups = 0, kept_terms_total = 0;
+};
+// run the screen on n sources (keys: W words each; amps: the product's input amplitudes)
+int screen_select(Ctx& c, const void* keys, const double* amps, u64 n, ScreenList* out);
+// groups per source (group 0 excluded), exclusive prefix in goff[0..n]
+template <int W> int group_offsets_impl(Ctx& c, const typename KeyOf<W>::T* keys, u64 n, u64* goff);
+// label bits of the groups of n sources: a group is alive when one of its terms
+// lands on a key of `out` (the product's output); bit goff[j] + g - 1 of labels
+template <int W> int label_impl(Ctx& c, const typename KeyOf<W>::T* keys, const double* amps, u64 n,
+                                const u64* goff, const Vec& out, uint32_t* labels);
+
 // width dispatch used by the ABI and the drivers
 int op_spmspv(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, double* diag);
 int op_energy(Ctx& c, const Vec& psi, double* E);

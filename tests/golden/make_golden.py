@@ -42,7 +42,9 @@ from oracle import oracle as orc  # noqa: E402
 
 BUNIT = 1000000
 _ARGS = [a for a in sys.argv[1:] if not a.startswith("--")]
-REF = _ARGS[0] if _ARGS else os.environ.get("SFCI_REFERENCE_ROOT", "/root/reference")
+# the reference tree: the first argument, else $SFCI_REFERENCE_ROOT, else a
+# checkout named "reference" beside this repository
+REF = _ARGS[0] if _ARGS else os.environ.get("SFCI_REFERENCE_ROOT") or os.path.join(os.path.dirname(ROOT), "reference")
 
 # name, kind, M, ne, seeds, Nd for the Lanczos case (0 = no Lanczos)
 SYSTEMS = [
@@ -331,8 +333,64 @@ def linear():
             shutil.rmtree(tmp)
 
 
+def krylov56(Nd=20000, Nl=30, restarts=2):
+    """The truncated Lanczos driver on the 56-spin-orbital, 14-electron RHF system
+    of seed 1 at a truncating Nd, over the compiled reference's SpMSpV and vector
+    algebra (oracle.lanczos restates src/sparse_solver.cpp:246-548 around them),
+    and the same driver over the oracle restatement.  The two CPU runs break
+    magnitude ties at every top-Nd edge differently (the reference's introsort
+    arbitrarily, the restatement by key): RHF spin-mirror determinants tie
+    exactly, so their difference measures how far tie-breaking alone moves the
+    energy.  Output: lz_r28.npz."""
+    import time
+    so = orc.build_ref(REF)
+    if not so:
+        raise SystemExit("reference sources not available under %s" % REF)
+    ref = orc.RefLib(so)
+    M, ne, seed = 28, 14, 1
+    N = 2 * M
+    tmp = tempfile.mkdtemp()
+    try:
+        fpath = os.path.join(tmp, "sys_fcidump")
+        h, q, v, e = fd.synthetic_rhf(M, seed)
+        fd.write_fcidump_rhf(fpath, h, q, v, e, ne)
+        txt = ref_convert(fpath, "-r")
+        inp = os.path.join(tmp, "sys_IN")
+        open(inp, "w").write(txt)
+        hf = np.array([(1 << ne) - 1], np.uint64)
+        out = {"M": M, "ne": ne, "kind": "rhf", "seeds": np.array([seed]), "hf": np.uint64(hf[0]),
+               "in_sha256": hashlib.sha256(txt.encode()).hexdigest(), "L_Nd": Nd, "L_Nl": Nl,
+               "L_restarts": restarts, "L_hpsi_cap": 60000000}
+        nt = os.cpu_count()
+        ref.setup(inp, N, ne, Nd, bucket_unit=BUNIT, nthread=nt, num_connected=2000000)
+        # The reference sizes its final buffer as len * 5000 for an input of len
+        # determinants (src/functions.cpp:542,565): |HF> alone (len 1) has 12,770
+        # survivors and overflows it.  Two zero-amplitude excitations of |HF> make
+        # len 3; they add only zero terms, so every amplitude and energy is unchanged.
+        h0 = int(hf[0])
+        start = np.array(sorted([h0, h0 ^ (1 << 12) ^ (1 << 14), h0 ^ (1 << 13) ^ (1 << 15)]), np.uint64)
+        start_a = np.where(start == h0, 1.0, 0.0)
+        t = time.time()
+        en, fe, vec = orc.lanczos(ref, start, start_a, Nl, restarts, Nd, log=print)
+        out.update(L_energies=en, L_final_e=fe, L_vec_len=len(vec[1]), L_seconds=time.time() - t)
+        print("reference driver:", en, fe, "%.0f s" % (time.time() - t))
+        port = orc.PortLib(words=1)
+        port.setup(inp, N, ne, Nd, nthread=nt)
+        t = time.time()
+        en2, fe2, vec2 = orc.lanczos(port, hf, np.array([1.0]), Nl, restarts, Nd)
+        out.update(P_energies=en2, P_final_e=fe2, P_seconds=time.time() - t)
+        ka, kb = set(int(x) for x in vec[0]), set(int(x) for x in vec2[0])
+        out["P_vec_keys_differ"] = len(ka ^ kb)
+        print("restated driver:", en2, fe2, "keys differing in the final vectors:", len(ka ^ kb))
+        np.savez_compressed(os.path.join(HERE, "lz_r28.npz"), **out)
+    finally:
+        shutil.rmtree(tmp)
+
+
 if __name__ == "__main__":
-    if "--subspace" in sys.argv[1:]:
+    if "--krylov56" in sys.argv[1:]:
+        krylov56()
+    elif "--subspace" in sys.argv[1:]:
         subspace()
     elif "--linear" in sys.argv[1:]:
         linear()

@@ -106,3 +106,34 @@ def test_solver_entry_points_reject_null_arguments():
     assert name(L.sfci_shift_invert(None, None, 0.0, 5, 1, C.byref(d))) == "SFCI_ERR_ARG"
     assert name(L.sfci_cisd(None, None, 0, 1, None, None, None, C.byref(n))) == "SFCI_ERR_ARG"
     assert name(L.sfci_fci(None, 1, None, None, None, C.byref(n))) == "SFCI_ERR_ARG"
+
+
+def test_dot_noalloc_rejects_bad_arguments_without_a_device_call():
+    """sfci_dot_noalloc checks its arguments before any CUDA call: null pointers,
+    a key width other than 1 or 2 words, and sizes beyond the fixed scratch
+    array's 16,777,216 entries are SFCI_ERR_ARG (the pointers below are never
+    dereferenced)."""
+    L = sg.load_library()
+    f = L.sfci_dot_noalloc
+    f.restype = C.c_int
+    f.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p, C.c_uint64, C.c_int, C.c_void_p,
+                  C.c_void_p]
+    name = lambda st: L.sfci_status_name(st).decode()
+    p = 16  # a non-null placeholder address
+    cases = [
+        (p, p, 10, p, p, 10, 1, None),            # null d_out
+        (None, p, 10, p, p, 10, 1, p),            # null x keys with nx > 0
+        (p, None, 10, p, p, 10, 1, p),            # null x amplitudes
+        (p, p, 10, None, p, 10, 1, p),            # null y keys with ny > 0
+        (p, p, 10, p, None, 10, 2, p),            # null y amplitudes
+        (p, p, 10, p, p, 10, 3, p),               # three-word keys
+        (p, p, 10, p, p, 10, 0, p),               # zero-word keys
+        (p, p, 1 << 24, p, p, 1, 1, p),           # nx + ny = 2^24 + 1
+        (p, p, (1 << 24) + 1, p, p, 0, 1, p),     # nx alone beyond the limit
+        (p, p, 0, p, p, (1 << 24) + 1, 2, p),     # ny alone beyond the limit
+    ]
+    for c in cases:
+        st = f(c[0], c[1], c[2], c[3], c[4], c[5], c[6], c[7], None)
+        assert name(st) == "SFCI_ERR_ARG", c
+    st = f(p, p, 1 << 24, p, p, 1, 1, p, None)
+    assert b"16777216" in L.sfci_last_error()

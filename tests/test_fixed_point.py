@@ -5,8 +5,8 @@ The merge sums each determinant's terms as integers in units of 2^-64 (a
 low and a high addend per term, kept in two words without carries between
 them) and converts the sum back to double once.  So a merged amplitude must
 equal the correctly rounded (nearest, ties to even) value of the exact sum of
-the terms, each truncated toward zero to the 2^-64 grid, whatever the order of
-the terms."""
+the terms, each rounded to the nearest point of the 2^-64 grid (ties to even),
+whatever the order of the terms."""
 import ctypes as C
 import math
 import os
@@ -35,22 +35,30 @@ def fx(tmp_path_factory):
     L.gh_fx_sum.argtypes = [np.ctypeslib.ndpointer(np.float64), C.c_long, C.POINTER(C.c_int)]
     L.gh_fx_roundtrip.restype = C.c_double
     L.gh_fx_roundtrip.argtypes = [C.c_double, C.POINTER(C.c_int)]
+    L.gh_fx32_sum.restype = C.c_double
+    L.gh_fx32_sum.argtypes = [np.ctypeslib.ndpointer(np.float64), C.c_long, C.POINTER(C.c_int)]
     return L
 
 
-def trunc_grid(x):
-    q = Fraction(x) * (1 << FRAC)
-    return int(q) if q >= 0 else -int(-q)
+def to_grid(x):
+    """x * 2^64 rounded to the nearest integer, ties to even (Python's round of a Fraction)."""
+    return round(Fraction(x) * (1 << FRAC))
 
 
 def exact(terms):
-    return float(Fraction(sum(trunc_grid(float(t)) for t in terms), 1 << FRAC))
+    return float(Fraction(sum(to_grid(float(t)) for t in terms), 1 << FRAC))
 
 
 def fsum(L, terms):
     bad = C.c_int(0)
     a = np.ascontiguousarray(terms, dtype=np.float64)
     return L.gh_fx_sum(a, len(a), C.byref(bad)), bad.value
+
+
+def f32sum(L, terms):
+    big = C.c_int(0)
+    a = np.ascontiguousarray(terms, dtype=np.float64)
+    return L.gh_fx32_sum(a, len(a), C.byref(big)), big.value
 
 
 def test_random_sums_are_correctly_rounded(fx):
@@ -90,14 +98,36 @@ def test_rounding_ties_to_even(fx):
         assert got == -big
 
 
-def test_truncation_below_the_grid(fx):
+def test_rounding_to_the_grid(fx):
     bad = C.c_int(0)
-    assert fx.gh_fx_roundtrip(math.ldexp(1.0, -65), C.byref(bad)) == 0.0
-    assert fx.gh_fx_roundtrip(math.ldexp(1.0, -64), C.byref(bad)) == math.ldexp(1.0, -64)
-    assert fx.gh_fx_roundtrip(-math.ldexp(1.5, -64), C.byref(bad)) == -math.ldexp(1.0, -64)
-    for x in (1e-5, -0.3, 123.456, -7.5e6, 5e-300, 0.0, -0.0):
+    g = math.ldexp(1.0, -64)  # the grid unit
+    assert fx.gh_fx_roundtrip(math.ldexp(1.0, -66), C.byref(bad)) == 0.0   # 1/4 unit
+    assert fx.gh_fx_roundtrip(math.ldexp(1.0, -65), C.byref(bad)) == 0.0   # 1/2 unit: tie to even 0
+    assert fx.gh_fx_roundtrip(0.75 * g, C.byref(bad)) == g
+    assert fx.gh_fx_roundtrip(g, C.byref(bad)) == g
+    assert fx.gh_fx_roundtrip(-1.5 * g, C.byref(bad)) == -2 * g             # tie to even 2
+    assert fx.gh_fx_roundtrip(2.5 * g, C.byref(bad)) == 2 * g               # tie to even 2
+    assert fx.gh_fx_roundtrip(-2.75 * g, C.byref(bad)) == -3 * g
+    for x in (1e-5, -0.3, 123.456, -7.5e6, 5e-300, 0.0, -0.0, 1e-19, -3.3e-20):
         assert fx.gh_fx_roundtrip(x, C.byref(bad)) == exact([x])
     assert bad.value == 0
+
+
+def test_no_drift_over_many_same_sign_terms(fx):
+    """10^4 small terms of one sign on one key (a hot determinant near the cut):
+    with each term rounded to nearest the error grows like sqrt(n) * 2^-66, far
+    below the n * 2^-65 a truncation toward zero would accumulate."""
+    rng = np.random.default_rng(12)
+    n = 10000
+    for sign in (1.0, -1.0):
+        terms = sign * rng.uniform(1e-10, 1e-9, n)
+        got, bad = fsum(fx, terms)
+        assert bad == 0
+        ref = math.fsum(terms)
+        assert abs(got - ref) < 2e-18, (got, ref, got - ref)       # truncation: ~2.7e-16
+        assert abs(got - ref) <= 1e-12 * abs(ref)
+        f32, big = f32sum(fx, terms)
+        assert big == 0 and f32 == got
 
 
 def test_range_flag(fx):
@@ -119,25 +149,16 @@ def test_many_terms_on_one_accumulator(fx):
         terms = np.full(n, sign * big)
         got, bad = fsum(fx, terms)
         assert bad == 0
-        assert got == sign * float(Fraction(trunc_grid(big)) * n / (1 << FRAC))
+        assert got == sign * float(Fraction(to_grid(big)) * n / (1 << FRAC))
     rng = np.random.default_rng(3)
     terms = rng.uniform(-1, 1, n) * np.exp2(rng.uniform(-60, 23, n))
     got, _ = fsum(fx, terms)
-    assert got == float(Fraction(sum(trunc_grid(float(t)) for t in terms[:20000])
-                                 + sum(trunc_grid(float(t)) for t in terms[20000:]), 1 << FRAC))
+    assert got == float(Fraction(sum(to_grid(float(t)) for t in terms), 1 << FRAC))
 
 
 @pytest.fixture(scope="module")
 def fx32(fx):
-    fx.gh_fx32_sum.restype = C.c_double
-    fx.gh_fx32_sum.argtypes = [np.ctypeslib.ndpointer(np.float64), C.c_long, C.POINTER(C.c_int)]
     return fx
-
-
-def f32sum(L, terms):
-    big = C.c_int(0)
-    a = np.ascontiguousarray(terms, dtype=np.float64)
-    return L.gh_fx32_sum(a, len(a), C.byref(big)), big.value
 
 
 def test_digit_form_sums_exactly(fx32):
@@ -162,6 +183,6 @@ def test_digit_form_capacity_and_range(fx32):
     for sign in (1.0, -1.0):
         got, flag = f32sum(fx32, np.full(n, sign * big))
         assert flag == 0
-        assert got == sign * float(Fraction(trunc_grid(big)) * n / (1 << FRAC))
+        assert got == sign * float(Fraction(to_grid(big)) * n / (1 << FRAC))
     for x in (math.ldexp(1.0, 18), -3e5, float("inf"), float("nan")):
         assert f32sum(fx32, np.array([x]))[1] == 1

@@ -294,3 +294,46 @@ def test_pass_plans_give_identical_products(golden_in):
         assert np.array_equal(a.view(np.uint64), ref[1].view(np.uint64))
         assert close(d, ref[2])
     assert any(2 <= p <= 4 for p in seen[1:]) and any(p > 4 for p in seen[1:]), seen
+
+
+@pytest.mark.parametrize("nsrc,target", [(None, 5e-5), (1100, 1.2e-5)])
+def test_hot_key_sum_rounds_to_nearest(golden_in, port, nsrc, target):
+    """One determinant (|HF> of the 56-spin-orbital system) receives a term from
+    every input determinant: all 30,723 it connects to (a leaf for the CTA tier's
+    wide accumulators), or the 1,100 with the largest elements (a warp-table
+    leaf, narrow accumulators).  The amplitudes are chosen so that every term has
+    the same sign and the merged amplitude sits near the 1e-5 cut.  It must agree
+    within 1e-12 relative with math.fsum of the oracle's raw terms
+    (OffDiagGen_bit, src/bitstr.cpp:162-302, from the receiving side by the
+    symmetry of H).  Terms truncated toward zero would drift by n * 2.7e-20
+    (2.5e-12 to 1.7e-11 relative here); rounded to nearest they stay near
+    sqrt(n) * 1.6e-20."""
+    import math
+    g, path = golden_in("r28")
+    hf = (1 << 14) - 1
+    be = port.PortLib(words=1)
+    be.setup(path, 56, 14, 200000, nthread=8)
+    rk, ra = be.offdiag(np.array([hf], np.uint64))
+    keys, inv = np.unique(rk, return_inverse=True)
+    H = np.zeros(len(keys))
+    np.add.at(H, inv, ra)
+    if nsrc is not None:
+        keep = np.sort(np.argsort(-np.abs(H), kind="stable")[:nsrc])
+        sel = np.zeros(len(keys), bool)
+        sel[keep] = True
+        keys, H = keys[keep], H[keep]
+        raw = sel[inv]
+        rk, ra, inv = rk[raw], ra[raw], np.searchsorted(keys, rk[raw])
+    rng = np.random.default_rng(17)
+    w = rng.uniform(0.5, 1.5, len(keys))
+    amps = np.sign(H) * w
+    amps *= target / float(np.sum(np.abs(H) * w))
+    want = math.fsum(float(x) for x in amps[inv] * ra)
+    c = sg.Context(path, 56, 14, Nd=200000)
+    vin = c.vec_from(keys, amps)
+    out = c.vec(2000000)
+    c.SpMVMtply_bucket(vin, out, 0.0, 1.0)
+    k, a = out.download()
+    i = np.searchsorted(k, np.uint64(hf))
+    assert i < len(k) and k[i] == hf
+    assert abs(a[i] - want) <= 1e-12 * abs(want), (a[i], want, (a[i] - want) / want)

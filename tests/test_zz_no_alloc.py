@@ -87,8 +87,32 @@ def test_dot_noalloc_two_word_keys(golden_in):
         assert close(float(out.item()), ref)
 
 
-def test_dot_noalloc_rejects_oversize():
+def test_dot_noalloc_leaves_free_memory_unchanged(golden_in):
+    """After the first call (which looks up the fixed array's address), repeated
+    calls, including ones near the size limit, change the device's free memory
+    by nothing: the entry point allocates no device memory of its own."""
+    torch = pytest.importorskip("torch")
+    g, _ = golden_in("c1")
     L = _lib()
-    st = L.sfci_dot_noalloc(1, 1, 1 << 24, 1, 1, 1, 1, 1, None)
-    assert L.sfci_status_name(st).decode() == "SFCI_ERR_ARG"
-    assert b"16777216" in L.sfci_last_error()
+    n = (1 << 23) - 7  # two vectors of this length: close to the 16,777,216-entry limit
+    big_k = torch.arange(0, 2 * n, 2, dtype=torch.int64, device="cuda")
+    big_a = torch.ones(n, dtype=torch.float64, device="cuda")
+    dxk, dxa = _dev(torch, g["B_in_keys"]), _dev(torch, g["B_in_amps"])
+    dyk, dya = _dev(torch, g["B_keys"]), _dev(torch, g["B_amps"])
+    out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+
+    def call(xk, xa, nx, yk, ya, ny):
+        st = L.sfci_dot_noalloc(xk.data_ptr(), xa.data_ptr(), nx, yk.data_ptr(), ya.data_ptr(), ny, 1,
+                                out.data_ptr(), stream)
+        assert st == 0, L.sfci_last_error()
+
+    call(dxk, dxa, len(g["B_in_amps"]), dyk, dya, len(g["B_amps"]))
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(5):
+        call(dxk, dxa, len(g["B_in_amps"]), dyk, dya, len(g["B_amps"]))
+        call(big_k, big_a, n, big_k, big_a, n)
+    torch.cuda.synchronize()
+    assert float(out.item()) == float(n)
+    assert torch.cuda.mem_get_info()[0] == free0

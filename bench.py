@@ -342,10 +342,10 @@ def run_gpu(args, rank, ws, local, dist):
     nd = args.nd
     M, NE, W = sysd["M"], sysd["ne"], key_words(sysd)
     in_k, in_a = input_on_gpu(sg, path, sysd, nd)
-    ctx = sg.Context(path, 2 * M, NE, Nd=nd, hpsi_cap=HPSI_CAP, mem_budget=args.mem_budget)
+    ctx = sg.Context(path, 2 * M, NE, Nd=nd, hpsi_cap=HPSI_CAP, mem_budget=args.mem_budget, coeff_cut=args.cut)
     vin = ctx.vec_from(in_k, in_a, cap=nd)
     n_in = vin.len
-    out = ctx.vec(HPSI_CAP)
+    out = ctx.vec(args.out_cap or HPSI_CAP)
     C = connected_per_det(M, NE // 2, NE // 2)
     T_conn = n_in * C
     for _ in range(args.warmup):
@@ -602,6 +602,101 @@ def run_screen(args):
     print(json.dumps(res), flush=True)
 
 
+def run_batch(args):
+    """Batched bond-stretch curve: 32 instances (seed-4 synthetic RHF integrals
+    interpolated in t, 40-80 spin orbitals, 10-16 electrons, Nd geometric from
+    1e5 to 2e6 times --batch-scale), advanced together by the batched Lanczos
+    driver (one product over all instances per Krylov step), against the 32
+    unbatched runs one after another.  The product plan is autotuned on the
+    largest instance first."""
+    import sfci_gb300 as sg
+    from sfci_gb300 import fcidump as fd
+    sg.load_library()
+    curve = fd.bond_stretch_curve(32, 4, args.batch_scale)
+    d = os.path.join(tempfile.gettempdir(), "sfci_bench", "curve")
+    os.makedirs(d, exist_ok=True)
+    paths = []
+    t0 = time.perf_counter()
+    for k, inst in enumerate(curve):
+        p = os.path.join(d, "c%02d_m%d_ne%d_IN" % (k, inst["num_orb"] // 2, inst["num_e"]))
+        if not os.path.exists(p):
+            fd.bond_stretch_to_in_file(p + ".tmp", inst["num_orb"] // 2, inst["num_e"], 4, inst["t"])
+            os.replace(p + ".tmp", p)
+        paths.append(p)
+    t_files = time.perf_counter() - t0
+    Nl, R = args.batch_nl, 1
+    orbs = [x["num_orb"] for x in curve]
+    nes = [x["num_e"] for x in curve]
+    cap = int(sum(x["Nd"] for x in curve) * 200)
+    bc = sg.Context.batch(paths, orbs, nes, Nd=10 ** 9, hpsi_cap=min(cap, 400000000))
+    # autotune on the largest instance's two-step vector, in the batched context
+    big = len(curve) - 1
+    hf = bc.vec(1)
+    hf.upload(sg.tag_keys(np.array([[(1 << nes[big]) - 1, 0]], np.uint64), big), np.array([1.0]))
+    w = bc.vec(HPSI_CAP)
+    bc.SpMVMtply_bucket(hf, w, 0.0, 1.0)
+    w.normalize()
+    v2 = bc.vec(curve[big]["Nd"])
+    tmp = bc.vec(HPSI_CAP)
+    bc.SpMVMtply_bucket(w, tmp, 0.0, 1.0)
+    v2.shrinkFrom(tmp)
+    v2.normalize()
+    plan, plan_ms = bc.autotune(v2, tmp)
+    del hf, w, v2, tmp
+
+    def start_vectors(ctx, tagged):
+        vs = []
+        for k, inst in enumerate(curve):
+            v = ctx.vec(inst["Nd"])
+            key = np.array([[(1 << inst["num_e"]) - 1, 0]], np.uint64)
+            v.upload(sg.tag_keys(key, k) if tagged else key, np.array([1.0]))
+            vs.append(v)
+        return vs
+
+    bc.batch_lanczos(start_vectors(bc, True), 2, 1)  # warm-up: scratch allocation
+    vs = start_vectors(bc, True)
+    l0 = bc.launches()
+    tb0 = time.perf_counter()
+    en_b, fe_b = bc.batch_lanczos(vs, Nl, R)
+    t_batched = time.perf_counter() - tb0
+    launches_b = bc.launches() - l0
+    plan_b = bc.tuning()
+    bc.trim()
+    # unbatched: every instance in its own context, one after another
+    en_u, fe_u, t_un = [], [], 0.0
+    launches_u = 0
+    for k, inst in enumerate(curve):
+        c = sg.Context(paths[k], inst["num_orb"], inst["num_e"], Nd=inst["Nd"], hpsi_cap=HPSI_CAP)
+        c.set_tuning(**plan_b)
+        v = c.vec(inst["Nd"])
+        v.upload(sg.keys_from_ints([(1 << inst["num_e"]) - 1], c.words), np.array([1.0]))
+        l0 = c.launches()
+        ta = time.perf_counter()
+        e, f = c.sparse_krylov_solve_eigenval(v, Nl, R)
+        t_un += time.perf_counter() - ta
+        launches_u += c.launches() - l0
+        en_u.append(e)
+        fe_u.append(f)
+        del v, c
+    dE = [float(abs(fe_b[k] - fe_u[k])) for k in range(len(curve))]
+    dG = [float(np.nanmax(np.abs(en_b[k] - en_u[k]))) for k in range(len(curve))]
+    res = {"metric": METRIC, "mode": "batched bond-stretch curve", "unit": "s per batched Lanczos run",
+           "value": t_batched, "higher_is_better": False, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": "32-instance bond-stretch curve, seed-4 synthetic RHF interpolated in t "
+                                  "(off-diagonal x(1+3t), diagonal gap x(1-0.6t))",
+                      "num_orb": [min(orbs), max(orbs)], "num_e": [min(nes), max(nes)],
+                      "Nd": [curve[0]["Nd"], curve[-1]["Nd"]], "Nd_scale": args.batch_scale, "Nl": Nl,
+                      "restarts": R},
+           "instances": [{"t": x["t"], "num_orb": x["num_orb"], "num_e": x["num_e"], "Nd": x["Nd"],
+                          "energy": float(fe_b[k]), "dE_vs_unbatched": dE[k], "dE_gsaes": dG[k]}
+                         for k, x in enumerate(curve)],
+           "max_dE_vs_unbatched": max(dE), "max_dE_gsaes": max(dG),
+           "batched_seconds": t_batched, "unbatched_seconds": t_un, "speedup": t_un / t_batched,
+           "gpu_launches": {"batched": launches_b, "unbatched": launches_u},
+           "autotune": {"plan": plan_b, "ms": plan_ms}, "files_seconds": t_files}
+    print(json.dumps(res), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -615,6 +710,11 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-step-s", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cut", type=float, default=1e-5,
+                    help="post-merge cut of the timed product (profiling: a smaller cut gives more survivors)")
+    ap.add_argument("--out-cap", type=int, default=0,
+                    help="capacity of the product's output (profiling: a cap below the survivors runs the "
+                         "radix select and compaction)")
     ap.add_argument("--mem-budget", type=int, default=0,
                     help="device bytes the SpMSpV may use (0: 80%% of free); a small budget forces several "
                          "generation passes on a small case, e.g. for profiling")
@@ -628,9 +728,17 @@ def main():
     ap.add_argument("--screen-seed", type=int, default=5)
     ap.add_argument("--screen-tol", type=float, default=1e-5)
     ap.add_argument("--screen-thresholds", type=float, nargs="+", default=[0.02, 0.05, 0.1, 0.2, 0.35])
+    ap.add_argument("--batch", action="store_true",
+                    help="batched bond-stretch curve: 32 instances, batched vs unbatched Lanczos")
+    ap.add_argument("--batch-scale", type=float, default=0.01,
+                    help="scale of the instances' Nd (1.0: 1e5 to 2e6)")
+    ap.add_argument("--batch-nl", type=int, default=10)
     args = ap.parse_args()
     if args.screen:
         run_screen(args)
+        return
+    if args.batch:
+        run_batch(args)
         return
     rank, ws, local, dist = dist_init()
     try:

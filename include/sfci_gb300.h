@@ -47,7 +47,8 @@ typedef struct sfci_vec sfci_vec;
 typedef struct sfci_opts {
   uint64_t Nd;             /* Krylov truncation (default 200000, src/main.cpp:23) */
   uint64_t hpsi_cap;       /* capacity of H*v products (default 6e7, src/main.cpp:194) */
-  double coeff_cut;        /* post-merge magnitude cut (default 1e-5, src/main.cpp:196) */
+  double coeff_cut;        /* post-merge magnitude cut (0: the default 1e-5, src/main.cpp:196;
+                              negative: no cut, every merged determinant is kept) */
   uint64_t bucket_unit;    /* accepted and ignored: sizes come from prefix sums */
   uint64_t mem_budget;     /* bytes of device scratch the SpMSpV may use (0: 90% of free) */
   int verbose;             /* 1: print the reference's progress lines */
@@ -224,6 +225,27 @@ int sfci_fci(sfci_ctx* ctx, int n_evals, double* evals, sfci_vec* ground, double
 int sfci_dot_noalloc(const uint64_t* x_keys, const double* x_amps, uint64_t nx, const uint64_t* y_keys,
                      const double* y_amps, uint64_t ny, int key_words, double* d_out, void* stream);
 
+/* ---- batched instances (no counterpart in the reference) -------------------------
+ * A batched context holds n <= 32 Hamiltonians (each <= 120 spin orbitals, keys
+ * of two words): a key's top five bits (bits 123..127) name its instance, so
+ * vectors of different instances never merge and one product multiplies the
+ * vectors of every instance at once, each by its own Hamiltonian.  Tag keys with
+ * the instance before upload.  sfci_batch_lanczos runs sparse_krylov_solve_eigenval
+ * (src/sparse_solver.cpp:246-548) on every instance with one batched product
+ * per Krylov step; each instance's Nd is its vector's capacity; energies[i *
+ * restarts + r], final_e[i] per instance. */
+int sfci_batch_create(int n, const char* const* in_paths, const int* num_orb, const int* num_e,
+                      const sfci_opts* opts, sfci_ctx** out);
+int sfci_batch_lanczos(sfci_ctx* ctx, sfci_vec* const* v, int n, int Nl, int restarts, double* energies,
+                       double* final_e);
+/* Product plan tunables {level-1 bits 4-9, partition digit bits 6-9, distinct keys
+ * per leaf 16-120, generation CTAs per SM 1-2}: they change speed, never results
+ * (the merge is exact).  sfci_autotune times candidate plans on the product of
+ * `in` (into `out`), checks that they agree, and keeps the fastest. */
+int sfci_ctx_set_tuning(sfci_ctx* ctx, const int* tuning4);
+int sfci_ctx_get_tuning(const sfci_ctx* ctx, int* tuning4);
+int sfci_autotune(sfci_ctx* ctx, const sfci_vec* in, sfci_vec* out, int* best4, double* best_ms);
+
 /* ---- learned excitation screen (no counterpart in the reference) ---------------
  * A BF16 MLP (3 layers, hidden width 256, FP32 accumulation, sigmoid output),
  * trained and run on the tensor cores, that predicts for each term group of a
@@ -242,6 +264,9 @@ int sfci_dot_noalloc(const uint64_t* x_keys, const double* x_amps, uint64_t nx, 
  * sfci_energy are never screened, so calc_energy stays the judge of a screened
  * run's energy. */
 typedef struct sfci_screen sfci_screen;
+/* A screen lives on the context it is created on; destroying that context first
+ * frees the screen's device memory and leaves a handle that only
+ * sfci_screen_destroy accepts. */
 int sfci_screen_create(sfci_ctx* ctx, uint64_t seed, sfci_screen** out);
 int sfci_screen_destroy(sfci_screen* s);
 /* Appends labelled examples: every term group of the determinants of `in` (at

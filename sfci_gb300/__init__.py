@@ -98,6 +98,11 @@ def _sigs(L):
     L.sfci_krylov_linear.argtypes = [_vp, _vp, _vp, C.c_double, C.c_int, C.c_int, _vp]
     L.sfci_shift_invert.argtypes = [_vp, _vp, C.c_double, C.c_int, C.c_int, C.POINTER(C.c_double)]
     _u64p = C.POINTER(C.c_uint64)
+    L.sfci_batch_create.argtypes = [C.c_int, C.POINTER(C.c_char_p), _vp, _vp, C.POINTER(Opts), C.POINTER(_vp)]
+    L.sfci_batch_lanczos.argtypes = [_vp, C.POINTER(_vp), C.c_int, C.c_int, C.c_int, _vp, _vp]
+    L.sfci_ctx_set_tuning.argtypes = [_vp, _vp]
+    L.sfci_ctx_get_tuning.argtypes = [_vp, _vp]
+    L.sfci_autotune.argtypes = [_vp, _vp, _vp, _vp, C.POINTER(C.c_double)]
     L.sfci_screen_create.argtypes = [_vp, C.c_uint64, C.POINTER(_vp)]
     L.sfci_screen_destroy.argtypes = [_vp]
     L.sfci_screen_log.argtypes = [_vp, _vp, _vp, _u64p, _u64p]
@@ -204,11 +209,21 @@ def psi_read(path: str, num_orb: int, key_words: int = 1):
 
 
 
+INST_SHIFT = 59  # instance tag: the top five bits of a batched context's two-word keys
+
+
+def tag_keys(keys, inst: int):
+    """Two-word keys (n, 2) of batched instance `inst` (bits 123..127 of the key)."""
+    k = np.array(keys, dtype=np.uint64, copy=True).reshape(-1, 2)
+    k[:, 1] |= np.uint64(int(inst) << INST_SHIFT)
+    return k
+
+
 class Context:
     """Integrals + options + one CUDA stream (the reference's global state, made explicit)."""
 
     def __init__(self, in_path: str, num_orb: int, num_e: int, Nd: int = 200000, hpsi_cap: int = 60000000,
-                 coeff_cut: float = 1e-5, mem_budget: int = 0, verbose: bool = False):
+                 coeff_cut: float = 1e-5, mem_budget: int = 0, verbose: bool = False, _batch=None):
         self.L = load_library()
         o = Opts()
         o.Nd = int(Nd)
@@ -217,12 +232,52 @@ class Context:
         o.mem_budget = int(mem_budget)
         o.verbose = 1 if verbose else 0
         h = _vp()
-        _check(self.L.sfci_ctx_create(in_path.encode(), int(num_orb), int(num_e), C.byref(o), C.byref(h)))
+        if _batch is None:
+            _check(self.L.sfci_ctx_create(in_path.encode(), int(num_orb), int(num_e), C.byref(o), C.byref(h)))
+        else:
+            paths, orbs, nes = _batch
+            n = len(paths)
+            pa = (C.c_char_p * n)(*[p.encode() for p in paths])
+            oa = np.ascontiguousarray(orbs, np.int32)
+            ea = np.ascontiguousarray(nes, np.int32)
+            _check(self.L.sfci_batch_create(n, pa, _ptr(oa), _ptr(ea), C.byref(o), C.byref(h)))
+            self.instances = n
         self.h = h
         self.num_orb, self.num_e = num_orb, num_e
         self.words = self.L.sfci_key_words(h)
         self.Nd = int(Nd)
         self.hpsi_cap = int(hpsi_cap)
+
+    @classmethod
+    def batch(cls, in_paths, num_orbs, num_es, Nd: int = 200000, hpsi_cap: int = 60000000, **kw):
+        """A batched context: one Hamiltonian per instance (<= 32 instances, <= 120 spin
+        orbitals each); keys carry their instance in their top bits (tag_keys)."""
+        return cls(None, 128, max(num_es), Nd=Nd, hpsi_cap=hpsi_cap, _batch=(list(in_paths), num_orbs, num_es), **kw)
+
+    def batch_lanczos(self, vecs, Nl: int, num_restart: int):
+        """sparse_krylov_solve_eigenval on every instance, one batched product per Krylov step."""
+        n = len(vecs)
+        arr = (_vp * n)(*[v.h for v in vecs])
+        en = np.full(n * num_restart, np.nan)
+        fe = np.zeros(n)
+        _check(self.L.sfci_batch_lanczos(self.h, arr, n, int(Nl), int(num_restart), _ptr(en), _ptr(fe)))
+        return en.reshape(n, num_restart), fe
+
+    def tuning(self):
+        t = np.zeros(4, np.int32)
+        _check(self.L.sfci_ctx_get_tuning(self.h, _ptr(t)))
+        return dict(zip(["l1_bits", "digit_bits", "leaf_keys", "gen_ctas_per_sm"], [int(x) for x in t]))
+
+    def set_tuning(self, l1_bits=9, digit_bits=9, leaf_keys=120, gen_ctas_per_sm=2):
+        t = np.array([l1_bits, digit_bits, leaf_keys, gen_ctas_per_sm], np.int32)
+        _check(self.L.sfci_ctx_set_tuning(self.h, _ptr(t)))
+
+    def autotune(self, vin: "SpVec", vout: "SpVec"):
+        """Time the candidate product plans on vin and keep the fastest (results never depend on the plan)."""
+        t = np.zeros(4, np.int32)
+        ms = C.c_double()
+        _check(self.L.sfci_autotune(self.h, vin.h, vout.h, _ptr(t), C.byref(ms)))
+        return dict(zip(["l1_bits", "digit_bits", "leaf_keys", "gen_ctas_per_sm"], [int(x) for x in t])), ms.value
 
     def close(self):
         if getattr(self, "h", None):

@@ -7,6 +7,7 @@
 #include <string>
 #include <vector>
 
+#include "gen.cuh"
 #include "internal.h"
 #include "spmspv.h"
 
@@ -223,7 +224,8 @@ int sfci_ctx_create(const char* in_path, int num_orb, int num_e, const sfci_opts
   if (opts) c.opts = *opts;
   if (!c.opts.Nd) c.opts.Nd = 200000;
   if (!c.opts.hpsi_cap) c.opts.hpsi_cap = 60000000;
-  if (!(c.opts.coeff_cut > 0)) c.opts.coeff_cut = 1e-5;
+  // 0 (or NaN): the reference's 1e-5; a negative cut keeps every merged determinant
+  if (c.opts.coeff_cut == 0.0 || c.opts.coeff_cut != c.opts.coeff_cut) c.opts.coeff_cut = 1e-5;
   std::string err;
   int st = load_in_file(in_path, num_orb, c.ham, err);
   if (st) {
@@ -249,6 +251,159 @@ int sfci_ctx_create(const char* in_path, int num_orb, int num_e, const sfci_opts
   return SFCI_OK;
 }
 
+int sfci_batch_create(int n, const char* const* in_paths, const int* num_orb, const int* num_e,
+                      const sfci_opts* opts, sfci_ctx** out) {
+  if (!out || !in_paths || !num_orb || !num_e) return set_error(SFCI_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (n < 1 || n > INST_MAX) return set_error(SFCI_ERR_ARG, "a batch holds 1 to 32 instances");
+  for (int i = 0; i < n; ++i) {
+    if (!in_paths[i]) return set_error(SFCI_ERR_ARG, "null integral path");
+    if (num_orb[i] <= 0 || num_orb[i] > INST_MAX_ORB || (num_orb[i] & 1))
+      return set_error(SFCI_ERR_ARG, "batched instances need an even num_orb in [2, 120]");
+    if (num_e[i] < 0 || num_e[i] >= num_orb[i]) return set_error(SFCI_ERR_ARG, "num_e must be in [0, num_orb)");
+  }
+  sfci_ctx* x = new sfci_ctx();
+  Ctx& c = x->c;
+  c.ninst = n;
+  c.W = 2;
+  c.N = 128;  // sorts cover the instance tag
+  c.M = 0;
+  c.ne = 0;
+  for (int i = 0; i < n; ++i) {
+    c.M = std::max(c.M, num_orb[i] / 2);
+    c.ne = std::max(c.ne, num_e[i]);
+  }
+  c.P = c.M * (c.M + 1) / 2;
+  if (opts) c.opts = *opts;
+  if (!c.opts.Nd) c.opts.Nd = 200000;
+  if (!c.opts.hpsi_cap) c.opts.hpsi_cap = 60000000;
+  // 0 (or NaN): the reference's 1e-5; a negative cut keeps every merged determinant
+  if (c.opts.coeff_cut == 0.0 || c.opts.coeff_cut != c.opts.coeff_cut) c.opts.coeff_cut = 1e-5;
+  c.inst_ham.resize(n);
+  for (int i = 0; i < n; ++i) {
+    std::string err;
+    int st = load_in_file(in_paths[i], num_orb[i], c.inst_ham[i], err);
+    if (st) {
+      delete x;
+      return set_error(st, std::string("instance ") + std::to_string(i) + ": " + err);
+    }
+    c.inst_N.push_back(num_orb[i]);
+    c.inst_ne.push_back(num_e[i]);
+  }
+  c.ham = c.inst_ham[0];
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c.sm_count, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking);
+  std::vector<HamView> views(n);
+  c.inst_h1.assign(n, nullptr);
+  c.inst_V.assign(n, nullptr);
+  for (int i = 0; i < n && e == cudaSuccess; ++i) {
+    const HamHost& h = c.inst_ham[i];
+    e = cudaMalloc(&c.inst_h1[i], h.h1.size() * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&c.inst_V[i], h.V.size() * sizeof(double));
+    if (e == cudaSuccess)
+      e = cudaMemcpy(c.inst_h1[i], h.h1.data(), h.h1.size() * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(c.inst_V[i], h.V.data(), h.V.size() * sizeof(double), cudaMemcpyHostToDevice);
+    views[i].N = h.N;
+    views[i].M = h.M;
+    views[i].P = h.P;
+    views[i].h1 = c.inst_h1[i];
+    views[i].V = c.inst_V[i];
+    views[i].ecore = h.ecore;
+    views[i].inst = nullptr;
+  }
+  c.d_h1 = c.inst_h1[0];
+  c.d_V = c.inst_V[0];
+  if (e == cudaSuccess) e = cudaMalloc(&c.d_insts, n * sizeof(HamView));
+  if (e == cudaSuccess) e = cudaMemcpy(c.d_insts, views.data(), n * sizeof(HamView), cudaMemcpyHostToDevice);
+  for (int i = 0; i < 16 && e == cudaSuccess; ++i) e = cudaEventCreate(&c.ev[i]);
+  if (e != cudaSuccess) {
+    int s2 = cuda_fail(e, "batched context set-up");
+    sfci_ctx_destroy(x);
+    return s2;
+  }
+  *out = x;
+  return SFCI_OK;
+}
+
+int sfci_batch_lanczos(sfci_ctx* x, sfci_vec* const* v, int n, int Nl, int restarts, double* energies,
+                       double* final_e) {
+  if (!x || !v || !energies || !final_e) return set_error(SFCI_ERR_ARG, "null argument");
+  std::vector<Vec*> vs(n > 0 ? n : 0);
+  for (int i = 0; i < n; ++i) {
+    if (!v[i] || v[i]->v.ctx != &x->c) return set_error(SFCI_ERR_ARG, "batched Lanczos: vector of another context");
+    if (v[i]->v.len == 0) return set_error(SFCI_ERR_ARG, "batched Lanczos: an empty start vector");
+    vs[i] = &v[i]->v;
+  }
+  return lanczos_batched(x->c, vs.data(), n, Nl, restarts, energies, final_e);
+}
+
+int sfci_ctx_set_tuning(sfci_ctx* x, const int* t4) {
+  if (!x || !t4) return set_error(SFCI_ERR_ARG, "null argument");
+  if (t4[0] < 4 || t4[0] > 9 || t4[1] < 6 || t4[1] > 9 || t4[2] < 16 || t4[2] > 120 || t4[3] < 1 || t4[3] > 2)
+    return set_error(SFCI_ERR_ARG, "tuning out of range: l1 bits 4-9, digit bits 6-9, leaf keys 16-120, CTAs/SM 1-2");
+  Ctx& c = x->c;
+  c.tune_l1_bits = t4[0];
+  c.tune_digit_bits = t4[1];
+  c.tune_leaf_uniq = t4[2];
+  c.tune_gen_ctas = t4[3];
+  return SFCI_OK;
+}
+
+int sfci_ctx_get_tuning(const sfci_ctx* x, int* t4) {
+  if (!x || !t4) return set_error(SFCI_ERR_ARG, "null argument");
+  const Ctx& c = x->c;
+  t4[0] = c.tune_l1_bits;
+  t4[1] = c.tune_digit_bits;
+  t4[2] = c.tune_leaf_uniq;
+  t4[3] = c.tune_gen_ctas;
+  return SFCI_OK;
+}
+
+int sfci_autotune(sfci_ctx* x, const sfci_vec* in, sfci_vec* out, int* best4, double* best_ms) {
+  if (!x || !in || !out) return set_error(SFCI_ERR_ARG, "null argument");
+  Ctx& c = x->c;
+  // candidates: level-1 bins, partition digit width, leaf size, generation occupancy
+  static const int cand[][4] = {{9, 9, 120, 2}, {9, 8, 120, 2}, {8, 9, 120, 2}, {9, 9, 80, 2},
+                                {9, 9, 60, 2},  {9, 9, 120, 1}, {7, 8, 120, 2}, {9, 8, 80, 2}};
+  const int save[4] = {c.tune_l1_bits, c.tune_digit_bits, c.tune_leaf_uniq, c.tune_gen_ctas};
+  double best = 1e300;
+  int bi = 0;
+  uint64_t ref_len = 0;
+  double ref_diag = 0.0;
+  for (int k = 0; k < (int)(sizeof(cand) / sizeof(cand[0])); ++k) {
+    int st = sfci_ctx_set_tuning(x, cand[k]);
+    if (st) return st;
+    double dg = 0.0;
+    if ((st = op_spmspv(c, in->v, out->v, 0.0, 1.0, &dg))) return st;  // warm-up: scratch at this plan's sizes
+    cudaEvent_t e0 = c.ev[14], e1 = c.ev[15];
+    SFCI_CUDA(cudaEventRecord(e0, c.stream));
+    if ((st = op_spmspv(c, in->v, out->v, 0.0, 1.0, &dg))) return st;
+    SFCI_CUDA(cudaEventRecord(e1, c.stream));
+    SFCI_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    SFCI_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    // the merge is exact: every plan must give the same product
+    if (k == 0) {
+      ref_len = out->v.len;
+      ref_diag = dg;
+    } else if (out->v.len != ref_len || std::fabs(dg - ref_diag) > 1e-12 * std::fabs(ref_diag) + 1e-14) {
+      sfci_ctx_set_tuning(x, save);
+      return set_error(SFCI_ERR_NUMERIC, "autotune: plans disagree on the product");
+    }
+    if (ms < best) {
+      best = ms;
+      bi = k;
+    }
+  }
+  sfci_ctx_set_tuning(x, cand[bi]);
+  if (best4)
+    for (int i = 0; i < 4; ++i) best4[i] = cand[bi][i];
+  if (best_ms) *best_ms = best;
+  return SFCI_OK;
+}
+
 int sfci_ctx_destroy(sfci_ctx* x) {
   if (!x) return SFCI_OK;
   Ctx& c = x->c;
@@ -262,9 +417,17 @@ int sfci_ctx_destroy(sfci_ctx* x) {
     v->cap = v->len = 0;
   }
   c.live.clear();
+  for (Screen* s : std::set<Screen*>(c.screens)) screen_orphan(s);  // screens that outlive their context
+  c.screens.clear();
+  c.screen = nullptr;
   scratch_free_all(c);
   if (c.d_h1) cudaFree(c.d_h1);
   if (c.d_V) cudaFree(c.d_V);
+  for (size_t i = 1; i < c.inst_h1.size(); ++i) {  // instance 0's tables are d_h1 / d_V
+    if (c.inst_h1[i]) cudaFree(c.inst_h1[i]);
+    if (c.inst_V[i]) cudaFree(c.inst_V[i]);
+  }
+  if (c.d_insts) cudaFree(c.d_insts);
   for (int i = 0; i < 16; ++i)
     if (c.ev[i]) cudaEventDestroy(c.ev[i]);
   for (auto e : c.ev_pool) cudaEventDestroy(e);

@@ -32,7 +32,25 @@ struct HamView {
   const double* __restrict__ h1;  // [2][M][M]
   const double* __restrict__ V;   // [4][P][P]
   double ecore;
+  // Batched contexts: one view per instance, selected by the instance id that
+  // two-word keys carry in their top INST_BITS bits (nullptr: one Hamiltonian)
+  const HamView* inst;
 };
+
+// Instance tag of a batched context's keys: bits 123..127 of a two-word key
+// (instances need at most 120 spin orbitals, so the tag never meets an orbital
+// bit).  Keys of different instances never compare equal, so one product
+// merges every instance's terms separately.
+constexpr int INST_BITS = 5;
+constexpr int INST_SHIFT = 64 - INST_BITS;  // within the high word
+constexpr int INST_MAX = 1 << INST_BITS;
+constexpr int INST_MAX_ORB = 120;
+SFCI_HD unsigned inst_of(const u64&) { return 0u; }
+SFCI_HD unsigned inst_of(const K128& k) { return (unsigned)(k.hi >> INST_SHIFT); }
+template <class KT>
+SFCI_HD HamView ham_for(const HamView& h, const KT& k) {
+  return h.inst ? h.inst[inst_of(k)] : h;
+}
 
 // Single-excitation descriptor of spin orbitals i (occupied) -> a (empty):
 // i | a << 7 | spatial_pair(i>>1, a>>1) << 14 | phase << 26, where the phase

@@ -62,8 +62,23 @@ struct Ctx {
   // pinned host staging for small readbacks
   u64* h_pin = nullptr;
   size_t h_pin_words = 0;
+  // batched contexts: one Hamiltonian per instance (device HamView table);
+  // ninst = 0 for an ordinary context
+  int ninst = 0;
+  std::vector<HamHost> inst_ham;
+  std::vector<double*> inst_h1, inst_V;
+  std::vector<int> inst_N, inst_ne;
+  void* d_insts = nullptr;
+  std::vector<double> inst_diag;  // <v|Hv> of each instance, from the last product
+  // tunables of the product (the autotuner sets them; results do not depend on them)
+  int tune_l1_bits = 9;       // level-1 bins of the generation sweep: 2^bits
+  int tune_digit_bits = 9;    // most bits per partition level
+  int tune_leaf_uniq = 120;   // distinct keys a leaf is sized for
+  int tune_gen_ctas = 2;      // generation CTAs per SM
   // learned excitation screen applied by the products (nullptr: plain products)
   struct Screen* screen = nullptr;
+  // screens created on this context (freed with it; their handles become orphans)
+  std::set<struct Screen*> screens;
   double screen_thr = 0.5;
   uint64_t screen_stats[4] = {};  // groups, kept groups, kept terms, screened products
 };
@@ -74,6 +89,9 @@ struct Vec {
   u64* keys = nullptr;   // len*W words
   double* amps = nullptr;
 };
+
+// release a screen's device memory and detach it from its context (mlp.cu)
+void screen_orphan(struct Screen* s);
 
 // growable named device scratch (contents not preserved on growth)
 void* scratch_get(Ctx& c, const char* name, size_t bytes);

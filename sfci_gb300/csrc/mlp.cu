@@ -1234,6 +1234,23 @@ struct sfci_screen {
 
 using namespace sfci;
 
+namespace sfci {
+void screen_orphan(Screen* s) {
+  if (!s) return;
+  if (s->ctx) {
+    cudaStreamSynchronize(s->ctx->stream);
+    if (s->ctx->screen == s) s->ctx->screen = nullptr;
+    s->ctx->screens.erase(s);
+  }
+  for (void*& p : s->owned)
+    if (p) {
+      cudaFree(p);
+      p = nullptr;
+    }
+  s->ctx = nullptr;
+}
+}  // namespace sfci
+
 extern "C" int sfci_screen_create(sfci_ctx* ctx, uint64_t seed, sfci_screen** out) {
   if (!ctx || !out) return set_error(SFCI_ERR_ARG, "sfci_screen_create: null argument");
   *out = nullptr;
@@ -1246,16 +1263,16 @@ extern "C" int sfci_screen_create(sfci_ctx* ctx, uint64_t seed, sfci_screen** ou
     delete x;
     return st;
   }
+  ctx->c.screens.insert(&x->s);
   *out = x;
   return SFCI_OK;
 }
 
+// A screen whose context was destroyed first is an orphan: its device memory
+// went with the context, and only the handle is left to free.
 extern "C" int sfci_screen_destroy(sfci_screen* x) {
   if (!x) return SFCI_OK;
-  if (x->s.ctx && x->s.ctx->screen == &x->s) x->s.ctx->screen = nullptr;
-  if (x->s.ctx) cudaStreamSynchronize(x->s.ctx->stream);
-  for (void* p : x->s.owned)
-    if (p) cudaFree(p);
+  screen_orphan(&x->s);
   delete x;
   return SFCI_OK;
 }
@@ -1263,6 +1280,7 @@ extern "C" int sfci_screen_destroy(sfci_screen* x) {
 extern "C" int sfci_screen_log(sfci_screen* x, const sfci_vec* in, const sfci_vec* out, uint64_t* examples,
                                uint64_t* positives) {
   if (!x || !in || !out) return set_error(SFCI_ERR_ARG, "sfci_screen_log: null argument");
+  if (!x->s.ctx) return set_error(SFCI_ERR_ARG, "sfci_screen_log: the screen's context was destroyed");
   if (!in->v.ctx || !out->v.ctx) return set_error(SFCI_ERR_ARG, "sfci_screen_log: vector of a destroyed context");
   u64 ne = 0, np = 0;
   int st = screen_log(x->s, in->v, out->v, &ne, &np);
@@ -1274,6 +1292,7 @@ extern "C" int sfci_screen_log(sfci_screen* x, const sfci_vec* in, const sfci_ve
 extern "C" int sfci_screen_train(sfci_screen* x, int steps, int batch_tiles, double lr, double pos_weight,
                                  int sequential, double* loss) {
   if (!x || steps < 0 || batch_tiles <= 0) return set_error(SFCI_ERR_ARG, "sfci_screen_train: bad argument");
+  if (!x->s.ctx) return set_error(SFCI_ERR_ARG, "sfci_screen_train: the screen's context was destroyed");
   return screen_train(x->s, steps, (unsigned)batch_tiles, lr, pos_weight, sequential, loss);
 }
 
@@ -1291,6 +1310,8 @@ extern "C" int sfci_screen_predict(sfci_screen* x, const sfci_vec* in, double th
                                    uint64_t* kept_groups, uint64_t* kept_terms, float* prob_host,
                                    uint64_t prob_cap) {
   if (!x || !in) return set_error(SFCI_ERR_ARG, "sfci_screen_predict: null argument");
+  if (!x->s.ctx || in->v.ctx != x->s.ctx)
+    return set_error(SFCI_ERR_ARG, "sfci_screen_predict: a vector of the screen's own (live) context");
   Screen& s = x->s;
   Ctx& c = *s.ctx;
   int st;
@@ -1330,6 +1351,7 @@ extern "C" int sfci_screen_predict(sfci_screen* x, const sfci_vec* in, double th
 extern "C" int sfci_screen_params(sfci_screen* x, float* get, const float* set, uint64_t n) {
   if (!x) return set_error(SFCI_ERR_ARG, "sfci_screen_params: null screen");
   if (n != NPARAM) return set_error(SFCI_ERR_ARG, "sfci_screen_params: n must be the parameter count");
+  if (!x->s.ctx) return set_error(SFCI_ERR_ARG, "sfci_screen_params: the screen's context was destroyed");
   Ctx& c = *x->s.ctx;
   if (get) {
     SFCI_CUDA(cudaStreamSynchronize(c.stream));
@@ -1347,6 +1369,7 @@ extern "C" int sfci_screen_params(sfci_screen* x, float* get, const float* set, 
 extern "C" int sfci_screen_grads(sfci_screen* x, float* get, uint64_t n) {
   if (!x || !get) return set_error(SFCI_ERR_ARG, "sfci_screen_grads: null argument");
   if (n != NPARAM) return set_error(SFCI_ERR_ARG, "sfci_screen_grads: n must be the parameter count");
+  if (!x->s.ctx) return set_error(SFCI_ERR_ARG, "sfci_screen_grads: the screen's context was destroyed");
   SFCI_CUDA(cudaStreamSynchronize(x->s.ctx->stream));
   SFCI_CUDA(cudaMemcpy(get, x->s.grads, NPARAM * sizeof(float), cudaMemcpyDeviceToHost));
   return SFCI_OK;

@@ -431,3 +431,189 @@ int sfci_minres(sfci_ctx* x, const sfci_vec* rhs, const sfci_vec* guess, sfci_ve
 }
 
 }  // extern "C"
+
+namespace sfci {
+
+// ---- batched instances ------------------------------------------------------------
+// sparse_krylov_solve_eigenval (src/sparse_solver.cpp:246-548) on n instances
+// of a batched context at once.  Every Krylov step is ONE product over all
+// active instances: their vectors (keys tagged by instance, so concatenation in
+// instance order is key order) are concatenated, multiplied by one pass of the
+// product pipeline, and the result is split at the instance tags.  Each
+// instance's <v|Hv> comes from the same pass.  The rest of the step (dots,
+// axpys, truncation to the instance's Nd = its vector capacity, the Nl x Nl
+// eigenproblem) is per instance, as in the single-instance driver.  The merge is
+// exact, so each instance's product equals its unbatched product bit for bit;
+// energies agree with unbatched runs to the rounding of the <v|Hv> partial sums.
+namespace {
+struct GrowVec {
+  DVec d;
+  int need(Ctx& c, uint64_t cap) {
+    if (d.v.keys && d.v.cap >= cap) return SFCI_OK;
+    if (d.v.keys) cudaFree(d.v.keys);
+    if (d.v.amps) cudaFree(d.v.amps);
+    d.v.keys = nullptr;
+    d.v.amps = nullptr;
+    return d.alloc(c, std::max<uint64_t>(cap, 1024));
+  }
+};
+struct Inst {
+  Vec* v = nullptr;
+  uint64_t Nd = 0;
+  std::vector<std::unique_ptr<DVec>> KB;
+  GrowVec u, temp, temp_u;
+  DVec v_next, vv;
+  std::vector<double> KM, S, ev, X;
+  double previousE = 0.0, nearestE = -1000000.0, alpha = 0.0, beta = 0.0;
+  bool active = true;
+};
+}  // namespace
+
+// one product over the instances in `idx` (inputs in[i]), outputs split into out[i]
+static int batched_product(Ctx& c, std::vector<Inst>& S, const std::vector<int>& idx, GrowVec& all_in,
+                           GrowVec& all_out, bool use_next, int nin) {
+  uint64_t tot = 0;
+  for (int i : idx) tot += use_next ? S[i].v_next.v.len : S[i].v->len;
+  TRY(all_in.need(c, tot));
+  uint64_t o = 0;
+  for (int i : idx) {
+    const Vec& x = use_next ? S[i].v_next.v : *S[i].v;
+    if (x.len) {
+      SFCI_CUDA(cudaMemcpyAsync(all_in.d.v.keys + o * 2, x.keys, x.len * 2 * sizeof(u64), cudaMemcpyDeviceToDevice,
+                                c.stream));
+      SFCI_CUDA(cudaMemcpyAsync(all_in.d.v.amps + o, x.amps, x.len * sizeof(double), cudaMemcpyDeviceToDevice,
+                                c.stream));
+    }
+    o += x.len;
+  }
+  all_in.d.v.len = tot;
+  TRY(all_out.need(c, c.opts.hpsi_cap));
+  double dg = 0.0;
+  const uint64_t Nd = c.opts.Nd;
+  c.opts.Nd = std::max<uint64_t>(Nd, tot);  // each instance is already truncated to its own Nd
+  int st = op_spmspv(c, all_in.d.v, all_out.d.v, 0.0, 1.0, &dg);
+  c.opts.Nd = Nd;
+  TRY(st);
+  std::vector<u64> b(nin + 1);
+  TRY(inst_bounds(c, all_out.d.v, nin, b.data()));
+  for (int i : idx) {
+    GrowVec& dst = use_next ? S[i].temp_u : S[i].u;
+    const uint64_t n = b[i + 1] - b[i];
+    // room for the axpy that follows (at most Nd more entries), as the single
+    // driver's HPsiCap-sized vectors have
+    TRY(dst.need(c, std::min<uint64_t>(c.opts.hpsi_cap, n + S[i].Nd)));
+    if (n) {
+      SFCI_CUDA(cudaMemcpyAsync(dst.d.v.keys, all_out.d.v.keys + b[i] * 2, n * 2 * sizeof(u64),
+                                cudaMemcpyDeviceToDevice, c.stream));
+      SFCI_CUDA(cudaMemcpyAsync(dst.d.v.amps, all_out.d.v.amps + b[i], n * sizeof(double), cudaMemcpyDeviceToDevice,
+                                c.stream));
+    }
+    dst.d.v.len = n;
+    S[i].alpha = c.inst_diag.size() > (size_t)i ? c.inst_diag[i] : 0.0;
+  }
+  return SFCI_OK;
+}
+
+int lanczos_batched(Ctx& c, Vec* const* v, int n, int Nl, int restarts, double* energies, double* final_e) {
+  if (!c.ninst || c.W != 2) return set_error(SFCI_ERR_ARG, "batched Lanczos needs a batched context");
+  if (n != c.ninst) return set_error(SFCI_ERR_ARG, "batched Lanczos: one vector per instance");
+  if (Nl < 2 || restarts < 1) return set_error(SFCI_ERR_ARG, "batched Lanczos: Nl >= 2 and restarts >= 1");
+  std::vector<Inst> S(n);
+  for (int i = 0; i < n; ++i) {
+    Inst& s = S[i];
+    s.v = v[i];
+    s.Nd = v[i]->cap;
+    s.KB.resize(Nl);
+    for (int k = 0; k < Nl; ++k) {
+      s.KB[k].reset(new DVec);
+      TRY(s.KB[k]->alloc(c, s.Nd));
+    }
+    TRY(s.v_next.alloc(c, s.Nd));
+    TRY(s.vv.alloc(c, (uint64_t)Nl * s.Nd));
+    s.KM.assign((size_t)Nl * Nl, 0.0);
+    s.S.assign((size_t)Nl * Nl, 0.0);
+    s.ev.assign(Nl, 0.0);
+    s.X.assign((size_t)Nl * Nl, 0.0);
+    for (int r = 0; r < restarts; ++r) energies[(size_t)i * restarts + r] = std::numeric_limits<double>::quiet_NaN();
+  }
+  GrowVec all_in, all_out;
+  const double deltaE = 1e-5;
+  for (int res = 0; res < restarts; ++res) {
+    std::vector<int> idx;
+    for (int i = 0; i < n; ++i)
+      if (S[i].active) idx.push_back(i);
+    if (idx.empty()) break;
+    for (int i : idx) TRY(op_copy(c, S[i].KB[0]->v, *S[i].v));
+    TRY(batched_product(c, S, idx, all_in, all_out, false, n));
+    for (int i : idx) {
+      auto km = [&](int a, int b) -> double& { return S[i].KM[(size_t)b * Nl + a]; };
+      km(0, 0) = S[i].alpha;
+    }
+    for (int it = 1; it < Nl; ++it) {
+      for (int i : idx) {
+        Inst& s = S[i];
+        TRY(s.temp.need(c, std::min<uint64_t>(c.opts.hpsi_cap, s.u.d.v.len + s.v->len)));
+        TRY(op_copy(c, s.temp.d.v, s.u.d.v));
+        TRY(op_add_two(c, s.temp.d.v, *s.v, -s.alpha));
+        TRY(op_shrink(c, s.v_next.v, s.temp.d.v));
+        double gamma = 0.0;
+        TRY(norm_of(c, s.v_next.v, &gamma));
+        s.beta = gamma;
+        TRY(scale_impl(c, s.v_next.v, 1.0 / gamma));
+      }
+      TRY(batched_product(c, S, idx, all_in, all_out, true, n));
+      for (int i : idx) {
+        Inst& s = S[i];
+        auto km = [&](int a, int b) -> double& { return s.KM[(size_t)b * Nl + a]; };
+        km(it, it) = s.alpha;
+        for (int j = 0; j < it; ++j) {
+          double d = 0.0;
+          TRY(op_dot(c, s.KB[j]->v, s.temp_u.d.v, &d));
+          km(j, it) = d;
+          km(it, j) = d;
+        }
+        TRY(op_add_two(c, s.temp_u.d.v, *s.v, -s.beta));
+        TRY(s.u.need(c, s.temp_u.d.v.len));
+        TRY(op_copy(c, s.u.d.v, s.temp_u.d.v));
+        TRY(op_copy(c, *s.v, s.v_next.v));
+        TRY(op_copy(c, s.KB[it]->v, *s.v));
+      }
+    }
+    for (int i : idx) {
+      Inst& s = S[i];
+      auto sm = [&](int a, int b) -> double& { return s.S[(size_t)b * Nl + a]; };
+      for (int a = 0; a < Nl; ++a)
+        for (int b = a; b < Nl; ++b) {
+          double d = 0.0;
+          TRY(op_dot(c, s.KB[a]->v, s.KB[b]->v, &d));
+          sm(a, b) = d;
+          sm(b, a) = d;
+        }
+      TRY(gsaes_impl(Nl, s.KM.data(), s.S.data(), s.ev.data(), s.X.data()));
+      int k = 0;
+      double gap = std::fabs(s.nearestE - s.ev[0]);
+      for (int a = 1; a < Nl; ++a)
+        if (std::fabs(s.nearestE - s.ev[a]) < gap) {
+          gap = std::fabs(s.nearestE - s.ev[a]);
+          k = a;
+        }
+      s.nearestE = s.ev[k];
+      std::vector<const Vec*> ptr(Nl);
+      for (int a = 0; a < Nl; ++a) ptr[a] = &s.KB[a]->v;
+      TRY(op_combine(c, s.vv.v, ptr.data(), s.X.data() + (size_t)k * Nl, Nl));
+      TRY(op_shrink(c, *s.v, s.vv.v));
+      double nv = 0.0;
+      TRY(norm_of(c, *s.v, &nv));
+      TRY(scale_impl(c, *s.v, 1.0 / nv));
+      std::fill(s.KM.begin(), s.KM.end(), 0.0);
+      for (int a = 0; a < Nl; ++a) s.KB[a]->v.len = 0;
+      energies[(size_t)i * restarts + res] = s.ev[k];
+      if (s.previousE - s.ev[k] < deltaE) s.active = false;  // the signed test of :535
+      s.previousE = s.ev[k];
+    }
+  }
+  for (int i = 0; i < n; ++i) TRY(op_energy(c, *S[i].v, &final_e[i]));
+  return SFCI_OK;
+}
+
+}  // namespace sfci

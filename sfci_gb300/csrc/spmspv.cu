@@ -178,11 +178,12 @@ __global__ void k_det_prep(const KT* __restrict__ keys, u64 n, HamView h, u64* _
   u64 nw = ((u64)gridDim.x * blockDim.x) >> 5;
   for (; w < n; w += nw) {
     KT k = keys[w];
-    double D = diag_element_warp(k, h);
+    const HamView hk = ham_for(h, k);
+    double D = diag_element_warp(k, hk);
     if (lane == 0) {
       unsigned a0, a1;
-      spin_counts(k, h.N, a0, a1);
-      unsigned v0 = h.M - a0, v1 = h.M - a1;
+      spin_counts(k, hk.N, a0, a1);
+      unsigned v0 = hk.M - a0, v1 = hk.M - a1;
       cnt[w] = det_terms(a0, v0, a1, v1);
       diagE[w] = D;
     }
@@ -363,7 +364,8 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
       break;
     }
     const u64 dbeg = g.doff[det], dend = g.doff[det + 1];
-    if (tid < 32) det_setup_warp(d, g.keys[det], g.coeff * g.amps[det], g.diagE[det], g.lambda, g.h.M);
+    const HamView hv = ham_for(g.h, g.keys[det]);  // this determinant's Hamiltonian
+    if (tid < 32) det_setup_warp(d, g.keys[det], g.coeff * g.amps[det], g.diagE[det], g.lambda, hv.M);
     if (tid == 0 && det >= g.nmain) d.h.dterm = g.amps[det];  // a single term, as given
     const bool screened = (MODE == M_COUNT || MODE == M_SCATTER) && g.kl_start && det < g.nmain;
     if (screened) {
@@ -458,7 +460,7 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
             key = dh.key;
             amp = dh.dterm;
           } else {
-            amp = double_term(dh, d, pt, g.h, remap(l), key);
+            amp = double_term(dh, d, pt, hv, remap(l), key);
           }
           g.okeys[pos] = key;
           g.oamps[pos] = amp;
@@ -471,7 +473,7 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
             const bool act = q < nsq;
             const unsigned i = act ? sq[q] : 0u;
             const Exc e = decode(dh, pt, rb + sx[i]);
-            const double v = single_amp_half(dh, d, e, g.h, act && e.cls == 1);
+            const double v = single_amp_half(dh, d, e, hv, act && e.cls == 1);
             if (act && (tid & 15) == 0) {
               const u64 pos = rbase[sb[i]] + i;
               g.okeys[pos] = target_key(dh, d, e);
@@ -500,7 +502,7 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
               const Exc e = decode(dh, pt, l);
               const KT key = target_key(dh, d, e);
               int s = table_find_global(g.tkeys, g.tmask, key);
-              if (s >= 0) eacc += term_amp(dh, d, e, g.h) * __ldcg(g.tvals + s);
+              if (s >= 0) eacc += term_amp(dh, d, e, hv) * __ldcg(g.tvals + s);
             }
           }
           if (MODE == M_PROJECT && l < l1) {
@@ -510,7 +512,7 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
             const int s = table_find_global(g.tkeys, g.tmask, target_key(dh, d, e));
             if (s >= 0) {
               u64 xl, xh;
-              fx_addends(term_amp(dh, d, e, g.h), xl, xh, pbad);
+              fx_addends(term_amp(dh, d, e, hv), xl, xh, pbad);
               fx_red(g.plo + s, g.phi + s, xl, xh);
             }
           }
@@ -718,6 +720,7 @@ struct LeafArgs {
   unsigned ovf_cap;
   u64* uniq;           // merged distinct determinants (statistics)
   unsigned* bad;       // set when a term is outside the fixed-point range
+  double* dinst;       // nullable: <v|Hv> per instance of a batched context
 };
 
 // Shared-memory layout of a merge table with `n` slots: keys, then the low and
@@ -828,7 +831,11 @@ __global__ void __launch_bounds__(LW_WARPS * 32, sizeof(KT) == 8 ? 4 : 3) k_leaf
     for (u64 e = a.in_off[gl] + lane; e < a.in_off[gl + 1]; e += 32) {
       const KT k = a.in_keys[e];
       int s = table_find(t.k, tb - 1, k, leaf_slot(k, tbits));
-      if (s >= 0) dacc += t.amp(s) * a.in_amps[e];
+      if (s >= 0) {
+        const double x = t.amp(s) * a.in_amps[e];
+        dacc += x;
+        if (a.dinst) atomicAdd(a.dinst + inst_of(k), x);
+      }
     }
     for (unsigned base = 0; base < tb; base += 32) {
       const unsigned s = base + lane;
@@ -953,7 +960,11 @@ __global__ void __launch_bounds__(LC_THREADS) k_leafc(LeafArgs<KT> a, const unsi
     for (u64 e = a.in_off[gl] + tid; e < a.in_off[gl + 1]; e += LC_THREADS) {
       const KT k = a.in_keys[e];
       int s = table_find(t.k, LC_SLOTS - 1, k, (unsigned)slot_hash(k) & (LC_SLOTS - 1));
-      if (s >= 0) dacc += t.amp(s) * a.in_amps[e];
+      if (s >= 0) {
+        const double x = t.amp(s) * a.in_amps[e];
+        dacc += x;
+        if (a.dinst) atomicAdd(a.dinst + inst_of(k), x);
+      }
     }
     constexpr int PER = LC_SLOTS / LC_THREADS;
     unsigned c = 0, cu = 0;
@@ -1029,13 +1040,17 @@ __global__ void k_big_insert(const KT* __restrict__ keys, const double* __restri
 template <class KT>
 __global__ void k_big_finish(const KT* tk, const u64* tl, const u64* th, unsigned mask, const KT* in_keys,
                              const double* in_amps, u64 ib, u64 ie, FxCut cut, KT* skeys, double* samps,
-                             u64* scount, double* dsum, u64* uniq, double* qsum) {
+                             u64* scount, double* dsum, u64* uniq, double* qsum, double* dinst) {
   const KT empty = key_empty<KT>();
   u64 gt = (u64)blockIdx.x * blockDim.x + threadIdx.x, gs = (u64)gridDim.x * blockDim.x;
   double acc = 0.0, qacc = 0.0;
   for (u64 e = ib + gt; e < ie; e += gs) {
     int s = table_find_global(tk, mask, in_keys[e]);
-    if (s >= 0) acc += fx_to_double(__ldcg(tl + s), __ldcg(th + s)) * in_amps[e];
+    if (s >= 0) {
+      const double x = fx_to_double(__ldcg(tl + s), __ldcg(th + s)) * in_amps[e];
+      acc += x;
+      if (dinst) atomicAdd(dinst + inst_of(in_keys[e]), x);
+    }
   }
   if (acc != 0.0) atomicAdd(dsum, acc);
   for (u64 s = gt; s <= mask; s += gs) {
@@ -1122,6 +1137,7 @@ static HamView ham_view(Ctx& c) {
   h.h1 = c.d_h1;
   h.V = c.d_V;
   h.ecore = c.ham.ecore;
+  h.inst = (const HamView*)c.d_insts;
   return h;
 }
 
@@ -1181,7 +1197,7 @@ static int prep_dets(Ctx& c, const typename KeyOf<W>::T* keys, u64 n, u64** doff
 }
 
 static unsigned gen_grid(Ctx& c, u64 T) {
-  u64 g = (u64)c.sm_count * 2;
+  u64 g = (u64)c.sm_count * std::max(1, std::min(2, c.tune_gen_ctas));
   u64 need = (T + GEN_ROUND - 1) / GEN_ROUND;
   if (need < g) g = need;
   return (unsigned)(g ? g : 1);
@@ -1302,10 +1318,13 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
   // distinct key) of the previous product on this context (default 8).
   const double dup = c.dup_est > 0.0 ? c.dup_est : 8.0;
   const double uniq_est = std::max(1.0, (double)T / std::max(1.0, dup));
-  const int b = std::max(1, std::min(B_MAX, (int)std::ceil(std::log2(std::max(2.0, uniq_est / TW_UNIQ)))));
-  const int d0 = std::min(b, L1_BITS);
+  const int leaf_uniq = std::max(16, std::min(TW_UNIQ, c.tune_leaf_uniq));
+  const int l1_bits = std::max(4, std::min(L1_BITS, c.tune_l1_bits));
+  const int digit_bits = std::max(6, std::min(DIGIT_MAX, c.tune_digit_bits));
+  const int b = std::max(1, std::min(B_MAX, (int)std::ceil(std::log2(std::max(2.0, uniq_est / leaf_uniq)))));
+  const int d0 = std::min(b, l1_bits);
   const int rem = b - d0;
-  const int nlev = rem ? (rem + DIGIT_MAX - 1) / DIGIT_MAX : 0;
+  const int nlev = rem ? (rem + digit_bits - 1) / digit_bits : 0;
   std::vector<int> dig(nlev);
   for (int k = 0; k < nlev; ++k) dig[k] = rem / nlev + (k < rem % nlev ? 1 : 0);
   const unsigned NB1 = 1u << d0;
@@ -1438,6 +1457,12 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
   double* dbig = (double*)scratch_get(c, "sp_dbig", sizeof(double));
   if (!dbig) return SFCI_ERR_NOMEM;
   SFCI_CUDA(cudaMemsetAsync(dbig, 0, sizeof(double), c.stream));
+  double* dinst = nullptr;  // batched contexts: <v|Hv> per instance
+  if (c.ninst) {
+    dinst = (double*)scratch_get(c, "sp_dinst", INST_MAX * sizeof(double));
+    if (!dinst) return SFCI_ERR_NOMEM;
+    SFCI_CUDA(cudaMemsetAsync(dinst, 0, INST_MAX * sizeof(double), c.stream));
+  }
   const size_t lsm = (sizeof(KT) + WSLOT_BYTES_EXTRA) * TW_MAX * LW_WARPS;
   std::vector<u64> segs, nsegs_h;
   std::vector<Unit> units;
@@ -1581,6 +1606,7 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
       la.ovf_cap = OVF_CAP;
       la.uniq = scount + 1;
       la.bad = (unsigned*)(scount + 2);
+      la.dinst = dinst;
       SFCI_CUDA(cudaMemsetAsync(ovf, 0, sizeof(unsigned), c.stream));
       const unsigned lg = (unsigned)std::min<u64>((nleaves + LW_WARPS - 1) / LW_WARPS, leaf_resident);
       SFCI_LAUNCH(c, k_leafw<KT>, lg, LW_WARPS * 32, lsm, la);
@@ -1622,7 +1648,7 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
           gr = (unsigned)std::min<u64>((tsz + 255) / 256, (u64)c.sm_count * 8);
           SFCI_LAUNCH(c, k_big_finish<KT>, gr, 256, 0, (const KT*)bk, (const u64*)ba, (const u64*)(ba + tsz),
                       (unsigned)(tsz - 1), (const KT*)ink, (const double*)ina, (u64)ib_ie[0], (u64)ib_ie[1],
-                      la.cut, sk, sa, scount, dbig, scount + 1, qpart ? qpart + leafgrid + 1 : nullptr);
+                      la.cut, sk, sa, scount, dbig, scount + 1, qpart ? qpart + leafgrid + 1 : nullptr, la.dinst);
         }
       }
       if ((st = read_words(c, scount, sizeof(u64), &scount_h))) return st;
@@ -1666,6 +1692,10 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
     if (uq) c.dup_est = (double)T / (double)uq;
   }
   *diag = dl + dbig_h;
+  if (dinst) {
+    c.inst_diag.assign(INST_MAX, 0.0);
+    if ((st = read_words(c, dinst, INST_MAX * sizeof(double), c.inst_diag.data()))) return st;
+  }
   if (qpart) {
     SFCI_LAUNCH(c, k_sum_parts, 1, 32, 0, (const double*)qpart, (int)leafgrid, qpart + leafgrid);
     double q2[2] = {0.0, 0.0};

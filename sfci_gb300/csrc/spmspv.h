@@ -61,6 +61,13 @@ template <int W> int group_offsets_impl(Ctx& c, const typename KeyOf<W>::T* keys
 template <int W> int label_impl(Ctx& c, const typename KeyOf<W>::T* keys, const double* amps, u64 n,
                                 const u64* goff, const Vec& out, uint32_t* labels);
 
+// batched contexts: first position of each instance tag 0..n in a key-sorted
+// vector (n + 1 entries, host)
+int inst_bounds(Ctx& c, const Vec& v, int n, u64* out_host);
+// the truncated Lanczos driver on n instances of a batched context, one batched
+// product per Krylov step (solver.cpp)
+int lanczos_batched(Ctx& c, Vec* const* v, int n, int Nl, int restarts, double* energies, double* final_e);
+
 // width dispatch used by the ABI and the drivers
 int op_spmspv(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, double* diag);
 int op_energy(Ctx& c, const Vec& psi, double* E);

@@ -11,6 +11,7 @@
 #include <cmath>
 #include <vector>
 
+#include "gen.cuh"
 #include "prims.cuh"
 #include "spmspv.h"
 
@@ -340,5 +341,31 @@ template int combine_impl<1>(Ctx&, Vec&, const Vec* const*, const double*, int);
 template int combine_impl<2>(Ctx&, Vec&, const Vec* const*, const double*, int);
 template int sort_vec_impl<1>(Ctx&, Vec&);
 template int sort_vec_impl<2>(Ctx&, Vec&);
+
+}  // namespace sfci
+
+namespace sfci {
+
+// first position of each instance tag t = 0..n in a key-sorted two-word vector
+// (the tag is the top INST_BITS of the high word, so the vector is sorted by it)
+__global__ void k_inst_bounds(const K128* __restrict__ keys, u64 len, int n, u64* __restrict__ out) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t > n) return;
+  const u64 hi_t = (u64)t << INST_SHIFT;
+  u64 lo = 0, hi = len;  // first key with hi word >= hi_t
+  while (lo < hi) {
+    const u64 mid = (lo + hi) >> 1;
+    if (keys[mid].hi < hi_t) lo = mid + 1; else hi = mid;
+  }
+  out[t] = t == n ? len : lo;
+}
+
+int inst_bounds(Ctx& c, const Vec& v, int n, u64* out_host) {
+  if (c.W != 2) return set_error(SFCI_ERR_ARG, "instance bounds need two-word keys");
+  u64* d = (u64*)scratch_get(c, "ib_out", (n + 1) * sizeof(u64));
+  if (!d) return SFCI_ERR_NOMEM;
+  SFCI_LAUNCH(c, k_inst_bounds, 1, 64, 0, (const K128*)v.keys, (u64)v.len, n, d);
+  return read_words(c, d, (n + 1) * sizeof(u64), out_host);
+}
 
 }  // namespace sfci

@@ -95,6 +95,48 @@ def synthetic_rhf(M: int, seed: int):
     return h, (i, j, k, l), v, 0.0
 
 
+def bond_stretch_rhf(M: int, seed: int, t: float):
+    """A point of the synthetic bond-stretch curve: the seeded RHF integrals with
+    the off-diagonal one-body elements and the 'other' two-body values scaled by
+    (1 + 3t), and the gap of the diagonal one-body elements, h_pp + 3 =
+    0.25 p, scaled by (1 - 0.6t); Coulomb (pp|qq) and exchange (pq|pq) values
+    are those of t = 0.  t runs over [0, 1]."""
+    h, (i, j, k, l), v, e = synthetic_rhf(M, seed)
+    off = ~np.eye(M, dtype=bool)
+    h = h.copy()
+    h[off] *= 1.0 + 3.0 * t
+    h[np.diag_indices(M)] = -3.0 + 0.25 * np.arange(M) * (1.0 - 0.6 * t)
+    coulomb = (i == j) & (k == l)
+    exchange = (~coulomb) & (((i == k) & (j == l)) | ((i == l) & (j == k)))
+    v = np.where(coulomb | exchange, v, v * (1.0 + 3.0 * t))
+    return h, (i, j, k, l), v, e
+
+
+def bond_stretch_to_in_file(out_path: str, M: int, ne: int, seed: int, t: float,
+                            fcidump_path: str | None = None):
+    """The bond-stretch point (M, seed, t) -> FCIDUMP -> ``_IN``.  Returns the _IN path."""
+    h, q, v, e = bond_stretch_rhf(M, seed, t)
+    fd = fcidump_path or (out_path + ".fcidump")
+    write_fcidump_rhf(fd, h, q, v, e, ne)
+    write_in(out_path, convert_rhf(fd))
+    return out_path
+
+
+def bond_stretch_curve(n: int = 32, seed: int = 4, scale: float = 1.0):
+    """The n instances of the batched bond-stretch workload: t_i = i/(n-1);
+    num_orb unevenly in [40, 80] spin orbitals (a quadratic ramp, even), num_e
+    in {10, 12, 14, 16} by t, Nd geometric from 1e5 to 2e6 (times `scale`).
+    Returns a list of dicts (t, num_orb, num_e, Nd, seed)."""
+    out = []
+    for i in range(n):
+        t = i / max(n - 1, 1)
+        M = 20 + int(round(20 * t * t))
+        ne = 10 + 2 * min(3, int(4 * t))
+        nd = int(round(1e5 * (20.0 ** t) * scale))
+        out.append({"t": t, "num_orb": 2 * M, "num_e": ne, "Nd": max(nd, 16), "seed": seed})
+    return out
+
+
 def synthetic_uhf(M: int, seed_a: int, seed_b: int):
     """Seeded synthetic UHF integrals.
 

@@ -243,6 +243,12 @@ int sfci_batch_lanczos(sfci_ctx* ctx, sfci_vec* const* v, int n, int Nl, int res
  * (the merge is exact).  sfci_autotune times candidate plans on the product of
  * `in` (into `out`), checks that they agree, and keeps the fastest. */
 int sfci_ctx_set_tuning(sfci_ctx* ctx, const int* tuning4);
+/* Generation passes of a product whose terms exceed the device budget: by ranges
+ * of the targets' alpha class (mode 0: when three or more passes are needed; 1:
+ * whenever the product can be split so; -1: never), each pass generating only
+ * its own terms, or by hash bins, each pass regenerating every term.  Results
+ * never depend on the mode. */
+int sfci_ctx_set_class_passes(sfci_ctx* ctx, int mode);
 int sfci_ctx_get_tuning(const sfci_ctx* ctx, int* tuning4);
 int sfci_autotune(sfci_ctx* ctx, const sfci_vec* in, sfci_vec* out, int* best4, double* best_ms);
 

@@ -101,6 +101,7 @@ def _sigs(L):
     L.sfci_batch_create.argtypes = [C.c_int, C.POINTER(C.c_char_p), _vp, _vp, C.POINTER(Opts), C.POINTER(_vp)]
     L.sfci_batch_lanczos.argtypes = [_vp, C.POINTER(_vp), C.c_int, C.c_int, C.c_int, _vp, _vp]
     L.sfci_ctx_set_tuning.argtypes = [_vp, _vp]
+    L.sfci_ctx_set_class_passes.argtypes = [_vp, C.c_int]
     L.sfci_ctx_get_tuning.argtypes = [_vp, _vp]
     L.sfci_autotune.argtypes = [_vp, _vp, _vp, _vp, C.POINTER(C.c_double)]
     L.sfci_screen_create.argtypes = [_vp, C.c_uint64, C.POINTER(_vp)]
@@ -271,6 +272,10 @@ class Context:
     def set_tuning(self, l1_bits=9, digit_bits=9, leaf_keys=120, gen_ctas_per_sm=2):
         t = np.array([l1_bits, digit_bits, leaf_keys, gen_ctas_per_sm], np.int32)
         _check(self.L.sfci_ctx_set_tuning(self.h, _ptr(t)))
+
+    def set_class_passes(self, mode: int):
+        """Generation passes by target alpha class: 0 when needed, 1 always, -1 never."""
+        _check(self.L.sfci_ctx_set_class_passes(self.h, int(mode)))
 
     def autotune(self, vin: "SpVec", vout: "SpVec"):
         """Time the candidate product plans on vin and keep the fastest (results never depend on the plan)."""

@@ -351,6 +351,12 @@ int sfci_ctx_set_tuning(sfci_ctx* x, const int* t4) {
   return SFCI_OK;
 }
 
+int sfci_ctx_set_class_passes(sfci_ctx* x, int mode) {
+  if (!x || mode < -1 || mode > 1) return set_error(SFCI_ERR_ARG, "class-pass mode is -1, 0 or 1");
+  x->c.tune_class_passes = mode;
+  return SFCI_OK;
+}
+
 int sfci_ctx_get_tuning(const sfci_ctx* x, int* t4) {
   if (!x || !t4) return set_error(SFCI_ERR_ARG, "null argument");
   const Ctx& c = x->c;

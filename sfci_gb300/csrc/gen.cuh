@@ -71,7 +71,17 @@ struct DetHead {
   unsigned nvp[2];  // C(nv, 2)
   unsigned nsb;     // na[1] * nv[1]
   float inv_nvp[2], inv_nsb;
+  unsigned acls;    // alpha class of the determinant (see alpha_class_of_orb)
 };
+
+// Alpha class: an 8-bit XOR-linear hash of a determinant's spin-0 (alpha)
+// occupation, the XOR of a fixed pseudo-random byte per spin-0 orbital.  A
+// move i -> a changes it by the XOR of the two orbitals' bytes, so every term
+// that keeps the alpha string (the diagonal, spin-1 singles and spin-1 doubles)
+// has its source's class, and an opposite-spin double has the class of its
+// spin-0 move, whatever its spin-1 move.  Generation passes own ranges of
+// classes, so a pass skips whole blocks of terms without building their keys.
+SFCI_HD unsigned alpha_class_of_orb(int o) { return (unsigned)(mix64(0x5bd1e995ull + (u64)o) >> 56); }
 
 template <class KT>
 struct DetInfo {
@@ -83,6 +93,7 @@ struct DetInfo {
   // the two key bits it flips
   unsigned sd[2][1024];
   KT kx[2][1024];
+  unsigned char hx[1024];  // alpha-class change of each spin-0 single
 };
 
 // fill the single-excitation tables; thread k0 of `step` threads
@@ -99,6 +110,7 @@ SFCI_HD void det_fill_singles(DetInfo<KT>& d, unsigned k0, unsigned step) {
       key_flip(m, i);
       key_flip(m, a);
       d.kx[s][k] = m;
+      if (s == 0) d.hx[k] = (unsigned char)(alpha_class_of_orb(i) ^ alpha_class_of_orb(a));
     }
   }
 }
@@ -150,9 +162,11 @@ __device__ void det_setup_warp(DetInfo<KT>& d, const KT& key, double cc, double 
     d.h.dterm = (D - lambda) * cc;
   }
   unsigned cnt_o[2] = {0, 0}, cnt_v[2] = {0, 0};
+  unsigned acls = 0;
   for (int base = 0; base < M; base += 32) {
     int o = base + lane;
     bool in = o < M;
+    if (in && key_test(key, 2 * o)) acls ^= alpha_class_of_orb(2 * o);
 #pragma unroll
     for (int s = 0; s < 2; ++s) {
       int b = 2 * o + s;
@@ -166,7 +180,9 @@ __device__ void det_setup_warp(DetInfo<KT>& d, const KT& key, double cc, double 
       cnt_v[s] += __popc(bv);
     }
   }
+  acls = __reduce_xor_sync(0xffffffffu, acls);
   if (lane == 0) {
+    d.h.acls = acls;
     for (int s = 0; s < 2; ++s) {
       d.h.na[s] = cnt_o[s];
       d.h.nv[s] = cnt_v[s];
@@ -264,6 +280,22 @@ SFCI_HD KT target_key(const DetHead<KT>& h, const DetInfo<KT>& d, const Exc& e) 
     key_xor(k, d.kx[1][e.y]);
   }
   return k;
+}
+
+// Alpha class of the target of full term index l (see alpha_class_of_orb)
+template <class KT>
+SFCI_HD unsigned term_class(const DetHead<KT>& dh, const DetInfo<KT>& d, const unsigned short* pt, unsigned l) {
+  if (l < dh.c[1]) return l == 0 ? dh.acls : dh.acls ^ d.hx[l - dh.c[0]];  // diagonal, spin-0 singles
+  if (l < dh.c[2]) return dh.acls;                                          // spin-1 singles
+  if (l < dh.c[3]) {                                                        // spin-0 doubles
+    const unsigned r = l - dh.c[2], op = fdiv(r, dh.nvp[0], dh.inv_nvp[0]);
+    unsigned x, y, u, v;
+    pair_of(pt, op, x, y);
+    pair_of(pt, r - op * dh.nvp[0], u, v);
+    return dh.acls ^ d.hx[x * dh.nv[0] + u] ^ d.hx[y * dh.nv[0] + v];
+  }
+  if (l < dh.c[4]) return dh.acls;                                          // spin-1 doubles
+  return dh.acls ^ d.hx[fdiv(l - dh.c[4], dh.nsb, dh.inv_nsb)];             // opposite spin
 }
 
 // V[blk][pa][pb]

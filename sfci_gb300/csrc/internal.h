@@ -75,6 +75,7 @@ struct Ctx {
   int tune_digit_bits = 9;    // most bits per partition level
   int tune_leaf_uniq = 120;   // distinct keys a leaf is sized for
   int tune_gen_ctas = 2;      // generation CTAs per SM
+  int tune_class_passes = 0;  // generation passes by target alpha class: 0 when needed, 1 always, -1 never
   // learned excitation screen applied by the products (nullptr: plain products)
   struct Screen* screen = nullptr;
   // screens created on this context (freed with it; their handles become orphans)

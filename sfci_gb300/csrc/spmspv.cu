@@ -229,6 +229,13 @@ struct GenArgs {
   unsigned kl_cap = 0;      // shared-memory entries (the longest list)
   const u64* goff = nullptr;  // LABEL: first example of each source
   uint32_t* labels = nullptr; // LABEL: one bit per (source, group >= 1)
+  // class pass (COUNT / SCATTER): only targets whose alpha class is in
+  // [cls_lo, cls_hi).  A determinant's index space is then [0, c[3]) (diagonal,
+  // singles, spin-0 doubles: filtered term by term), its spin-1 doubles when its
+  // own class is in the pass, and the opposite-spin blocks (one spin-0 single
+  // each) whose class is in the pass
+  int cls_on = 0;
+  unsigned cls_lo = 0, cls_hi = 0;
 };
 
 template <class KT>
@@ -367,8 +374,9 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
     const HamView hv = ham_for(g.h, g.keys[det]);  // this determinant's Hamiltonian
     if (tid < 32) det_setup_warp(d, g.keys[det], g.coeff * g.amps[det], g.diagE[det], g.lambda, hv.M);
     if (tid == 0 && det >= g.nmain) d.h.dterm = g.amps[det];  // a single term, as given
-    const bool screened = (MODE == M_COUNT || MODE == M_SCATTER) && g.kl_start && det < g.nmain;
-    if (screened) {
+    const bool cls_pass = (MODE == M_COUNT || MODE == M_SCATTER) && g.cls_on && det < g.nmain;
+    const bool screened = (MODE == M_COUNT || MODE == M_SCATTER) && (g.kl_start || g.cls_on) && det < g.nmain;
+    if (screened && !cls_pass) {
       const u64 k0 = g.kl_off[det], nk = g.kl_off[det + 1] - k0;
       for (unsigned i = tid; i < nk; i += GEN_THREADS) {
         kst[i] = g.kl_start[k0 + i];
@@ -379,18 +387,56 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
     __syncthreads();
     if (det < g.nmain) det_fill_singles(d, tid, GEN_THREADS);  // (term 0 needs no tables)
     __syncthreads();
+    if (cls_pass) {
+      // the pass's blocks of this determinant, in term order: [0, c[3]) always,
+      // the spin-1 doubles when the determinant's class is in the pass, then the
+      // opposite-spin blocks of the spin-0 singles whose class is
+      const unsigned lo = g.cls_lo, hi = g.cls_hi;
+      const bool own = d.h.acls >= lo && d.h.acls < hi;
+      const unsigned nx = d.h.na[0] * d.h.nv[0], nsb = d.h.nsb;
+      if (tid == 0) {
+        kst[0] = 0;
+        kpr[0] = 0;
+        if (own) {
+          kst[1] = d.h.c[3];
+          kpr[1] = d.h.c[3];
+        }
+      }
+      const unsigned e0 = own ? 2u : 1u, p0 = own ? d.h.c[4] : d.h.c[3];
+      unsigned run = 0;
+      for (unsigned xb = 0; xb < nx; xb += GEN_THREADS) {
+        const unsigned x = xb + tid;
+        const unsigned cx = x < nx ? (d.h.acls ^ d.hx[x]) : 0u;
+        const bool keep = x < nx && cx >= lo && cx < hi && nsb > 0;
+        uint32_t tot;
+        const uint32_t ex = block_excl_scan<uint32_t, GEN_THREADS>(keep ? 1u : 0u, &tot, s_scan);
+        if (keep) {
+          kst[e0 + run + ex] = d.h.c[4] + x * nsb;
+          kpr[e0 + run + ex] = p0 + (run + ex) * nsb;
+        }
+        run += tot;
+      }
+      if (tid == 0) s_nk = e0 + run;
+      __syncthreads();
+    }
     const DetHead<KT> dh = d.h;
     const unsigned nk = screened ? s_nk : 0u;
     // screened term index -> full term index: group 0 maps to itself, then a
     // binary search over the kept groups' screened starts
     auto remap = [&](unsigned l) -> unsigned {
-      if (!screened || l < dh.c[2]) return l;
+      if (!screened || l < (cls_pass ? dh.c[3] : dh.c[2])) return l;
       unsigned lo = 0, hi = nk;
       while (hi - lo > 1) {
         const unsigned mid = (lo + hi) >> 1;
         if (kpr[mid] <= l) lo = mid; else hi = mid;
       }
       return kst[lo] + (l - kpr[lo]);
+    };
+    // class pass: is the target of (full) term index lf in the pass?
+    auto in_pass = [&](unsigned lf) -> bool {
+      if (!cls_pass || lf >= dh.c[3]) return true;  // blocks past c[3] were chosen whole
+      const unsigned cl = term_class(dh, d, pt, lf);
+      return cl >= g.cls_lo && cl < g.cls_hi;
     };
     const unsigned l0 = (unsigned)(t0 - dbeg);
     const unsigned l1 = (unsigned)((t1 < dend ? t1 : dend) - dbeg);
@@ -405,8 +451,9 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
         for (int it = 0; it < GEN_IPT; ++it) {
           unsigned l = rb + it * GEN_THREADS + tid;
           br[it] = ~0u;
-          if (l < l1) {
-            const unsigned bin = (unsigned)(key_hash(target_key(dh, d, decode(dh, pt, remap(l)))) >> shift1);
+          const unsigned lf = l < l1 ? remap(l) : 0u;
+          if (l < l1 && in_pass(lf)) {
+            const unsigned bin = (unsigned)(key_hash(target_key(dh, d, decode(dh, pt, lf))) >> shift1);
             if (bin >= g.bin_lo && bin < g.bin_hi) {
               unsigned lb = bin - g.bin_lo;
               unsigned r = atomicAdd(&hist[lb], 1u);
@@ -487,7 +534,9 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
           unsigned l = rb + it * GEN_THREADS + tid;
           if (l < l1) {
             if (MODE == M_COUNT) {
-              atomicAdd(&hist[(unsigned)(key_hash(target_key(dh, d, decode(dh, pt, remap(l)))) >> shift1)], 1u);
+              const unsigned lf = remap(l);
+              if (in_pass(lf))
+                atomicAdd(&hist[(unsigned)(key_hash(target_key(dh, d, decode(dh, pt, lf))) >> shift1)], 1u);
             } else if (MODE == M_LABEL) {
               // a group is alive when one of its terms lands on the product's output
               if (table_find_global(g.tkeys, g.tmask, target_key(dh, d, decode(dh, pt, l))) >= 0) {
@@ -1160,6 +1209,117 @@ __global__ void k_fill_u64(u64* p, u64 n, u64 v) {
   for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (u64)gridDim.x * blockDim.x) p[i] = v;
 }
 
+// ---------------------------------------------------------------------------
+// class passes: term counts per alpha class, and per determinant within a pass
+// ---------------------------------------------------------------------------
+// One warp per determinant: its spin-0 occupied / empty orbitals' class bytes
+// in shared memory; returns the determinant's class and its spin counts.
+template <class KT>
+__device__ __forceinline__ unsigned class_lists(const KT& k, int N, int M, unsigned char* oc, unsigned char* vc,
+                                                unsigned* na, unsigned* nv) {
+  const int lane = threadIdx.x & 31;
+  unsigned cls = 0, no = 0, nvv = 0, nb1 = 0;
+  for (int base = 0; base < M; base += 32) {
+    const int o = base + lane;
+    const bool in = o < M;
+    const bool occ = in && key_test(k, 2 * o), vir = in && !occ;
+    const unsigned bo = __ballot_sync(0xffffffffu, occ), bv = __ballot_sync(0xffffffffu, vir);
+    const unsigned lt = (1u << lane) - 1u;
+    const unsigned b = in ? alpha_class_of_orb(2 * o) : 0u;
+    if (occ) {
+      oc[no + __popc(bo & lt)] = (unsigned char)b;
+      cls ^= b;
+    }
+    if (vir) vc[nvv + __popc(bv & lt)] = (unsigned char)b;
+    no += __popc(bo);
+    nvv += __popc(bv);
+    nb1 += __popc(__ballot_sync(0xffffffffu, in && key_test(k, 2 * o + 1)));
+  }
+  __syncwarp();
+  na[0] = no;
+  nv[0] = nvv;
+  na[1] = nb1;
+  nv[1] = M - nb1;
+  return __reduce_xor_sync(0xffffffffu, cls);
+}
+
+constexpr int CLS_N = 256;
+
+// terms of every target class over all determinants (the plan of the class passes)
+template <class KT>
+__global__ void __launch_bounds__(256) k_class_hist(const KT* __restrict__ keys, u64 n, int N, int M,
+                                                    u64* __restrict__ hist) {
+  __shared__ unsigned long long sh[CLS_N];
+  __shared__ unsigned char s_oc[8][64], s_vc[8][64];
+  __shared__ unsigned s_hv[8][CLS_N];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int i = threadIdx.x; i < CLS_N; i += blockDim.x) sh[i] = 0;
+  __syncthreads();
+  unsigned char* oc = s_oc[warp];
+  unsigned char* vc = s_vc[warp];
+  unsigned* hv = s_hv[warp];
+  for (u64 j = ((u64)blockIdx.x * blockDim.x + threadIdx.x) >> 5; j < n; j += ((u64)gridDim.x * blockDim.x) >> 5) {
+    unsigned na[2], nv[2];
+    const unsigned ac = class_lists(keys[j], N, M, oc, vc, na, nv);
+    const u64 nsb = (u64)na[1] * nv[1];
+    if (lane == 0) atomicAdd(&sh[ac], 1ull + nsb + (u64)c2(na[1]) * c2(nv[1]));  // keeps the alpha string
+    // spin-0 singles (one term each) and opposite-spin blocks (nsb terms each)
+    for (unsigned x = lane; x < na[0] * nv[0]; x += 32) {
+      const unsigned ii = x / nv[0], aa = x - ii * nv[0];
+      atomicAdd(&sh[ac ^ oc[ii] ^ vc[aa]], 1ull + nsb);
+    }
+    // spin-0 doubles: the class histogram of the empty pairs, shifted per occupied pair
+    for (int i = lane; i < CLS_N; i += 32) hv[i] = 0;
+    __syncwarp();
+    const unsigned nvp = c2(nv[0]);
+    for (unsigned q = lane; q < nvp; q += 32) {
+      unsigned u, v;
+      unrank_pair(q, u, v);
+      atomicAdd(&hv[vc[u] ^ vc[v]], 1u);
+    }
+    __syncwarp();
+    for (unsigned op = 0; op < c2(na[0]); ++op) {
+      unsigned x, y;
+      unrank_pair(op, x, y);
+      const unsigned sh_c = ac ^ oc[x] ^ oc[y];
+      for (int c = lane; c < CLS_N; c += 32)
+        if (hv[c]) atomicAdd(&sh[sh_c ^ c], (unsigned long long)hv[c]);
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < CLS_N; i += blockDim.x)
+    if (sh[i]) atomicAdd(hist + i, sh[i]);
+}
+
+// index-space size of every determinant in the class pass [lo, hi): [0, c[3]),
+// the spin-1 doubles when its class is in the pass, and nsb per spin-0 single
+// whose class is (the generator's class-pass index space)
+template <class KT>
+__global__ void __launch_bounds__(256) k_pass_counts(const KT* __restrict__ keys, u64 n, int N, int M, unsigned lo,
+                                                     unsigned hi, u64* __restrict__ cnt) {
+  __shared__ unsigned char s_oc[8][64], s_vc[8][64];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (u64 j = ((u64)blockIdx.x * blockDim.x + threadIdx.x) >> 5; j < n; j += ((u64)gridDim.x * blockDim.x) >> 5) {
+    unsigned na[2], nv[2];
+    const unsigned ac = class_lists(keys[j], N, M, s_oc[warp], s_vc[warp], na, nv);
+    const u64 nsb = (u64)na[1] * nv[1];
+    unsigned kept = 0;
+    for (unsigned x = lane; x < na[0] * nv[0]; x += 32) {
+      const unsigned ii = x / nv[0], aa = x - ii * nv[0];
+      const unsigned cx = ac ^ s_oc[warp][ii] ^ s_vc[warp][aa];
+      kept += (cx >= lo && cx < hi) ? 1u : 0u;
+    }
+    kept = warp_sum(kept);
+    if (lane == 0) {
+      const u64 c3 = 1ull + (u64)na[0] * nv[0] + nsb + (u64)c2(na[0]) * c2(nv[0]);
+      const bool own = ac >= lo && ac < hi;
+      cnt[j] = c3 + (own ? (u64)c2(na[1]) * c2(nv[1]) : 0ull) + (u64)kept * nsb;
+    }
+    __syncwarp();
+  }
+}
+
 // screened term count of a source: group 0 (diagonal and singles) plus its kept groups' terms
 template <class KT>
 __global__ void k_screen_counts(const KT* __restrict__ keys, u64 n, int N, int M, const u64* __restrict__ kept,
@@ -1310,90 +1470,76 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
   double* diagE = nullptr;
   if ((st = prep_dets<W>(c, gen_k, ng, &doff, &diagE, &T, ns, kept))) return st;
   c.stats[1] = T;
-  // hash digits: level 1 (generation) d0 bits, then nlev partition levels.
-  // 2^b leaves: the fewest (so the fewest partition levels, each a full read
-  // and write of the terms, and the best amortised per-leaf table set-up) whose
-  // expected distinct keys stay within TW_UNIQ, so that a warp table takes a
-  // leaf.  The distinct count is estimated from the duplication (terms per
-  // distinct key) of the previous product on this context (default 8).
+  // ---- generation plan.  One outer pass over every term; or, when the terms
+  // need several generation passes, class passes: each outer pass owns a range
+  // of alpha classes of the targets (alpha_class_of_orb), generates only its
+  // own terms (whole blocks skipped by class, the rest filtered term by term)
+  // and merges them completely, so the work is proportional to the terms and
+  // not to terms x passes.  Ordinary multi-pass plans regenerate and bin every
+  // term in every pass.
+  tok = phase_begin(c, PH_OTHER);
+  const size_t tb = sizeof(KT) + sizeof(double);
+  const u64 cap = out.cap;
+  size_t budget = 0;
+  {
+    size_t freeb = 0, totb = 0;
+    SFCI_CUDA(cudaMemGetInfo(&freeb, &totb));
+    size_t held = 0;
+    for (const char* nm : {"sp_l1k", "sp_l1a", "sp_l2k", "sp_l2a", "sp_sk", "sp_sa", "topk_k", "topk_a"}) {
+      auto it = c.scratch.find(nm);
+      if (it != c.scratch.end()) held += it->second.bytes;
+    }
+    budget = c.opts.mem_budget ? (size_t)c.opts.mem_budget : (size_t)((freeb + held) * 0.90);
+  }
+  const u64 avail = budget / tb;
   const double dup = c.dup_est > 0.0 ? c.dup_est : 8.0;
-  const double uniq_est = std::max(1.0, (double)T / std::max(1.0, dup));
   const int leaf_uniq = std::max(16, std::min(TW_UNIQ, c.tune_leaf_uniq));
   const int l1_bits = std::max(4, std::min(L1_BITS, c.tune_l1_bits));
   const int digit_bits = std::max(6, std::min(DIGIT_MAX, c.tune_digit_bits));
-  const int b = std::max(1, std::min(B_MAX, (int)std::ceil(std::log2(std::max(2.0, uniq_est / leaf_uniq)))));
-  const int d0 = std::min(b, l1_bits);
-  const int rem = b - d0;
-  const int nlev = rem ? (rem + digit_bits - 1) / digit_bits : 0;
-  std::vector<int> dig(nlev);
-  for (int k = 0; k < nlev; ++k) dig[k] = rem / nlev + (k < rem % nlev ? 1 : 0);
-  const unsigned NB1 = 1u << d0;
-  const unsigned G = gen_grid(c, T);
+  struct OuterPass {
+    unsigned lo, hi;  // class range (class passes)
+    u64 terms;        // terms this outer pass generates
+  };
+  std::vector<OuterPass> outer;
+  bool cls_mode = false;
+  MemPlan cmp;  // fixed buffers of the class passes
+  if (!kept && ng == ns && c.tune_class_passes >= 0 && ns > 0) {
+    cmp.C2 = std::max<u64>(avail / 16, 1ull << 20);
+    cmp.SC = std::min<u64>(cap, T) + cmp.C2;
+    if (avail > cmp.C2 + 2 * cmp.SC) cmp.C1 = avail - cmp.C2 - 2 * cmp.SC;
+    const bool many = c.tune_class_passes > 0 ? true : T > 3 * cmp.C1;  // several passes: worth the split
+    if (cmp.C1 > 0 && many) {
+      u64* hist = (u64*)scratch_get(c, "sp_clshist", CLS_N * sizeof(u64));
+      if (!hist) return SFCI_ERR_NOMEM;
+      SFCI_CUDA(cudaMemsetAsync(hist, 0, CLS_N * sizeof(u64), c.stream));
+      const unsigned gr = (unsigned)std::min<u64>((ns * 32 + 255) / 256, (u64)c.sm_count * 16);
+      SFCI_LAUNCH(c, k_class_hist<KT>, gr, 256, 0, src_k, ns, c.N, c.M, hist);
+      std::vector<u64> hh(CLS_N);
+      if ((st = read_words(c, hist, CLS_N * sizeof(u64), hh.data()))) return st;
+      u64 tot = 0, big = 0;
+      for (u64 v : hh) {
+        tot += v;
+        big = std::max(big, v);
+      }
+      if (tot != T) return set_error(SFCI_ERR_NUMERIC, "SpMSpV class histogram disagrees with term offsets");
+      (void)big;
+      // consecutive classes while they fit one pass; a class larger than a pass
+      // is an outer pass of its own, split further into bin passes that
+      // regenerate that class's terms only
+      cls_mode = true;
+      unsigned lo = 0;
+      while (lo < (unsigned)CLS_N) {
+        unsigned hi = lo + 1;
+        u64 sum = hh[lo];
+        while (hi < (unsigned)CLS_N && sum + hh[hi] <= cmp.C1) sum += hh[hi++];
+        if (sum) outer.push_back({lo, hi, sum});
+        lo = hi;
+      }
+      cmp.passes = (int)outer.size();
+    }
+  }
+  if (!cls_mode) outer.push_back({0u, 0u, T});
   phase_end(c, tok);
-
-  // 3. COUNT sweep -> [bin x CTA] matrix
-  tok = phase_begin(c, PH_COUNT);
-  u64* cntm = (u64*)scratch_get(c, "sp_cntm", ((u64)NB1 * G + 1) * sizeof(u64));
-  if (!cntm) return SFCI_ERR_NOMEM;
-  GenArgs<KT> g{};
-  g.keys = gen_k;
-  g.amps = gen_a;
-  g.ndet = ng;
-  g.nmain = ns;
-  g.doff = doff;
-  g.diagE = diagE;
-  g.coeff = coeff;
-  g.lambda = lambda;
-  g.h = ham_view(c);
-  g.T = T;
-  g.b1 = d0;
-  g.cntm = cntm;
-  if (kept) {
-    g.kl_start = sl.start;
-    g.kl_pre = sl.pre;
-    g.kl_off = sl.off;
-    g.kl_cap = std::max(sl.gmax, 1u);
-  }
-  if ((st = launch_gen<W, M_COUNT>(c, g, G, NB1))) return st;
-  if ((st = scan_excl(c, cntm, cntm, (u64)NB1 * G))) return st;
-  std::vector<u64> binoff(NB1 + 1);
-  {
-    u64* bo = (u64*)scratch_get(c, "sp_binoff", (NB1 + 1) * sizeof(u64));
-    if (!bo) return SFCI_ERR_NOMEM;
-    SFCI_CUDA(cudaMemcpy2DAsync(bo, sizeof(u64), cntm, G * sizeof(u64), sizeof(u64), NB1, cudaMemcpyDeviceToDevice,
-                                c.stream));
-    SFCI_CUDA(cudaMemcpyAsync(bo + NB1, cntm + (u64)NB1 * G, sizeof(u64), cudaMemcpyDeviceToDevice, c.stream));
-    if ((st = read_words(c, bo, (NB1 + 1) * sizeof(u64), binoff.data()))) return st;
-  }
-  phase_end(c, tok);
-  if (binoff[NB1] != T) return set_error(SFCI_ERR_NUMERIC, "SpMSpV count sweep disagrees with term offsets");
-
-  // 4. memory plan
-  tok = phase_begin(c, PH_OTHER);
-  const size_t tb = sizeof(KT) + sizeof(double);
-  u64 maxbin = 0;
-  for (unsigned i = 0; i < NB1; ++i) maxbin = std::max(maxbin, binoff[i + 1] - binoff[i]);
-  size_t freeb = 0, totb = 0;
-  SFCI_CUDA(cudaMemGetInfo(&freeb, &totb));
-  size_t held = 0;
-  for (const char* nm : {"sp_l1k", "sp_l1a", "sp_l2k", "sp_l2a", "sp_sk", "sp_sa", "topk_k", "topk_a"}) {
-    auto it = c.scratch.find(nm);
-    if (it != c.scratch.end()) held += it->second.bytes;
-  }
-  size_t budget = c.opts.mem_budget ? (size_t)c.opts.mem_budget : (size_t)((freeb + held) * 0.90);
-  u64 avail = budget / tb;
-  const u64 cap = out.cap;
-  MemPlan mp;
-  if (!plan_memory(binoff, NB1, T, avail, std::min<u64>(cap, T), maxbin, nlev > 0, mp))
-    return set_error(SFCI_ERR_NOMEM, "SpMSpV device-memory budget too small");
-  const u64 C2 = mp.C2, C1 = mp.C1, SC = mp.SC;
-  KT* l1k = (KT*)scratch_get(c, "sp_l1k", C1 * sizeof(KT));
-  double* l1a = (double*)scratch_get(c, "sp_l1a", C1 * sizeof(double));
-  KT* l2k = nlev ? (KT*)scratch_get(c, "sp_l2k", C2 * sizeof(KT)) : nullptr;
-  double* l2a = nlev ? (double*)scratch_get(c, "sp_l2a", C2 * sizeof(double)) : nullptr;
-  KT* sk = (KT*)scratch_get(c, "sp_sk", SC * sizeof(KT));
-  double* sa = (double*)scratch_get(c, "sp_sa", SC * sizeof(double));
-  if (!l1k || !l1a || !sk || !sa || (nlev && (!l2k || !l2a))) return SFCI_ERR_NOMEM;
   // [0] survivors, [1] distinct, [2] fixed-point range flag
   u64* scount = (u64*)scratch_get(c, "sp_scount", 4 * sizeof(u64));
   const unsigned leafgrid = (unsigned)c.sm_count * 8;
@@ -1422,37 +1568,9 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
     SFCI_CUDA(cudaMemsetAsync(qpart, 0, (leafgrid + 2) * sizeof(double), c.stream));
   }
 
-  // input dets grouped by global leaf (top b bits of the hash)
-  const u64 NL = 1ull << b;
-  uint32_t* inoff = (uint32_t*)scratch_get(c, "sp_inoff", (NL + 1) * sizeof(uint32_t));
-  uint32_t* incur = (uint32_t*)scratch_get(c, "sp_incur", (NL + 1) * sizeof(uint32_t));
-  KT* ink = (KT*)scratch_get(c, "sp_ink", ns * sizeof(KT));
-  double* ina = (double*)scratch_get(c, "sp_ina", ns * sizeof(double));
-  if (!inoff || !incur || !ink || !ina) return SFCI_ERR_NOMEM;
-  SFCI_CUDA(cudaMemsetAsync(inoff, 0, (NL + 1) * sizeof(uint32_t), c.stream));
-  {
-    unsigned gr = (unsigned)std::min<u64>((ns + 255) / 256, (u64)c.sm_count * 8);
-    SFCI_LAUNCH(c, k_in_count<KT>, gr, 256, 0, src_k, ns, b, inoff);
-    if ((st = scan_excl_u32(c, inoff, inoff, NL))) return st;
-    SFCI_CUDA(cudaMemcpyAsync(incur, inoff, NL * sizeof(uint32_t), cudaMemcpyDeviceToDevice, c.stream));
-    SFCI_LAUNCH(c, k_in_scatter<KT>, gr, 256, 0, src_k, src_a, ns, b, incur, ink, ina);
-  }
-  phase_end(c, tok);
-
-  // pass plan over level-1 bins
-  std::vector<std::pair<unsigned, unsigned>> passes;
-  {
-    unsigned lo = 0;
-    while (lo < NB1) {
-      unsigned hi = lo + 1;
-      while (hi < NB1 && binoff[hi + 1] - binoff[lo] <= C1) ++hi;
-      passes.push_back({lo, hi});
-      lo = hi;
-    }
-  }
-  c.stats[5] = passes.size();
-  c.stats[6] = NL;
-  u64 scount_h = 0, big_leaves = 0;
+  u64 scount_h = 0, big_leaves = 0, T_gen = 0;
+  KT* sk = nullptr;    // survivors of every outer pass (kept across them: the buffers do not
+  double* sa = nullptr;  // change size between class passes)
   double dbig_h = 0.0;
   double* dbig = (double*)scratch_get(c, "sp_dbig", sizeof(double));
   if (!dbig) return SFCI_ERR_NOMEM;
@@ -1468,195 +1586,319 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
   std::vector<Unit> units;
   std::vector<u64> segbase;
   std::vector<unsigned> segnu;
-  for (auto& ps : passes) {
-    const unsigned lo = ps.first, hi = ps.second;
-    // 5. SCATTER sweep for this pass (level-1 buffer holds bins [lo, hi))
-    tok = phase_begin(c, PH_SCATTER);
-    g.bin_lo = lo;
-    g.bin_hi = hi;
-    g.basem = cntm;
-    g.pass_base = binoff[lo];
-    g.okeys = l1k;
-    g.oamps = l1a;
-    if ((st = launch_gen<W, M_SCATTER>(c, g, G, hi - lo))) return st;
-    phase_end(c, tok);
-    unsigned glo = lo;
-    while (glo < hi) {
-      unsigned ghi = glo + 1;
-      while (ghi < hi && binoff[ghi + 1] - binoff[glo] <= C2) ++ghi;
-      const u64 gterms = binoff[ghi] - binoff[glo];
-      if (scount_h + gterms > SC && scount_h > cap) {
-        int t2 = phase_begin(c, PH_SELECT);
-        size_t m = 0;
-        if ((st = top_k_stable<W>(c, sk, sa, scount_h, cap, -1.0, sk, sa, &m))) return st;
-        scount_h = m;
-        SFCI_CUDA(cudaMemcpyAsync(scount, &scount_h, sizeof(u64), cudaMemcpyHostToDevice, c.stream));
-        phase_end(c, t2);
-      }
-      const unsigned nbg = ghi - glo;
-      // segments of this group: its level-1 bins, positions in the level-1 buffer
-      segs.assign(nbg + 1, 0);
-      for (unsigned i = 0; i <= nbg; ++i) segs[i] = binoff[glo + i] - binoff[lo];
-      const u64 gbase = segs[0];
-      KT* srck = l1k;
-      double* srca = l1a;
-      KT* dstk = l2k;
-      double* dsta = l2a;
-      bool dst_is_l1 = false;
-      u64* loff_dev = nullptr;
-      // 6a. partition levels
-      tok = phase_begin(c, PH_PARTITION);
-      int consumed = d0;
-      for (int k = 0; k < nlev; ++k) {
-        const unsigned nd = 1u << dig[k];
-        const u64 nseg = segs.size() - 1;
-        units.clear();
-        segbase.assign(nseg, 0);
-        segnu.assign(nseg, 0);
-        u64 cbase = 0;
-        for (u64 s = 0; s < nseg; ++s) {
-          const u64 a0 = segs[s], a1 = segs[s + 1], n = a1 - a0;
-          const unsigned nu = (unsigned)std::max<u64>(1, (n + UNIT_ITEMS - 1) / UNIT_ITEMS);
-          segbase[s] = cbase;
-          segnu[s] = nu;
-          for (unsigned j = 0; j < nu; ++j) {
-            Unit un;
-            un.start = a0 + (u64)j * UNIT_ITEMS;
-            un.end = std::min<u64>(a1, un.start + UNIT_ITEMS);
-            if (un.start > un.end) un.start = un.end;
-            un.cbase = cbase + j;
-            un.stride = nu;
-            un.pad = 0;
-            units.push_back(un);
-          }
-          cbase += (u64)nu * nd;
-        }
-        const u64 mlen = cbase;
-        Unit* du = (Unit*)scratch_get(c, "sp_units", units.size() * sizeof(Unit));
-        u64* cm = (u64*)scratch_get(c, "sp_cm", (mlen + 1) * sizeof(u64));
-        u64* dsb = (u64*)scratch_get(c, "sp_segbase", nseg * sizeof(u64));
-        unsigned* dsn = (unsigned*)scratch_get(c, "sp_segnu", nseg * sizeof(unsigned));
-        u64* nextoff = (u64*)scratch_get(c, k == nlev - 1 ? "sp_loff" : "sp_segoff", (nseg * nd + 1) * sizeof(u64));
-        if (!du || !cm || !dsb || !dsn || !nextoff) return SFCI_ERR_NOMEM;
-        SFCI_CUDA(cudaMemcpyAsync(du, units.data(), units.size() * sizeof(Unit), cudaMemcpyHostToDevice, c.stream));
-        SFCI_CUDA(cudaMemcpyAsync(dsb, segbase.data(), nseg * sizeof(u64), cudaMemcpyHostToDevice, c.stream));
-        SFCI_CUDA(cudaMemcpyAsync(dsn, segnu.data(), nseg * sizeof(unsigned), cudaMemcpyHostToDevice, c.stream));
-        PartArgs<KT> pa{};
-        pa.ikeys = srck;
-        pa.iamps = srca;
-        pa.units = du;
-        pa.nunits = (unsigned)units.size();
-        pa.shift = 64 - consumed - dig[k];
-        pa.nd = nd;
-        pa.cm = cm;
-        pa.dst_base = dst_is_l1 ? gbase : 0;
-        pa.okeys = dstk;
-        pa.oamps = dsta;
-        const unsigned pgrid = (unsigned)std::min<u64>(units.size(), (u64)c.sm_count * 4);
-        const size_t smc = part_smem_bytes<KT, IPT>(M_COUNT, nd);
-        const size_t sms = part_smem_bytes<KT, IPT>(M_SCATTER, nd);
-        SFCI_LAUNCH(c, (k_part<KT, M_COUNT, IPT>), pgrid, PT_THREADS, smc, pa);
-        if ((st = scan_excl(c, cm, cm, mlen))) return st;
-        SFCI_LAUNCH(c, (k_part<KT, M_SCATTER, IPT>), pgrid, PT_THREADS, sms, pa);
-        {
-          const u64 nn = nseg * nd + 1;
-          unsigned gr = (unsigned)std::min<u64>((nn + 255) / 256, (u64)c.sm_count * 8);
-          SFCI_LAUNCH(c, k_seg_gather, gr, 256, 0, (const u64*)cm, (const u64*)dsb, (const unsigned*)dsn, nseg, nd,
-                      mlen, pa.dst_base, nextoff);
-        }
-        consumed += dig[k];
-        if (k == nlev - 1) {
-          loff_dev = nextoff;
-          segs.resize(nseg * nd + 1);  // sizes only needed for the leaf count below
-        } else {
-          nsegs_h.resize(nseg * nd + 1);
-          if ((st = read_words(c, nextoff, (nseg * nd + 1) * sizeof(u64), nsegs_h.data()))) return st;
-          segs.swap(nsegs_h);
-        }
-        std::swap(srck, dstk);
-        std::swap(srca, dsta);
-        dst_is_l1 = !dst_is_l1;
-      }
+  for (const OuterPass& opass : outer) {
+    // the outer pass's index space: every term, or the class pass's blocks
+    u64* doffp = doff;
+    u64 Tp = T;
+    if (cls_mode) {
+      tok = phase_begin(c, PH_OTHER);
+      doffp = (u64*)scratch_get(c, "sp_pdoff", (ns + 1) * sizeof(u64));
+      if (!doffp) return SFCI_ERR_NOMEM;
+      const unsigned gr = (unsigned)std::min<u64>((ns * 32 + 255) / 256, (u64)c.sm_count * 16);
+      SFCI_LAUNCH(c, k_pass_counts<KT>, gr, 256, 0, src_k, ns, c.N, c.M, opass.lo, opass.hi, doffp);
+      if ((st = scan_excl(c, doffp, doffp, ns))) return st;
+      if ((st = read_words(c, doffp + ns, sizeof(u64), &Tp))) return st;
       phase_end(c, tok);
-      const u64 nleaves = segs.size() - 1;
-      if (nlev == 0) {
-        loff_dev = (u64*)scratch_get(c, "sp_loff", (nleaves + 1) * sizeof(u64));
-        if (!loff_dev) return SFCI_ERR_NOMEM;
-        SFCI_CUDA(cudaMemcpyAsync(loff_dev, segs.data(), (nleaves + 1) * sizeof(u64), cudaMemcpyHostToDevice,
+    }
+    // hash digits: level 1 (generation) d0 bits, then nlev partition levels.
+    // 2^b leaves: the fewest (so the fewest partition levels, each a full read
+    // and write of the terms, and the best amortised per-leaf table set-up) whose
+    // expected distinct keys stay within TW_UNIQ, so that a warp table takes a
+    // leaf.  The distinct count is estimated from the duplication (terms per
+    // distinct key) of the previous product on this context (default 8).
+    const double uniq_est = std::max(1.0, (double)opass.terms / std::max(1.0, dup));
+    const int b = std::max(1, std::min(B_MAX, (int)std::ceil(std::log2(std::max(2.0, uniq_est / leaf_uniq)))));
+    const int d0 = std::min(b, l1_bits);
+    const int rem = b - d0;
+    const int nlev = rem ? (rem + digit_bits - 1) / digit_bits : 0;
+    std::vector<int> dig(nlev);
+    for (int k = 0; k < nlev; ++k) dig[k] = rem / nlev + (k < rem % nlev ? 1 : 0);
+    const unsigned NB1 = 1u << d0;
+    const unsigned G = gen_grid(c, Tp);
+
+    // 3. COUNT sweep -> [bin x CTA] matrix
+    tok = phase_begin(c, PH_COUNT);
+    u64* cntm = (u64*)scratch_get(c, "sp_cntm", ((u64)NB1 * G + 1) * sizeof(u64));
+    if (!cntm) return SFCI_ERR_NOMEM;
+    GenArgs<KT> g{};
+    g.keys = gen_k;
+    g.amps = gen_a;
+    g.ndet = ng;
+    g.nmain = ns;
+    g.doff = doffp;
+    g.diagE = diagE;
+    g.coeff = coeff;
+    g.lambda = lambda;
+    g.h = ham_view(c);
+    g.T = Tp;
+    g.b1 = d0;
+    g.cntm = cntm;
+    if (kept) {
+      g.kl_start = sl.start;
+      g.kl_pre = sl.pre;
+      g.kl_off = sl.off;
+      g.kl_cap = std::max(sl.gmax, 1u);
+    }
+    if (cls_mode) {
+      g.cls_on = 1;
+      g.cls_lo = opass.lo;
+      g.cls_hi = opass.hi;
+      g.kl_cap = 3 + (unsigned)(c.M * c.M / 4);  // [0, c3), spin-1 doubles, na0 * nv0 <= M^2 / 4 blocks
+    }
+    if ((st = launch_gen<W, M_COUNT>(c, g, G, NB1))) return st;
+    if ((st = scan_excl(c, cntm, cntm, (u64)NB1 * G))) return st;
+    std::vector<u64> binoff(NB1 + 1);
+    {
+      u64* bo = (u64*)scratch_get(c, "sp_binoff", (NB1 + 1) * sizeof(u64));
+      if (!bo) return SFCI_ERR_NOMEM;
+      SFCI_CUDA(cudaMemcpy2DAsync(bo, sizeof(u64), cntm, G * sizeof(u64), sizeof(u64), NB1, cudaMemcpyDeviceToDevice,
                                   c.stream));
+      SFCI_CUDA(cudaMemcpyAsync(bo + NB1, cntm + (u64)NB1 * G, sizeof(u64), cudaMemcpyDeviceToDevice, c.stream));
+      if ((st = read_words(c, bo, (NB1 + 1) * sizeof(u64), binoff.data()))) return st;
+    }
+    phase_end(c, tok);
+    if (binoff[NB1] != opass.terms)
+      return set_error(SFCI_ERR_NUMERIC, "SpMSpV count sweep disagrees with term offsets");
+    T_gen += binoff[NB1];
+
+    // 4. memory plan
+    tok = phase_begin(c, PH_OTHER);
+    u64 maxbin = 0;
+    for (unsigned i = 0; i < NB1; ++i) maxbin = std::max(maxbin, binoff[i + 1] - binoff[i]);
+    MemPlan mp = cmp;
+    if (!cls_mode && !plan_memory(binoff, NB1, T, avail, std::min<u64>(cap, T), maxbin, nlev > 0, mp))
+      return set_error(SFCI_ERR_NOMEM, "SpMSpV device-memory budget too small");
+    if (cls_mode && (maxbin > mp.C1 || maxbin > mp.C2))
+      return set_error(SFCI_ERR_NOMEM, "SpMSpV class pass: a level-1 bin above the buffer capacity");
+    const u64 C2 = mp.C2, C1 = mp.C1, SC = mp.SC;
+    KT* l1k = (KT*)scratch_get(c, "sp_l1k", C1 * sizeof(KT));
+    double* l1a = (double*)scratch_get(c, "sp_l1a", C1 * sizeof(double));
+    KT* l2k = nlev ? (KT*)scratch_get(c, "sp_l2k", C2 * sizeof(KT)) : nullptr;
+    double* l2a = nlev ? (double*)scratch_get(c, "sp_l2a", C2 * sizeof(double)) : nullptr;
+    sk = (KT*)scratch_get(c, "sp_sk", SC * sizeof(KT));
+    sa = (double*)scratch_get(c, "sp_sa", SC * sizeof(double));
+    if (!l1k || !l1a || !sk || !sa || (nlev && (!l2k || !l2a))) return SFCI_ERR_NOMEM;
+    // input dets grouped by global leaf (top b bits of the hash)
+    const u64 NL = 1ull << b;
+    uint32_t* inoff = (uint32_t*)scratch_get(c, "sp_inoff", (NL + 1) * sizeof(uint32_t));
+    uint32_t* incur = (uint32_t*)scratch_get(c, "sp_incur", (NL + 1) * sizeof(uint32_t));
+    KT* ink = (KT*)scratch_get(c, "sp_ink", ns * sizeof(KT));
+    double* ina = (double*)scratch_get(c, "sp_ina", ns * sizeof(double));
+    if (!inoff || !incur || !ink || !ina) return SFCI_ERR_NOMEM;
+    SFCI_CUDA(cudaMemsetAsync(inoff, 0, (NL + 1) * sizeof(uint32_t), c.stream));
+    {
+      unsigned gr = (unsigned)std::min<u64>((ns + 255) / 256, (u64)c.sm_count * 8);
+      SFCI_LAUNCH(c, k_in_count<KT>, gr, 256, 0, src_k, ns, b, inoff);
+      if ((st = scan_excl_u32(c, inoff, inoff, NL))) return st;
+      SFCI_CUDA(cudaMemcpyAsync(incur, inoff, NL * sizeof(uint32_t), cudaMemcpyDeviceToDevice, c.stream));
+      SFCI_LAUNCH(c, k_in_scatter<KT>, gr, 256, 0, src_k, src_a, ns, b, incur, ink, ina);
+    }
+    phase_end(c, tok);
+
+    // pass plan over level-1 bins
+    std::vector<std::pair<unsigned, unsigned>> passes;
+    {
+      unsigned lo = 0;
+      while (lo < NB1) {
+        unsigned hi = lo + 1;
+        while (hi < NB1 && binoff[hi + 1] - binoff[lo] <= C1) ++hi;
+        passes.push_back({lo, hi});
+        lo = hi;
       }
-      // 6b. leaf merge (one warp per leaf)
-      tok = phase_begin(c, PH_MERGE);
-      LeafArgs<KT> la{};
-      la.keys = srck;
-      la.amps = srca;
-      la.loff = loff_dev;
-      la.nleaves = nleaves;
-      la.gleaf0 = (u64)glo << (b - d0);
-      la.in_keys = ink;
-      la.in_amps = ina;
-      la.in_off = inoff;
-      la.cut = fx_cut(cut);
-      la.skeys = sk;
-      la.samps = sa;
-      la.scount = scount;
-      la.dpart = dpart;
-      la.qpart = qpart;
-      la.ovf = ovf;
-      la.ovf_cap = OVF_CAP;
-      la.uniq = scount + 1;
-      la.bad = (unsigned*)(scount + 2);
-      la.dinst = dinst;
-      SFCI_CUDA(cudaMemsetAsync(ovf, 0, sizeof(unsigned), c.stream));
-      const unsigned lg = (unsigned)std::min<u64>((nleaves + LW_WARPS - 1) / LW_WARPS, leaf_resident);
-      SFCI_LAUNCH(c, k_leafw<KT>, lg, LW_WARPS * 32, lsm, la);
-      unsigned novf = 0;
-      if ((st = read_words(c, ovf, sizeof(unsigned), &novf))) return st;
-      if (novf > OVF_CAP) return set_error(SFCI_ERR_NOMEM, "too many oversized SpMSpV leaves");
-      if (novf) {
-        // second tier: one CTA per overflowed leaf, all in one launch
-        SFCI_CUDA(cudaMemsetAsync(ovf2, 0, sizeof(unsigned), c.stream));
-        const unsigned cg = std::min<unsigned>(novf, leafgrid);
-        SFCI_LAUNCH(c, k_leafc<KT>, cg, LC_THREADS, (sizeof(KT) + SLOT_BYTES_EXTRA) * LC_SLOTS, la,
-                    (const unsigned*)(ovf + 1), novf, ovf2);
-        if ((st = read_words(c, ovf2, sizeof(unsigned), &novf))) return st;
-        if (novf > OVF_CAP) return set_error(SFCI_ERR_NOMEM, "too many oversized SpMSpV leaves");
-      }
-      if (novf) {
-        std::vector<unsigned> ids(novf);
-        if ((st = read_words(c, ovf2 + 1, novf * sizeof(unsigned), ids.data()))) return st;
-        big_leaves += novf;
-        for (unsigned id : ids) {
-          const u64 lid = id - la.gleaf0;
-          u64 lb2[2];
-          if ((st = read_words(c, loff_dev + lid, 2 * sizeof(u64), lb2))) return st;
-          const u64 beg = lb2[0], end = lb2[1], n = end - beg;
-          u64 tsz = 1;
-          while (tsz < 2 * n) tsz <<= 1;
-          KT* bk = (KT*)scratch_get(c, "sp_bigk", tsz * sizeof(KT));
-          u64* ba = (u64*)scratch_get(c, "sp_biga", 2 * tsz * sizeof(u64));
-          if (!bk || !ba) return SFCI_ERR_NOMEM;
-          unsigned gr = (unsigned)std::min<u64>((tsz + 255) / 256, (u64)c.sm_count * 8);
-          SFCI_LAUNCH(c, k_fill_empty<KT>, gr, 256, 0, bk, (double*)nullptr, tsz);
-          SFCI_CUDA(cudaMemsetAsync(ba, 0, 2 * tsz * sizeof(u64), c.stream));
-          gr = (unsigned)std::min<u64>((n + 255) / 256, (u64)c.sm_count * 8);
-          if (gr == 0) gr = 1;
-          SFCI_LAUNCH(c, k_big_insert<KT>, gr, 256, 0, (const KT*)srck, (const double*)srca, beg, end, bk, ba,
-                      ba + tsz, (unsigned)(tsz - 1), la.bad);
-          uint32_t ib_ie[2];
-          if ((st = read_words(c, inoff + id, 2 * sizeof(uint32_t), ib_ie))) return st;
-          gr = (unsigned)std::min<u64>((tsz + 255) / 256, (u64)c.sm_count * 8);
-          SFCI_LAUNCH(c, k_big_finish<KT>, gr, 256, 0, (const KT*)bk, (const u64*)ba, (const u64*)(ba + tsz),
-                      (unsigned)(tsz - 1), (const KT*)ink, (const double*)ina, (u64)ib_ie[0], (u64)ib_ie[1],
-                      la.cut, sk, sa, scount, dbig, scount + 1, qpart ? qpart + leafgrid + 1 : nullptr, la.dinst);
-        }
-      }
-      if ((st = read_words(c, scount, sizeof(u64), &scount_h))) return st;
+    }
+    c.stats[5] += passes.size();
+    c.stats[6] = NL;
+    for (auto& ps : passes) {
+      const unsigned lo = ps.first, hi = ps.second;
+      // 5. SCATTER sweep for this pass (level-1 buffer holds bins [lo, hi))
+      tok = phase_begin(c, PH_SCATTER);
+      g.bin_lo = lo;
+      g.bin_hi = hi;
+      g.basem = cntm;
+      g.pass_base = binoff[lo];
+      g.okeys = l1k;
+      g.oamps = l1a;
+      if ((st = launch_gen<W, M_SCATTER>(c, g, G, hi - lo))) return st;
       phase_end(c, tok);
-      glo = ghi;
+      unsigned glo = lo;
+      while (glo < hi) {
+        unsigned ghi = glo + 1;
+        while (ghi < hi && binoff[ghi + 1] - binoff[glo] <= C2) ++ghi;
+        const u64 gterms = binoff[ghi] - binoff[glo];
+        if (scount_h + gterms > SC && scount_h > cap) {
+          int t2 = phase_begin(c, PH_SELECT);
+          size_t m = 0;
+          if ((st = top_k_stable<W>(c, sk, sa, scount_h, cap, -1.0, sk, sa, &m))) return st;
+          scount_h = m;
+          SFCI_CUDA(cudaMemcpyAsync(scount, &scount_h, sizeof(u64), cudaMemcpyHostToDevice, c.stream));
+          phase_end(c, t2);
+        }
+        const unsigned nbg = ghi - glo;
+        // segments of this group: its level-1 bins, positions in the level-1 buffer
+        segs.assign(nbg + 1, 0);
+        for (unsigned i = 0; i <= nbg; ++i) segs[i] = binoff[glo + i] - binoff[lo];
+        const u64 gbase = segs[0];
+        KT* srck = l1k;
+        double* srca = l1a;
+        KT* dstk = l2k;
+        double* dsta = l2a;
+        bool dst_is_l1 = false;
+        u64* loff_dev = nullptr;
+        // 6a. partition levels
+        tok = phase_begin(c, PH_PARTITION);
+        int consumed = d0;
+        for (int k = 0; k < nlev; ++k) {
+          const unsigned nd = 1u << dig[k];
+          const u64 nseg = segs.size() - 1;
+          units.clear();
+          segbase.assign(nseg, 0);
+          segnu.assign(nseg, 0);
+          u64 cbase = 0;
+          for (u64 s = 0; s < nseg; ++s) {
+            const u64 a0 = segs[s], a1 = segs[s + 1], n = a1 - a0;
+            const unsigned nu = (unsigned)std::max<u64>(1, (n + UNIT_ITEMS - 1) / UNIT_ITEMS);
+            segbase[s] = cbase;
+            segnu[s] = nu;
+            for (unsigned j = 0; j < nu; ++j) {
+              Unit un;
+              un.start = a0 + (u64)j * UNIT_ITEMS;
+              un.end = std::min<u64>(a1, un.start + UNIT_ITEMS);
+              if (un.start > un.end) un.start = un.end;
+              un.cbase = cbase + j;
+              un.stride = nu;
+              un.pad = 0;
+              units.push_back(un);
+            }
+            cbase += (u64)nu * nd;
+          }
+          const u64 mlen = cbase;
+          Unit* du = (Unit*)scratch_get(c, "sp_units", units.size() * sizeof(Unit));
+          u64* cm = (u64*)scratch_get(c, "sp_cm", (mlen + 1) * sizeof(u64));
+          u64* dsb = (u64*)scratch_get(c, "sp_segbase", nseg * sizeof(u64));
+          unsigned* dsn = (unsigned*)scratch_get(c, "sp_segnu", nseg * sizeof(unsigned));
+          u64* nextoff = (u64*)scratch_get(c, k == nlev - 1 ? "sp_loff" : "sp_segoff", (nseg * nd + 1) * sizeof(u64));
+          if (!du || !cm || !dsb || !dsn || !nextoff) return SFCI_ERR_NOMEM;
+          SFCI_CUDA(cudaMemcpyAsync(du, units.data(), units.size() * sizeof(Unit), cudaMemcpyHostToDevice, c.stream));
+          SFCI_CUDA(cudaMemcpyAsync(dsb, segbase.data(), nseg * sizeof(u64), cudaMemcpyHostToDevice, c.stream));
+          SFCI_CUDA(cudaMemcpyAsync(dsn, segnu.data(), nseg * sizeof(unsigned), cudaMemcpyHostToDevice, c.stream));
+          PartArgs<KT> pa{};
+          pa.ikeys = srck;
+          pa.iamps = srca;
+          pa.units = du;
+          pa.nunits = (unsigned)units.size();
+          pa.shift = 64 - consumed - dig[k];
+          pa.nd = nd;
+          pa.cm = cm;
+          pa.dst_base = dst_is_l1 ? gbase : 0;
+          pa.okeys = dstk;
+          pa.oamps = dsta;
+          const unsigned pgrid = (unsigned)std::min<u64>(units.size(), (u64)c.sm_count * 4);
+          const size_t smc = part_smem_bytes<KT, IPT>(M_COUNT, nd);
+          const size_t sms = part_smem_bytes<KT, IPT>(M_SCATTER, nd);
+          SFCI_LAUNCH(c, (k_part<KT, M_COUNT, IPT>), pgrid, PT_THREADS, smc, pa);
+          if ((st = scan_excl(c, cm, cm, mlen))) return st;
+          SFCI_LAUNCH(c, (k_part<KT, M_SCATTER, IPT>), pgrid, PT_THREADS, sms, pa);
+          {
+            const u64 nn = nseg * nd + 1;
+            unsigned gr = (unsigned)std::min<u64>((nn + 255) / 256, (u64)c.sm_count * 8);
+            SFCI_LAUNCH(c, k_seg_gather, gr, 256, 0, (const u64*)cm, (const u64*)dsb, (const unsigned*)dsn, nseg, nd,
+                        mlen, pa.dst_base, nextoff);
+          }
+          consumed += dig[k];
+          if (k == nlev - 1) {
+            loff_dev = nextoff;
+            segs.resize(nseg * nd + 1);  // sizes only needed for the leaf count below
+          } else {
+            nsegs_h.resize(nseg * nd + 1);
+            if ((st = read_words(c, nextoff, (nseg * nd + 1) * sizeof(u64), nsegs_h.data()))) return st;
+            segs.swap(nsegs_h);
+          }
+          std::swap(srck, dstk);
+          std::swap(srca, dsta);
+          dst_is_l1 = !dst_is_l1;
+        }
+        phase_end(c, tok);
+        const u64 nleaves = segs.size() - 1;
+        if (nlev == 0) {
+          loff_dev = (u64*)scratch_get(c, "sp_loff", (nleaves + 1) * sizeof(u64));
+          if (!loff_dev) return SFCI_ERR_NOMEM;
+          SFCI_CUDA(cudaMemcpyAsync(loff_dev, segs.data(), (nleaves + 1) * sizeof(u64), cudaMemcpyHostToDevice,
+                                    c.stream));
+        }
+        // 6b. leaf merge (one warp per leaf)
+        tok = phase_begin(c, PH_MERGE);
+        LeafArgs<KT> la{};
+        la.keys = srck;
+        la.amps = srca;
+        la.loff = loff_dev;
+        la.nleaves = nleaves;
+        la.gleaf0 = (u64)glo << (b - d0);
+        la.in_keys = ink;
+        la.in_amps = ina;
+        la.in_off = inoff;
+        la.cut = fx_cut(cut);
+        la.skeys = sk;
+        la.samps = sa;
+        la.scount = scount;
+        la.dpart = dpart;
+        la.qpart = qpart;
+        la.ovf = ovf;
+        la.ovf_cap = OVF_CAP;
+        la.uniq = scount + 1;
+        la.bad = (unsigned*)(scount + 2);
+        la.dinst = dinst;
+        SFCI_CUDA(cudaMemsetAsync(ovf, 0, sizeof(unsigned), c.stream));
+        const unsigned lg = (unsigned)std::min<u64>((nleaves + LW_WARPS - 1) / LW_WARPS, leaf_resident);
+        SFCI_LAUNCH(c, k_leafw<KT>, lg, LW_WARPS * 32, lsm, la);
+        unsigned novf = 0;
+        if ((st = read_words(c, ovf, sizeof(unsigned), &novf))) return st;
+        if (novf > OVF_CAP) return set_error(SFCI_ERR_NOMEM, "too many oversized SpMSpV leaves");
+        if (novf) {
+          // second tier: one CTA per overflowed leaf, all in one launch
+          SFCI_CUDA(cudaMemsetAsync(ovf2, 0, sizeof(unsigned), c.stream));
+          const unsigned cg = std::min<unsigned>(novf, leafgrid);
+          SFCI_LAUNCH(c, k_leafc<KT>, cg, LC_THREADS, (sizeof(KT) + SLOT_BYTES_EXTRA) * LC_SLOTS, la,
+                      (const unsigned*)(ovf + 1), novf, ovf2);
+          if ((st = read_words(c, ovf2, sizeof(unsigned), &novf))) return st;
+          if (novf > OVF_CAP) return set_error(SFCI_ERR_NOMEM, "too many oversized SpMSpV leaves");
+        }
+        if (novf) {
+          std::vector<unsigned> ids(novf);
+          if ((st = read_words(c, ovf2 + 1, novf * sizeof(unsigned), ids.data()))) return st;
+          big_leaves += novf;
+          for (unsigned id : ids) {
+            const u64 lid = id - la.gleaf0;
+            u64 lb2[2];
+            if ((st = read_words(c, loff_dev + lid, 2 * sizeof(u64), lb2))) return st;
+            const u64 beg = lb2[0], end = lb2[1], n = end - beg;
+            u64 tsz = 1;
+            while (tsz < 2 * n) tsz <<= 1;
+            KT* bk = (KT*)scratch_get(c, "sp_bigk", tsz * sizeof(KT));
+            u64* ba = (u64*)scratch_get(c, "sp_biga", 2 * tsz * sizeof(u64));
+            if (!bk || !ba) return SFCI_ERR_NOMEM;
+            unsigned gr = (unsigned)std::min<u64>((tsz + 255) / 256, (u64)c.sm_count * 8);
+            SFCI_LAUNCH(c, k_fill_empty<KT>, gr, 256, 0, bk, (double*)nullptr, tsz);
+            SFCI_CUDA(cudaMemsetAsync(ba, 0, 2 * tsz * sizeof(u64), c.stream));
+            gr = (unsigned)std::min<u64>((n + 255) / 256, (u64)c.sm_count * 8);
+            if (gr == 0) gr = 1;
+            SFCI_LAUNCH(c, k_big_insert<KT>, gr, 256, 0, (const KT*)srck, (const double*)srca, beg, end, bk, ba,
+                        ba + tsz, (unsigned)(tsz - 1), la.bad);
+            uint32_t ib_ie[2];
+            if ((st = read_words(c, inoff + id, 2 * sizeof(uint32_t), ib_ie))) return st;
+            gr = (unsigned)std::min<u64>((tsz + 255) / 256, (u64)c.sm_count * 8);
+            SFCI_LAUNCH(c, k_big_finish<KT>, gr, 256, 0, (const KT*)bk, (const u64*)ba, (const u64*)(ba + tsz),
+                        (unsigned)(tsz - 1), (const KT*)ink, (const double*)ina, (u64)ib_ie[0], (u64)ib_ie[1],
+                        la.cut, sk, sa, scount, dbig, scount + 1, qpart ? qpart + leafgrid + 1 : nullptr, la.dinst);
+          }
+        }
+        if ((st = read_words(c, scount, sizeof(u64), &scount_h))) return st;
+        phase_end(c, tok);
+        glo = ghi;
+      }
     }
   }
   c.stats[7] = big_leaves;
+  c.stats[1] = T_gen;
   // 7. <v|Hv> and final selection + key sort
   tok = phase_begin(c, PH_OTHER);
   SFCI_LAUNCH(c, k_sum_parts, 1, 32, 0, (const double*)dpart, (int)leafgrid, dpart + leafgrid);
@@ -1689,7 +1931,7 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
     u64 uq = 0;
     if ((st = read_words(c, scount + 1, sizeof(u64), &uq))) return st;
     c.stats[2] = uq;
-    if (uq) c.dup_est = (double)T / (double)uq;
+    if (uq) c.dup_est = (double)T_gen / (double)uq;
   }
   *diag = dl + dbig_h;
   if (dinst) {

@@ -104,6 +104,17 @@ def test_configs2_system_products_lanczos_and_minres(sys128, port):
     rep = compare_vectors(rk, ra, k, a, cut=CUT, capped=len(ra) == 4000000)
     assert close(d, rd)
     print("128-orbital SpMSpV: %d determinants, max rel diff %.2e" % (rep["common"], rep["max_rel"]))
+    # the same product in class passes (a 3 GB budget: several passes, each
+    # generating only the terms whose target alpha class it owns): bit for bit
+    cc = sg.Context(sys128, N, ne, Nd=200000, mem_budget=3 << 30)
+    cc.set_class_passes(1)
+    out_c = cc.vec(4000000)
+    d_c = cc.SpMVMtply_bucket(cc.vec_from(keys, amps), out_c, 0.0, 1.0)
+    kc, ac = out_c.download()
+    assert cc.last_stats()["passes"] > 1
+    assert np.array_equal(kc, k) and np.array_equal(ac.view(np.uint64), a.view(np.uint64))
+    assert close(d_c, d)
+    del cc, out_c
     # top-Nd slice, shift and a negative coefficient, capped output
     c.set_Nd(400)
     be.set_nd(400)

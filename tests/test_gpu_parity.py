@@ -337,3 +337,31 @@ def test_hot_key_sum_rounds_to_nearest(golden_in, port, nsrc, target):
     i = np.searchsorted(k, np.uint64(hf))
     assert i < len(k) and k[i] == hf
     assert abs(a[i] - want) <= 1e-12 * abs(want), (a[i], want, (a[i] - want) / want)
+
+
+@pytest.mark.parametrize("budget", [640 << 20, 400 << 20, 200 << 20])
+def test_class_passes_give_the_single_pass_product(golden_in, budget):
+    """Generation passes that own ranges of the targets' alpha class (each pass
+    generating only its own terms) must give the single-pass product bit for
+    bit, whatever the budget and hence the number of passes."""
+    g, path = golden_in("r28")
+    rng = np.random.default_rng(43)
+    ints, amps = _sample_vector(rng, 56, 14, 3000)
+    keys = np.array(ints, np.uint64)
+    c0 = sg.Context(path, 56, 14, Nd=200000)
+    vin = c0.vec_from(keys, amps)
+    out = c0.vec(2000000)
+    d0 = c0.SpMVMtply_bucket(vin, out, 0.0, 1.0)
+    k0, a0 = out.download()
+    t0 = c0.last_stats()["terms"]
+    c = sg.Context(path, 56, 14, Nd=200000, mem_budget=budget)
+    c.set_class_passes(1)
+    vin = c.vec_from(keys, amps)
+    out = c.vec(2000000)
+    d = c.SpMVMtply_bucket(vin, out, 0.0, 1.0)
+    st = c.last_stats()
+    k, a = out.download()
+    assert st["passes"] > 1 and st["terms"] == t0, st
+    assert np.array_equal(k, k0)
+    assert np.array_equal(a.view(np.uint64), a0.view(np.uint64))
+    assert close(d, d0)

@@ -96,8 +96,14 @@ def hf_key(sysd):
     return np.array([[hf & (2 ** 64 - 1), hf >> 64]], np.uint64)
 
 
-INPUT_TEXT = ("top-Nd of H (H|HF>) by |amplitude|, normalised (both products without the 1e-5 cut; "
-              "H|HF> holds every connected determinant)")
+INPUT_TEXT = ("top-Nd of H v1 by |amplitude|, normalised, v1 = the top m = max(64, ceil(50 Nd / C)) of H|HF> "
+              "(normalised; both products without the 1e-5 cut; ties kept from the highest keys)")
+
+
+def input_m(sysd, nd):
+    """How many determinants of H|HF> the input's second product multiplies."""
+    C = connected_per_det(sysd["M"], sysd["ne"] // 2, sysd["ne"] // 2)
+    return min(C + 1, max(64, -(-50 * nd // C)))
 
 
 def bench_config(sysd, nd, input_dets):
@@ -117,11 +123,14 @@ def input_on_gpu(sg, path, sysd, nd):
     v1 = c0.vec(C1)
     c0.SpMVMtply_bucket(hf, v1, 0.0, 1.0)
     v1.normalize()
+    v1m = c0.vec(input_m(sysd, nd))
+    v1m.shrinkFrom(v1)  # top m by |amplitude|, ties kept from the highest keys
+    v1m.normalize()
     v2 = c0.vec(nd)
-    c0.SpMVMtply_bucket(v1, v2, 0.0, 1.0)
+    c0.SpMVMtply_bucket(v1m, v2, 0.0, 1.0)
     v2.normalize()
     k, a = v2.download()
-    del v1, v2, hf, c0
+    del v1, v1m, v2, hf, c0
     return k, a
 
 
@@ -131,6 +140,8 @@ def input_on_cpu(be, sysd, nd):
     be.set_cut(-1.0)
     try:
         k1, a1, _ = be.spmspv(hf_key(sysd), np.array([1.0]), C1, 0.0, 1.0)
+        a1 = a1 / np.linalg.norm(a1)
+        k1, a1 = be.shrink_from(k1, a1, input_m(sysd, nd))  # ties kept from the highest keys
         a1 = a1 / np.linalg.norm(a1)
         k2, a2, _ = be.spmspv(k1, a1, nd, 0.0, 1.0)
     finally:
@@ -475,6 +486,7 @@ def run_gpu(args, rank, ws, local, dist):
     if not args.no_cpu_baseline:
         base, sample, ref_out = cpu_baseline(sysd, path, keys_h, amps_h, target_s=args.cpu_seconds)
         res["cpu_baseline"] = base
+        ctx.trim()  # the timed product's scratch holds most of the device
         res["parity"] = parity_report(ctx, sample, ref_out)
     print(json.dumps(res), flush=True)
     barrier(dist)
@@ -526,8 +538,9 @@ def run_screen(args):
         vin = _krylov_input(sg, ctx, sysd, args.screen_log_nd)
         out = ctx.vec(HPSI_CAP)
         ctx.SpMVMtply_bucket(vin, out, 0.0, 1.0)
-        # the screen lives on the first context; each system logs from its own
-        ne, npos = scr.log(vin, out)
+        # the screen lives on the first context; each system logs from its own.
+        # A group is alive when a term above 1e-3 of the cut lands on a survivor.
+        ne, npos = scr.log(vin, out, min_term=args.screen_min_term)
         tr["systems"].append({"seed": sd, "sources": vin.len, "examples": ne, "positives": npos})
         tr["examples"] += ne
         tr["positives"] += npos
@@ -599,6 +612,56 @@ def run_screen(args):
     res["speedup_vs_plain"] = plain["seconds"] / best["seconds"] if best else 1.0
     res["fallback"] = best is None
     res["connected_per_det"] = C
+    print(json.dumps(res), flush=True)
+
+
+def run_mlp(args):
+    """Throughput of the screen's tensor-core kernels on the 56-spin-orbital
+    system: inference over every term group of a Krylov vector's top
+    --mlp-sources determinants (1,870 groups each), and Adam training steps on
+    the groups' labels.  Tensor FLOPs: 2 x 256 x 256 per group for inference;
+    per training example the forward and backward 256 x 256 products and the
+    weight-gradient products of both layers (2 x 256 x (256 + 256 + 576))."""
+    import sfci_gb300 as sg
+    sg.load_library()
+    sysd = SYSTEMS[1]
+    path = workload_in(sysd)
+    M, NE = sysd["M"], sysd["ne"]
+    ctx = sg.Context(path, 2 * M, NE, Nd=args.mlp_sources, hpsi_cap=HPSI_CAP)
+    vin = _krylov_input(sg, ctx, sysd, args.mlp_sources)
+    scr = sg.Screen(ctx, seed=3)
+    out = ctx.vec(HPSI_CAP)
+    ctx.SpMVMtply_bucket(vin, out, 0.0, 1.0)
+    ne, npos = scr.log(vin, out)
+    scr.predict(vin, 0.5)  # warm-up
+    t0 = time.perf_counter()
+    reps = 5
+    for _ in range(reps):
+        r = scr.predict(vin, 0.5)
+    t_inf = (time.perf_counter() - t0) / reps
+    groups = r["groups"]
+    scr.train(2, batch_tiles=args.mlp_batch_tiles, lr=1e-3)  # warm-up
+    steps = 50
+    t0 = time.perf_counter()
+    scr.train(steps, batch_tiles=args.mlp_batch_tiles, lr=1e-3)
+    t_tr = (time.perf_counter() - t0) / steps
+    B = args.mlp_batch_tiles * 128
+    f_inf = 2.0 * 256 * 256 * groups
+    f_tr = 2.0 * 256 * (256 + 256 + 256 + 576) * B
+    peak = None
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peak = float(json.load(f)["bf16_tflops"])
+    except Exception:
+        pass
+    res = {"metric": METRIC, "mode": "screen MLP throughput", "unit": "tensor TFLOP/s",
+           "config": {"workload": "MLP 576-256-256-1 on the term groups of a 56-spin-orbital Krylov vector",
+                      "sources": vin.len, "groups": groups, "batch": B},
+           "inference": {"seconds": t_inf, "groups_per_s": groups / t_inf, "tflops": f_inf / t_inf / 1e12,
+                         "frac_of_bf16_peak": (f_inf / t_inf / 1e12 / peak) if peak else None},
+           "training": {"seconds_per_step": t_tr, "examples_per_s": B / t_tr, "tflops": f_tr / t_tr / 1e12,
+                        "frac_of_bf16_peak": (f_tr / t_tr / 1e12 / peak) if peak else None},
+           "logged": {"examples": ne, "positives": npos}, "bf16_peak_tflops": peak}
     print(json.dumps(res), flush=True)
 
 
@@ -727,13 +790,20 @@ def main():
     ap.add_argument("--screen-lr", type=float, default=1e-3)
     ap.add_argument("--screen-seed", type=int, default=5)
     ap.add_argument("--screen-tol", type=float, default=1e-5)
+    ap.add_argument("--screen-min-term", type=float, default=1e-8)
     ap.add_argument("--screen-thresholds", type=float, nargs="+", default=[0.02, 0.05, 0.1, 0.2, 0.35])
     ap.add_argument("--batch", action="store_true",
                     help="batched bond-stretch curve: 32 instances, batched vs unbatched Lanczos")
     ap.add_argument("--batch-scale", type=float, default=0.01,
                     help="scale of the instances' Nd (1.0: 1e5 to 2e6)")
     ap.add_argument("--batch-nl", type=int, default=10)
+    ap.add_argument("--mlp", action="store_true", help="throughput of the screen's tensor-core MLP kernels")
+    ap.add_argument("--mlp-sources", type=int, default=20000)
+    ap.add_argument("--mlp-batch-tiles", type=int, default=128)
     args = ap.parse_args()
+    if args.mlp:
+        run_mlp(args)
+        return
     if args.screen:
         run_screen(args)
         return

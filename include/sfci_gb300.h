@@ -276,12 +276,12 @@ typedef struct sfci_screen sfci_screen;
 int sfci_screen_create(sfci_ctx* ctx, uint64_t seed, sfci_screen** out);
 int sfci_screen_destroy(sfci_screen* s);
 /* Appends labelled examples: every term group of the determinants of `in` (at
- * most Nd of them: the sources of a product), alive when one of its terms lands
- * on a key of `out`, the product's output.  `in` and `out` may belong to another
+ * most Nd of them: the sources of a product), alive when one of its terms of
+ * magnitude above min_term (0: any) lands on a key of `out`, the product's output.  `in` and `out` may belong to another
  * context with the same number of orbitals (another Hamiltonian, up to 64 of
  * them per screen); the screen keeps that Hamiltonian's integral bounds for the
  * examples' features. */
-int sfci_screen_log(sfci_screen* s, const sfci_vec* in, const sfci_vec* out, uint64_t* examples,
+int sfci_screen_log(sfci_screen* s, const sfci_vec* in, const sfci_vec* out, double min_term, uint64_t* examples,
                     uint64_t* positives);
 /* `steps` Adam steps on batches of batch_tiles x 128 logged examples (random
  * windows, or consecutive from the first example when `sequential`), binary

@@ -106,7 +106,7 @@ def _sigs(L):
     L.sfci_autotune.argtypes = [_vp, _vp, _vp, _vp, C.POINTER(C.c_double)]
     L.sfci_screen_create.argtypes = [_vp, C.c_uint64, C.POINTER(_vp)]
     L.sfci_screen_destroy.argtypes = [_vp]
-    L.sfci_screen_log.argtypes = [_vp, _vp, _vp, _u64p, _u64p]
+    L.sfci_screen_log.argtypes = [_vp, _vp, _vp, C.c_double, _u64p, _u64p]
     L.sfci_screen_train.argtypes = [_vp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, C.POINTER(C.c_double)]
     L.sfci_screen_stats.argtypes = [_vp, _u64p, _u64p, _u64p, _u64p]
     L.sfci_screen_predict.argtypes = [_vp, _vp, C.c_double, _u64p, _u64p, _u64p, _vp, C.c_uint64]
@@ -494,10 +494,11 @@ class Screen:
         except Exception:
             pass
 
-    def log(self, vin: "SpVec", vout: "SpVec"):
-        """Label the groups of vin's determinants by vout (the product of vin)."""
+    def log(self, vin: "SpVec", vout: "SpVec", min_term: float = 0.0):
+        """Label the groups of vin's determinants by vout (the product of vin): alive when
+        a term of magnitude above min_term lands on a determinant of vout."""
         ne, npos = C.c_uint64(), C.c_uint64()
-        _check(self.L.sfci_screen_log(self.h, vin.h, vout.h, C.byref(ne), C.byref(npos)))
+        _check(self.L.sfci_screen_log(self.h, vin.h, vout.h, float(min_term), C.byref(ne), C.byref(npos)))
         return ne.value, npos.value
 
     def train(self, steps: int, batch_tiles: int = 64, lr: float = 1e-3, pos_weight: float = 1.0,

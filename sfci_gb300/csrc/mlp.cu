@@ -1031,7 +1031,7 @@ __global__ void k_abs_copy(double* dst, const double* src, u64 n) {
 // labels from its output.  The vectors may live on another context over a
 // Hamiltonian with the same number of orbitals: its term groups are labelled
 // there, and its integral-bound table joins the screen's as a new system.
-static int screen_log(Screen& s, const Vec& in, const Vec& out, u64* nex_out, u64* npos_out) {
+static int screen_log(Screen& s, const Vec& in, const Vec& out, double min_term, u64* nex_out, u64* npos_out) {
   Ctx& c = *s.ctx;
   Ctx& vc = *in.ctx;
   int st;
@@ -1101,8 +1101,8 @@ static int screen_log(Screen& s, const Vec& in, const Vec& out, u64* nex_out, u6
   uint32_t* lab = (uint32_t*)scratch_get(vc, "sc_lab", ((ne + 31) / 32 + 1) * sizeof(uint32_t));
   if (!lab) return SFCI_ERR_NOMEM;
   SFCI_CUDA(cudaMemsetAsync(lab, 0, ((ne + 31) / 32 + 1) * sizeof(uint32_t), vc.stream));
-  if ((st = vc.W == 1 ? label_impl<1>(vc, (const u64*)keys, amps, n, goff, out, lab)
-                      : label_impl<2>(vc, (const K128*)keys, amps, n, goff, out, lab)))
+  if ((st = vc.W == 1 ? label_impl<1>(vc, (const u64*)keys, amps, n, goff, out, lab, min_term)
+                      : label_impl<2>(vc, (const K128*)keys, amps, n, goff, out, lab, min_term)))
     return st;
   // shift the new words into place (s.nex is not word-aligned in general)
   {
@@ -1277,13 +1277,13 @@ extern "C" int sfci_screen_destroy(sfci_screen* x) {
   return SFCI_OK;
 }
 
-extern "C" int sfci_screen_log(sfci_screen* x, const sfci_vec* in, const sfci_vec* out, uint64_t* examples,
-                               uint64_t* positives) {
+extern "C" int sfci_screen_log(sfci_screen* x, const sfci_vec* in, const sfci_vec* out, double min_term,
+                               uint64_t* examples, uint64_t* positives) {
   if (!x || !in || !out) return set_error(SFCI_ERR_ARG, "sfci_screen_log: null argument");
   if (!x->s.ctx) return set_error(SFCI_ERR_ARG, "sfci_screen_log: the screen's context was destroyed");
   if (!in->v.ctx || !out->v.ctx) return set_error(SFCI_ERR_ARG, "sfci_screen_log: vector of a destroyed context");
   u64 ne = 0, np = 0;
-  int st = screen_log(x->s, in->v, out->v, &ne, &np);
+  int st = screen_log(x->s, in->v, out->v, min_term, &ne, &np);
   if (examples) *examples = ne;
   if (positives) *positives = np;
   return st;

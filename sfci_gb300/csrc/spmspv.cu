@@ -229,6 +229,7 @@ struct GenArgs {
   unsigned kl_cap = 0;      // shared-memory entries (the longest list)
   const u64* goff = nullptr;  // LABEL: first example of each source
   uint32_t* labels = nullptr; // LABEL: one bit per (source, group >= 1)
+  double label_min = 0.0;     // LABEL: a term counts when |term| > label_min
   // class pass (COUNT / SCATTER): only targets whose alpha class is in
   // [cls_lo, cls_hi).  A determinant's index space is then [0, c[3]) (diagonal,
   // singles, spin-0 doubles: filtered term by term), its spin-1 doubles when its
@@ -539,7 +540,9 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
                 atomicAdd(&hist[(unsigned)(key_hash(target_key(dh, d, decode(dh, pt, lf))) >> shift1)], 1u);
             } else if (MODE == M_LABEL) {
               // a group is alive when one of its terms lands on the product's output
-              if (table_find_global(g.tkeys, g.tmask, target_key(dh, d, decode(dh, pt, l))) >= 0) {
+              const Exc e = decode(dh, pt, l);
+              if (table_find_global(g.tkeys, g.tmask, target_key(dh, d, e)) >= 0 &&
+                  (g.label_min <= 0.0 || fabs(term_amp(dh, d, e, hv)) > g.label_min)) {
                 const GroupCounts gc = group_counts(dh.na[0], dh.nv[0], dh.na[1], dh.nv[1]);
                 const unsigned gi = group_of_term(gc, dh.c, l);
                 if (gi) {
@@ -1554,10 +1557,7 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
     cudaGetLastError();
   }
   double* dpart = (double*)scratch_get(c, "sp_dpart", (leafgrid + 1) * sizeof(double));
-  const unsigned OVF_CAP = 1u << 20;
-  unsigned* ovf = (unsigned*)scratch_get(c, "sp_ovf", (OVF_CAP + 1) * sizeof(unsigned));
-  unsigned* ovf2 = (unsigned*)scratch_get(c, "sp_ovf2", (OVF_CAP + 1) * sizeof(unsigned));
-  if (!scount || !dpart || !ovf || !ovf2) return SFCI_ERR_NOMEM;
+  if (!scount || !dpart) return SFCI_ERR_NOMEM;
   SFCI_CUDA(cudaMemsetAsync(scount, 0, 4 * sizeof(u64), c.stream));
   SFCI_CUDA(cudaMemsetAsync(dpart, 0, (leafgrid + 1) * sizeof(double), c.stream));
   // optional sum of squared merged amplitudes: per-CTA partials, then the global tier's sum
@@ -1842,6 +1842,13 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
         la.scount = scount;
         la.dpart = dpart;
         la.qpart = qpart;
+        // overflow lists of the two table tiers: every leaf of the group can
+        // overflow a tier at most once (the leaf count comes from the previous
+        // product's duplication, which can be off by several times)
+        unsigned* ovf = (unsigned*)scratch_get(c, "sp_ovf", (nleaves + 1) * sizeof(unsigned));
+        unsigned* ovf2 = (unsigned*)scratch_get(c, "sp_ovf2", (nleaves + 1) * sizeof(unsigned));
+        if (!ovf || !ovf2) return SFCI_ERR_NOMEM;
+        const unsigned OVF_CAP = (unsigned)nleaves;
         la.ovf = ovf;
         la.ovf_cap = OVF_CAP;
         la.uniq = scount + 1;
@@ -2217,7 +2224,7 @@ int group_offsets_impl(Ctx& c, const typename KeyOf<W>::T* keys, u64 n, u64* gof
 
 template <int W>
 int label_impl(Ctx& c, const typename KeyOf<W>::T* keys, const double* amps, u64 n, const u64* goff, const Vec& out,
-               uint32_t* labels) {
+               uint32_t* labels, double min_term) {
   typedef typename KeyOf<W>::T KT;
   if (n == 0 || out.len == 0) return SFCI_OK;
   int st;
@@ -2250,13 +2257,14 @@ int label_impl(Ctx& c, const typename KeyOf<W>::T* keys, const double* amps, u64
   g.tmask = (unsigned)(tsz - 1);
   g.goff = goff;
   g.labels = labels;
+  g.label_min = min_term;
   return launch_gen<W, M_LABEL>(c, g, gen_grid(c, T), 0);
 }
 
 template int group_offsets_impl<1>(Ctx&, const u64*, u64, u64*);
 template int group_offsets_impl<2>(Ctx&, const K128*, u64, u64*);
-template int label_impl<1>(Ctx&, const u64*, const double*, u64, const u64*, const Vec&, uint32_t*);
-template int label_impl<2>(Ctx&, const K128*, const double*, u64, const u64*, const Vec&, uint32_t*);
+template int label_impl<1>(Ctx&, const u64*, const double*, u64, const u64*, const Vec&, uint32_t*, double);
+template int label_impl<2>(Ctx&, const K128*, const double*, u64, const u64*, const Vec&, uint32_t*, double);
 
 template int spmspv_impl<1>(Ctx&, const Vec&, Vec&, double, double, double*, const SpExtra*);
 template int spmspv_impl<2>(Ctx&, const Vec&, Vec&, double, double, double*, const SpExtra*);

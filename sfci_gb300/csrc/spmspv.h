@@ -56,10 +56,11 @@ struct ScreenList {
 int screen_select(Ctx& c, const void* keys, const double* amps, u64 n, ScreenList* out);
 // groups per source (group 0 excluded), exclusive prefix in goff[0..n]
 template <int W> int group_offsets_impl(Ctx& c, const typename KeyOf<W>::T* keys, u64 n, u64* goff);
-// label bits of the groups of n sources: a group is alive when one of its terms
-// lands on a key of `out` (the product's output); bit goff[j] + g - 1 of labels
+// label bits of the groups of n sources: a group is alive when one of its terms,
+// of magnitude above min_term, lands on a key of `out` (the product's output);
+// bit goff[j] + g - 1 of labels
 template <int W> int label_impl(Ctx& c, const typename KeyOf<W>::T* keys, const double* amps, u64 n,
-                                const u64* goff, const Vec& out, uint32_t* labels);
+                                const u64* goff, const Vec& out, uint32_t* labels, double min_term);
 
 // batched contexts: first position of each instance tag 0..n in a key-sorted
 // vector (n + 1 entries, host)

@@ -96,14 +96,15 @@ def hf_key(sysd):
     return np.array([[hf & (2 ** 64 - 1), hf >> 64]], np.uint64)
 
 
-INPUT_TEXT = ("top-Nd of H v1 by |amplitude|, normalised, v1 = the top m = max(64, ceil(50 Nd / C)) of H|HF> "
-              "(normalised; both products without the 1e-5 cut; ties kept from the highest keys)")
+INPUT_TEXT = ("third Krylov vector: v1 = H|HF>, v2 = H top_m1(v1), v3 = H top_m2(v2), input = top-Nd of v3 by "
+              "|amplitude|; m1 = 2000 and m2 = 30000 scaled by 30723 / C; every vector normalised, products "
+              "without the 1e-5 cut, ties kept from the highest keys")
 
 
-def input_m(sysd, nd):
-    """How many determinants of H|HF> the input's second product multiplies."""
+def input_ms(sysd):
+    """How many determinants of v1 and of v2 the input's later products multiply."""
     C = connected_per_det(sysd["M"], sysd["ne"] // 2, sysd["ne"] // 2)
-    return min(C + 1, max(64, -(-50 * nd // C)))
+    return max(64, 2000 * 30723 // C), max(256, 30000 * 30723 // C)
 
 
 def bench_config(sysd, nd, input_dets):
@@ -120,17 +121,18 @@ def input_on_gpu(sg, path, sysd, nd):
     hf = c0.vec(1)
     hf.upload(hf_key(sysd), np.array([1.0]))
     C1 = connected_per_det(sysd["M"], sysd["ne"] // 2, sysd["ne"] // 2) + 1
-    v1 = c0.vec(C1)
-    c0.SpMVMtply_bucket(hf, v1, 0.0, 1.0)
-    v1.normalize()
-    v1m = c0.vec(input_m(sysd, nd))
-    v1m.shrinkFrom(v1)  # top m by |amplitude|, ties kept from the highest keys
-    v1m.normalize()
-    v2 = c0.vec(nd)
-    c0.SpMVMtply_bucket(v1m, v2, 0.0, 1.0)
-    v2.normalize()
-    k, a = v2.download()
-    del v1, v1m, v2, hf, c0
+    m1, m2 = input_ms(sysd)
+    v = c0.vec(C1)
+    c0.SpMVMtply_bucket(hf, v, 0.0, 1.0)
+    for m, cap in ((m1, HPSI_CAP), (m2, nd)):
+        vm = c0.vec(m)
+        vm.shrinkFrom(v)  # top m by |amplitude|, ties kept from the highest keys
+        vm.normalize()
+        v = c0.vec(cap)
+        c0.SpMVMtply_bucket(vm, v, 0.0, 1.0)
+    v.normalize()
+    k, a = v.download()
+    del v, vm, hf, c0
     return k, a
 
 
@@ -139,11 +141,13 @@ def input_on_cpu(be, sysd, nd):
     C1 = connected_per_det(sysd["M"], sysd["ne"] // 2, sysd["ne"] // 2) + 1
     be.set_cut(-1.0)
     try:
-        k1, a1, _ = be.spmspv(hf_key(sysd), np.array([1.0]), C1, 0.0, 1.0)
-        a1 = a1 / np.linalg.norm(a1)
-        k1, a1 = be.shrink_from(k1, a1, input_m(sysd, nd))  # ties kept from the highest keys
-        a1 = a1 / np.linalg.norm(a1)
-        k2, a2, _ = be.spmspv(k1, a1, nd, 0.0, 1.0)
+        m1, m2 = input_ms(sysd)
+        k, a, _ = be.spmspv(hf_key(sysd), np.array([1.0]), C1, 0.0, 1.0)
+        for m, cap in ((m1, HPSI_CAP), (m2, nd)):
+            k, a = be.shrink_from(k, a, m)  # ties kept from the highest keys
+            a = a / np.linalg.norm(a)
+            k, a, _ = be.spmspv(k, a, cap, 0.0, 1.0)
+        k2, a2 = k, a
     finally:
         be.set_cut(1e-5)
     return k2, a2 / np.linalg.norm(a2)
@@ -384,6 +388,9 @@ def run_gpu(args, rank, ws, local, dist):
     ms_max = reduce_max(dist, ms, local)
     # ---- end to end from pinned host buffers
     keys_h, amps_h = in_k, in_a
+    if args.no_e2e:
+        return _finish_gpu(args, rank, ws, dist, ctx, sysd, path, nd, M, NE, W, n_in, C, T_conn, ms_max, clk, prof,
+                           stats, out_len, launches, diag, keys_h, amps_h, None, 0, 0)
     e2e_ms = None
     h2d = d2h = 0
     try:
@@ -418,6 +425,13 @@ def run_gpu(args, rank, ws, local, dist):
     tbytes = 8 * W + 8  # one determinant: key words + FP64 amplitude
     h2d = n_in * tbytes
     d2h = got.value * tbytes + 8
+    return _finish_gpu(args, rank, ws, dist, ctx, sysd, path, nd, M, NE, W, n_in, C, T_conn, ms_max, clk, prof, stats,
+                       out_len, launches, diag, keys_h, amps_h, e2e_s, h2d, d2h)
+
+
+def _finish_gpu(args, rank, ws, dist, ctx, sysd, path, nd, M, NE, W, n_in, C, T_conn, ms_max, clk, prof, stats,
+                out_len, launches, diag, keys_h, amps_h, e2e_s, h2d, d2h):
+    tbytes = 8 * W + 8  # one determinant: key words + FP64 amplitude
     if rank != 0:
         barrier(dist)
         return
@@ -453,7 +467,7 @@ def run_gpu(args, rank, ws, local, dist):
     traffic = (ncu_bytes_per_term[dom] * T * args.steps / max(dl, 1)) if (dom in ncu_bytes_per_term and W == 1) \
         else None  # measured for one-word keys
     value = T_conn * ws / (ms_max * 1e-3)
-    e2e_val = T_conn * ws / e2e_s
+    e2e_val = T_conn * ws / e2e_s if e2e_s else None
     # the whole product under the materialise-once model: read the input, write
     # and read every connected term once, write the merged determinants once
     B = (n_in + 2 * T_conn + stats["unique"]) * tbytes
@@ -477,8 +491,8 @@ def run_gpu(args, rank, ws, local, dist):
                              "achieved": prod_ach, "peak": hbm, "unit": "GB/s", "frac": prod_ach / hbm,
                              "peak_source": how},
         "phases_ms_per_step": {k: v[0] / args.steps for k, v in prof.items()},
-        "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "ms_per_step": e2e_s * 1e3},
+        "e2e": ({"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                 "ms_per_step": e2e_s * 1e3} if e2e_s else None),
         "gpu_launches": launches,
         "clocks": clk,
         "diag": diag,
@@ -586,7 +600,8 @@ def run_screen(args):
         d = {k: st1[k] - st0[k] for k in st1}
         return {"threshold": thr, "seconds": tb - ta, "gsaes_energy": float(en[0]), "energy": fe,
                 "kept_group_fraction": d["kept_groups"] / d["groups"] if d["groups"] else 1.0,
-                "products": d["products"], "kept_terms": d["kept_terms"]}
+                "skipped_term_fraction": 1.0 - d["kept_terms"] / d["all_terms"] if d["all_terms"] else 0.0,
+                "products": d["products"], "kept_terms": d["kept_terms"], "all_double_terms": d["all_terms"]}
 
     lanczos(None)  # warm-up (scratch allocation)
     plain = lanczos(None)
@@ -596,8 +611,6 @@ def run_screen(args):
     for thr in args.screen_thresholds:
         r = lanczos(thr)
         r["dE"] = r["energy"] - plain["energy"]
-        # skipped fraction of the doubles' terms, over the screened products
-        r["skipped_term_fraction"] = None
         runs.append(r)
         if abs(r["dE"]) <= args.screen_tol and (best is None or r["seconds"] < best["seconds"]):
             best = r
@@ -612,6 +625,33 @@ def run_screen(args):
     res["speedup_vs_plain"] = plain["seconds"] / best["seconds"] if best else 1.0
     res["fallback"] = best is None
     res["connected_per_det"] = C
+    print(json.dumps(res), flush=True)
+
+
+def run_lanczos(args):
+    """The whole truncated Lanczos ground-state solve of the configs' system
+    (sparse_krylov_solve_eigenval as the sfci binary runs it, from |HF>):
+    wall time, products, time per Krylov iteration and the energies."""
+    import sfci_gb300 as sg
+    sg.load_library()
+    sysd = SYSTEMS[args.config]
+    path = workload_in(sysd)
+    M, NE = sysd["M"], sysd["ne"]
+    ctx = sg.Context(path, 2 * M, NE, Nd=args.nd, hpsi_cap=HPSI_CAP)
+    v = ctx.vec(args.nd)
+    v.upload(hf_key(sysd), np.array([1.0]))
+    l0 = ctx.launches()
+    t0 = time.perf_counter()
+    en, fe = ctx.sparse_krylov_solve_eigenval(v, args.lanczos_nl, args.lanczos_restarts)
+    t = time.perf_counter() - t0
+    done = int(np.sum(~np.isnan(en)))
+    products = done * args.lanczos_nl
+    res = {"metric": METRIC, "mode": "truncated Lanczos solve", "unit": "s",
+           "config": {"workload": "sparse_krylov_solve_eigenval from |HF>, " + sysd["text"], "num_orb": 2 * M,
+                      "num_e": NE, "Nd": args.nd, "Nl": args.lanczos_nl, "num_restart": args.lanczos_restarts},
+           "value": t, "higher_is_better": False, "restarts_run": done, "products": products,
+           "s_per_krylov_iteration": t / max(products, 1), "energies": [float(x) for x in en[~np.isnan(en)]],
+           "final_energy": fe, "gpu_launches": ctx.launches() - l0, "dtype": "f64", "data": "synthetic"}
     print(json.dumps(res), flush=True)
 
 
@@ -773,6 +813,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-step-s", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end (host buffer) leg")
     ap.add_argument("--cut", type=float, default=1e-5,
                     help="post-merge cut of the timed product (profiling: a smaller cut gives more survivors)")
     ap.add_argument("--out-cap", type=int, default=0,
@@ -786,12 +827,12 @@ def main():
     ap.add_argument("--screen-nd", type=int, default=200000)
     ap.add_argument("--screen-nl", type=int, default=8)
     ap.add_argument("--screen-log-nd", type=int, default=1800)
-    ap.add_argument("--screen-steps", type=int, default=4000)
+    ap.add_argument("--screen-steps", type=int, default=3000)
     ap.add_argument("--screen-lr", type=float, default=1e-3)
     ap.add_argument("--screen-seed", type=int, default=5)
     ap.add_argument("--screen-tol", type=float, default=1e-5)
     ap.add_argument("--screen-min-term", type=float, default=1e-8)
-    ap.add_argument("--screen-thresholds", type=float, nargs="+", default=[0.02, 0.05, 0.1, 0.2, 0.35])
+    ap.add_argument("--screen-thresholds", type=float, nargs="+", default=[0.002, 0.005, 0.01, 0.02, 0.05])
     ap.add_argument("--batch", action="store_true",
                     help="batched bond-stretch curve: 32 instances, batched vs unbatched Lanczos")
     ap.add_argument("--batch-scale", type=float, default=0.01,
@@ -800,7 +841,13 @@ def main():
     ap.add_argument("--mlp", action="store_true", help="throughput of the screen's tensor-core MLP kernels")
     ap.add_argument("--mlp-sources", type=int, default=20000)
     ap.add_argument("--mlp-batch-tiles", type=int, default=128)
+    ap.add_argument("--lanczos", action="store_true", help="the whole truncated Lanczos solve (time per iteration)")
+    ap.add_argument("--lanczos-nl", type=int, default=30)
+    ap.add_argument("--lanczos-restarts", type=int, default=4)
     args = ap.parse_args()
+    if args.lanczos:
+        run_lanczos(args)
+        return
     if args.mlp:
         run_mlp(args)
         return

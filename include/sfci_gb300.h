@@ -304,8 +304,9 @@ int sfci_screen_params(sfci_screen* s, float* get, const float* set, uint64_t n)
 int sfci_screen_grads(sfci_screen* s, float* get, uint64_t n);
 /* Attach (s non-null) or detach the screen of the context's products. */
 int sfci_ctx_set_screen(sfci_ctx* ctx, sfci_screen* s, double threshold);
-/* groups seen, groups kept, terms kept, screened products since the context was made */
-int sfci_ctx_screen_stats(const sfci_ctx* ctx, uint64_t* out4);
+/* groups seen, groups kept, terms kept, screened products, terms of all groups,
+ * since the context was made (five counters) */
+int sfci_ctx_screen_stats(const sfci_ctx* ctx, uint64_t* out5);
 
 /* Generalised symmetric eigensolve K c = E S c (Eigen GSAES as used at
  * src/sparse_solver.cpp:450), FP64 on the host: eigenvalues ascending,

@@ -469,9 +469,9 @@ class Context:
         self._screen = screen
 
     def screen_stats(self) -> dict:
-        a = (C.c_uint64 * 4)()
+        a = (C.c_uint64 * 5)()
         _check(self.L.sfci_ctx_screen_stats(self.h, a))
-        return dict(zip(["groups", "kept_groups", "kept_terms", "products"], [int(x) for x in a]))
+        return dict(zip(["groups", "kept_groups", "kept_terms", "products", "all_terms"], [int(x) for x in a]))
 
 
 class Screen:

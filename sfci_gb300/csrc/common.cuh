@@ -316,6 +316,35 @@ SFCI_HD double fx_to_double(u64 lo, u64 hi) {
   return bits_dbl((neg << 63) | ((u64)(top - FX_FRAC + 1023) << 52) | (mant & 0xfffffffffffffull));
 }
 
+// x * 2^FX_FRAC rounded to the nearest integer (ties to even), as a 128-bit
+// two's-complement (h:l); sets *bad for |x| >= 2^62 or not finite (then 0).
+// The wide form for sums with more terms than the split accumulators take.
+SFCI_HD void fx128_of(double x, u64& l, u64& h, unsigned& bad) {
+  const u64 b = dbl_bits(x);
+  const int e = (int)((b >> 52) & 0x7ff);
+  const u64 m = (b & 0xfffffffffffffull) | (1ull << 52);
+  const int s = e - (1075 - FX_FRAC);  // F = m * 2^s
+  l = 0;
+  h = 0;
+  if (e >= 1023 + 62) {
+    bad = 1u;
+    return;
+  }
+  if (e == 0 || s < -53) return;
+  if (s < 0) {
+    l = shr_round(m, -s);
+  } else if (s < 64) {
+    l = m << s;
+    h = s ? (m >> (64 - s)) : 0ull;
+  } else {
+    h = m << (s - 64);
+  }
+  if (b >> 63) {
+    h = ~h + (l == 0 ? 1ull : 0ull);
+    l = 0ull - l;
+  }
+}
+
 // an accumulator's value as a double
 SFCI_HD double fx_acc_double(u64 acc_lo, u64 acc_hi) {
   u64 L, H;

@@ -81,7 +81,7 @@ struct Ctx {
   // screens created on this context (freed with it; their handles become orphans)
   std::set<struct Screen*> screens;
   double screen_thr = 0.5;
-  uint64_t screen_stats[4] = {};  // groups, kept groups, kept terms, screened products
+  uint64_t screen_stats[5] = {};  // groups, kept groups, kept terms, screened products, terms of all groups
 };
 
 struct Vec {

@@ -249,6 +249,7 @@ struct FwdArgs {
   uint32_t* keep;         // one bit per example
   u64* kept_terms;        // per source
   u64* kept_groups;       // per source
+  u64* all_terms;         // nullable: terms of every group (one counter)
   float* prob;            // nullable: per example
   // training
   const uint32_t* labels;
@@ -327,7 +328,9 @@ __global__ void __launch_bounds__(THREADS, 1) k_mlp_fwd(FwdArgs a) {
     Feat f{};
     KT key{};
     if (valid) {
-      j = source_of(a.x, e);
+      // sources are in example order: walk forward from the tile's first one
+      j = s_src[0];
+      while (j + 1 < a.x.nsrc && __ldg(a.x.goff + j + 1) <= e) ++j;
       key = load_key<KT>(a.x.keys, j);
       f = example_feat(a.x, key, a.x.cc[j], (unsigned)(e - a.x.goff[j]) + 1u, j);
     }
@@ -398,6 +401,10 @@ __global__ void __launch_bounds__(THREADS, 1) k_mlp_fwd(FwdArgs a) {
       const u64 jj = valid ? j : ~0ull;
       const unsigned same = __match_any_sync(0xffffffffu, jj);
       const unsigned nt = kept ? f.gsize : 0u, ng = kept ? 1u : 0u;
+      if (a.all_terms) {
+        const unsigned at = warp_sum(valid ? f.gsize : 0u);
+        if (lane == 0 && at) atomicAdd(a.all_terms, (u64)at);
+      }
       if (same == 0xffffffffu) {
         const unsigned st = warp_sum(nt), sg = warp_sum(ng);
         if (lane == 0 && valid && st) {
@@ -877,10 +884,11 @@ static int screen_infer(Ctx& c, Screen& s, const u64* keys, const double* amps, 
   if ((st = read_words(c, goff + n, sizeof(u64), &nex))) return st;
   const unsigned ntiles = (unsigned)((nex + TILE - 1) / TILE);
   uint32_t* keep = (uint32_t*)scratch_get(c, "sc_keep", ((size_t)ntiles * TILE / 32 + 1) * sizeof(uint32_t));
-  u64* kt = (u64*)scratch_get(c, "sc_kterms", 2 * (n + 1) * sizeof(u64));
+  u64* kt = (u64*)scratch_get(c, "sc_kterms", (2 * (n + 1) + 1) * sizeof(u64));
   if (!keep || !kt) return SFCI_ERR_NOMEM;
   u64* kg = kt + (n + 1);
-  SFCI_CUDA(cudaMemsetAsync(kt, 0, 2 * (n + 1) * sizeof(u64), c.stream));
+  u64* allt = kg + (n + 1);
+  SFCI_CUDA(cudaMemsetAsync(kt, 0, (2 * (n + 1) + 1) * sizeof(u64), c.stream));
   FwdArgs a{};
   a.x = ex_view(c, s, keys, amps, goff, n, nex);
   a.W1b = s.W1b;
@@ -891,6 +899,7 @@ static int screen_infer(Ctx& c, Screen& s, const u64* keys, const double* amps, 
   a.keep = keep;
   a.kept_terms = kt;
   a.kept_groups = kg;
+  a.all_terms = allt;
   a.prob = prob;
   a.err = s.err;
   if (ntiles) {
@@ -997,10 +1006,13 @@ int screen_select(Ctx& c, const void* keys, const double* amps, u64 n, ScreenLis
   out->groups = nex;
   out->kept_groups = nk;
   out->kept_terms_total = tk;
+  u64 all = 0;
+  if ((st = read_words(c, kg + (n + 1), sizeof(u64), &all))) return st;
   c.screen_stats[0] += nex;
   c.screen_stats[1] += nk;
   c.screen_stats[2] += tk;
   c.screen_stats[3] += 1;
+  c.screen_stats[4] += all;
   return SFCI_OK;
 }
 
@@ -1386,8 +1398,8 @@ extern "C" int sfci_ctx_set_screen(sfci_ctx* ctx, sfci_screen* x, double thresho
   return SFCI_OK;
 }
 
-extern "C" int sfci_ctx_screen_stats(const sfci_ctx* ctx, uint64_t* out4) {
-  if (!ctx || !out4) return set_error(SFCI_ERR_ARG, "sfci_ctx_screen_stats: null argument");
-  for (int i = 0; i < 4; ++i) out4[i] = ctx->c.screen_stats[i];
+extern "C" int sfci_ctx_screen_stats(const sfci_ctx* ctx, uint64_t* out5) {
+  if (!ctx || !out5) return set_error(SFCI_ERR_ARG, "sfci_ctx_screen_stats: null argument");
+  for (int i = 0; i < 5; ++i) out5[i] = ctx->c.screen_stats[i];
   return SFCI_OK;
 }

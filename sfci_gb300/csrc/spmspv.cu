@@ -54,6 +54,7 @@ constexpr int LC_SLOTS = 4096;
 constexpr unsigned LW_PROBE = 32;                 // probes before a warp table counts as overflowed
 constexpr unsigned LC_PROBE = 128;                // same for the second tier
 constexpr int B_MAX = 30;
+constexpr double LEAF_TERMS = 1024.0;                 // terms a leaf is sized for (at most, on average)
 
 enum { M_COUNT = 0, M_SCATTER = 1, M_ENERGY = 2, M_PROJECT = 3, M_LABEL = 4 };
 constexpr int PROJ_MAX = 64;  // vectors of one projection sweep
@@ -147,6 +148,18 @@ static FxCut fx_cut(double cut) {
     c.below_hi = (u64)(t >> 64);
   }
   return c;
+}
+
+// add x exactly to a 128-bit fixed-point accumulator acc[0..1] (low, high):
+// the carry of each low-word addition is known from its returned old value, so
+// the total is the exact sum whatever the order of the additions
+__device__ __forceinline__ void fx_atomic_add128(u64* acc, double x, unsigned& bad) {
+  u64 l, h;
+  fx128_of(x, l, h, bad);
+  if ((l | h) == 0) return;
+  const u64 old = atomicAdd((unsigned long long*)acc, (unsigned long long)l);
+  const u64 hh = h + ((old + l < old) ? 1ull : 0ull);
+  if (hh) atomicAdd((unsigned long long*)(acc + 1), (unsigned long long)hh);
 }
 
 // add a term's two addends to an accumulator (results unused: reductions)
@@ -766,13 +779,13 @@ struct LeafArgs {
   KT* skeys;
   double* samps;
   u64* scount;
-  double* dpart;       // per-CTA <v|Hv> partials (accumulated across launches)
+  u64* dexact;         // <v|Hv>: exact 128-bit fixed-point sum (low, high)
   double* qpart;       // nullable: per-CTA sums of squared merged amplitudes (before the cut)
   unsigned* ovf;       // [0] = count, then leaf ids (global)
   unsigned ovf_cap;
   u64* uniq;           // merged distinct determinants (statistics)
   unsigned* bad;       // set when a term is outside the fixed-point range
-  double* dinst;       // nullable: <v|Hv> per instance of a batched context
+  u64* dinst;          // nullable: <v|Hv> per instance of a batched context, exact, 2 words each
 };
 
 // Shared-memory layout of a merge table with `n` slots: keys, then the low and
@@ -816,11 +829,12 @@ __global__ void __launch_bounds__(LW_WARPS * 32, sizeof(KT) == 8 ? 4 : 3) k_leaf
   extern __shared__ __align__(16) unsigned char smem[];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   WTable<KT> t(smem + (sizeof(KT) + WSLOT_BYTES_EXTRA) * TW_MAX * warp, TW_MAX);
-  __shared__ double s_red[LW_WARPS], s_rq[LW_WARPS];
+  __shared__ double s_rq[LW_WARPS];
   __shared__ u64 s_uq[LW_WARPS];
   const KT empty = key_empty<KT>();
   const unsigned lt = (1u << lane) - 1u;
-  double dacc = 0.0, qacc = 0.0;
+  double qacc = 0.0;
+  unsigned dbad = 0;
   u64 uq = 0;
   for (u64 leaf = (u64)blockIdx.x * LW_WARPS + warp; leaf < a.nleaves; leaf += (u64)gridDim.x * LW_WARPS) {
     const u64 beg = a.loff[leaf], end = a.loff[leaf + 1], n = end - beg;
@@ -885,8 +899,8 @@ __global__ void __launch_bounds__(LW_WARPS * 32, sizeof(KT) == 8 ? 4 : 3) k_leaf
       int s = table_find(t.k, tb - 1, k, leaf_slot(k, tbits));
       if (s >= 0) {
         const double x = t.amp(s) * a.in_amps[e];
-        dacc += x;
-        if (a.dinst) atomicAdd(a.dinst + inst_of(k), x);
+        fx_atomic_add128(a.dexact, x, dbad);
+        if (a.dinst) fx_atomic_add128(a.dinst + 2 * inst_of(k), x, dbad);
       }
     }
     for (unsigned base = 0; base < tb; base += 32) {
@@ -916,23 +930,20 @@ __global__ void __launch_bounds__(LW_WARPS * 32, sizeof(KT) == 8 ? 4 : 3) k_leaf
     }
     __syncwarp();
   }
-  double v = warp_sum(dacc);
+  if (dbad) atomicOr(a.bad, 1u);
   const double vq = warp_sum(qacc);
   if (lane == 0) {
-    s_red[warp] = v;
     s_rq[warp] = vq;
     s_uq[warp] = uq;
   }
   __syncthreads();
   if (tid == 0) {
-    double s = 0.0, sq = 0.0;
+    double sq = 0.0;
     u64 q = 0;
     for (int w = 0; w < LW_WARPS; ++w) {
-      s += s_red[w];
       sq += s_rq[w];
       q += s_uq[w];
     }
-    atomicAdd(a.dpart + blockIdx.x, s);  // one adder per slot and launch: the order stays fixed
     if (a.qpart) atomicAdd(a.qpart + blockIdx.x, sq);
     if (q) atomicAdd(a.uniq, q);
   }
@@ -949,11 +960,11 @@ __global__ void __launch_bounds__(LC_THREADS) k_leafc(LeafArgs<KT> a, const unsi
   STable<KT> t(smem, LC_SLOTS);
   __shared__ unsigned s_nuniq, s_ovf;  // s_nuniq: claimed slots, counted after the inserts
   __shared__ u64 s_sum[LC_THREADS / 32 + 1];
-  __shared__ double s_red[LC_THREADS / 32], s_rq[LC_THREADS / 32];
+  __shared__ double s_rq[LC_THREADS / 32];
   __shared__ u64 s_base;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const KT empty = key_empty<KT>();
-  double dacc = 0.0, qacc = 0.0;
+  double qacc = 0.0;
   u64 uq = 0;
   unsigned bad = 0;
   for (unsigned q = blockIdx.x; q < nids; q += gridDim.x) {
@@ -1014,8 +1025,8 @@ __global__ void __launch_bounds__(LC_THREADS) k_leafc(LeafArgs<KT> a, const unsi
       int s = table_find(t.k, LC_SLOTS - 1, k, (unsigned)slot_hash(k) & (LC_SLOTS - 1));
       if (s >= 0) {
         const double x = t.amp(s) * a.in_amps[e];
-        dacc += x;
-        if (a.dinst) atomicAdd(a.dinst + inst_of(k), x);
+        fx_atomic_add128(a.dexact, x, bad);
+        if (a.dinst) fx_atomic_add128(a.dinst + 2 * inst_of(k), x, bad);
       }
     }
     constexpr int PER = LC_SLOTS / LC_THREADS;
@@ -1055,20 +1066,12 @@ __global__ void __launch_bounds__(LC_THREADS) k_leafc(LeafArgs<KT> a, const unsi
     __syncthreads();
   }
   if (bad) atomicOr(a.bad, 1u);
-  double v = warp_sum(dacc);
   const double vq = warp_sum(qacc);
-  if (lane == 0) {
-    s_red[warp] = v;
-    s_rq[warp] = vq;
-  }
+  if (lane == 0) s_rq[warp] = vq;
   __syncthreads();
   if (tid == 0) {
-    double s = 0.0, sq = 0.0;
-    for (int w = 0; w < LC_THREADS / 32; ++w) {
-      s += s_red[w];
-      sq += s_rq[w];
-    }
-    atomicAdd(a.dpart + blockIdx.x, s);
+    double sq = 0.0;
+    for (int w = 0; w < LC_THREADS / 32; ++w) sq += s_rq[w];
     if (a.qpart) atomicAdd(a.qpart + blockIdx.x, sq);
     if (uq) atomicAdd(a.uniq, uq);
   }
@@ -1092,25 +1095,26 @@ __global__ void k_big_insert(const KT* __restrict__ keys, const double* __restri
 template <class KT>
 __global__ void k_big_finish(const KT* tk, const u64* tl, const u64* th, unsigned mask, const KT* in_keys,
                              const double* in_amps, u64 ib, u64 ie, FxCut cut, KT* skeys, double* samps,
-                             u64* scount, double* dsum, u64* uniq, double* qsum, double* dinst) {
+                             u64* scount, u64* dexact, u64* uniq, double* qsum, u64* dinst, unsigned* bad) {
   const KT empty = key_empty<KT>();
   u64 gt = (u64)blockIdx.x * blockDim.x + threadIdx.x, gs = (u64)gridDim.x * blockDim.x;
-  double acc = 0.0, qacc = 0.0;
+  double qacc = 0.0;
+  unsigned dbad = 0;
   for (u64 e = ib + gt; e < ie; e += gs) {
     int s = table_find_global(tk, mask, in_keys[e]);
     if (s >= 0) {
-      const double x = fx_to_double(__ldcg(tl + s), __ldcg(th + s)) * in_amps[e];
-      acc += x;
-      if (dinst) atomicAdd(dinst + inst_of(in_keys[e]), x);
+      const double x = fx_acc_double(__ldcg(tl + s), __ldcg(th + s)) * in_amps[e];
+      fx_atomic_add128(dexact, x, dbad);
+      if (dinst) fx_atomic_add128(dinst + 2 * inst_of(in_keys[e]), x, dbad);
     }
   }
-  if (acc != 0.0) atomicAdd(dsum, acc);
+  if (dbad) atomicOr(bad, 1u);
   for (u64 s = gt; s <= mask; s += gs) {
     KT k = ldcg_key(tk + s);
     if (key_eq(k, empty)) continue;
     atomicAdd(uniq, 1ull);
     if (qsum) {
-      const double x = fx_to_double(__ldcg(tl + s), __ldcg(th + s));
+      const double x = fx_acc_double(__ldcg(tl + s), __ldcg(th + s));
       qacc += x * x;
     }
     double v = 0.0;
@@ -1556,10 +1560,12 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
       leaf_resident = std::min<unsigned>(leafgrid, (unsigned)per_sm * c.sm_count);
     cudaGetLastError();
   }
-  double* dpart = (double*)scratch_get(c, "sp_dpart", (leafgrid + 1) * sizeof(double));
-  if (!scount || !dpart) return SFCI_ERR_NOMEM;
+  // <v|Hv>: exact 128-bit fixed-point sums, the total and one per instance, so
+  // its value does not depend on the plan, the launch order or the batching
+  u64* dexact = (u64*)scratch_get(c, "sp_dexact", (2 + 2 * INST_MAX) * sizeof(u64));
+  if (!scount || !dexact) return SFCI_ERR_NOMEM;
   SFCI_CUDA(cudaMemsetAsync(scount, 0, 4 * sizeof(u64), c.stream));
-  SFCI_CUDA(cudaMemsetAsync(dpart, 0, (leafgrid + 1) * sizeof(double), c.stream));
+  SFCI_CUDA(cudaMemsetAsync(dexact, 0, (2 + 2 * INST_MAX) * sizeof(u64), c.stream));
   // optional sum of squared merged amplitudes: per-CTA partials, then the global tier's sum
   double* qpart = nullptr;
   if (ex && ex->sumsq) {
@@ -1571,16 +1577,7 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
   u64 scount_h = 0, big_leaves = 0, T_gen = 0;
   KT* sk = nullptr;    // survivors of every outer pass (kept across them: the buffers do not
   double* sa = nullptr;  // change size between class passes)
-  double dbig_h = 0.0;
-  double* dbig = (double*)scratch_get(c, "sp_dbig", sizeof(double));
-  if (!dbig) return SFCI_ERR_NOMEM;
-  SFCI_CUDA(cudaMemsetAsync(dbig, 0, sizeof(double), c.stream));
-  double* dinst = nullptr;  // batched contexts: <v|Hv> per instance
-  if (c.ninst) {
-    dinst = (double*)scratch_get(c, "sp_dinst", INST_MAX * sizeof(double));
-    if (!dinst) return SFCI_ERR_NOMEM;
-    SFCI_CUDA(cudaMemsetAsync(dinst, 0, INST_MAX * sizeof(double), c.stream));
-  }
+  u64* dinst = c.ninst ? dexact + 2 : nullptr;  // batched contexts: <v|Hv> per instance
   const size_t lsm = (sizeof(KT) + WSLOT_BYTES_EXTRA) * TW_MAX * LW_WARPS;
   std::vector<u64> segs, nsegs_h;
   std::vector<Unit> units;
@@ -1607,7 +1604,12 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
     // leaf.  The distinct count is estimated from the duplication (terms per
     // distinct key) of the previous product on this context (default 8).
     const double uniq_est = std::max(1.0, (double)opass.terms / std::max(1.0, dup));
-    const int b = std::max(1, std::min(B_MAX, (int)std::ceil(std::log2(std::max(2.0, uniq_est / leaf_uniq)))));
+    // at most LEAF_TERMS terms a leaf as well: with many terms per key (hot
+    // determinants) a leaf sized by distinct keys alone outgrows the warp
+    // tier's FX32_MAX_TERMS
+    const int b_terms = (int)std::ceil(std::log2(std::max(2.0, (double)opass.terms / LEAF_TERMS)));
+    const int b = std::max(1, std::min(B_MAX, std::max(b_terms,
+                                                       (int)std::ceil(std::log2(std::max(2.0, uniq_est / leaf_uniq))))));
     const int d0 = std::min(b, l1_bits);
     const int rem = b - d0;
     const int nlev = rem ? (rem + digit_bits - 1) / digit_bits : 0;
@@ -1840,7 +1842,7 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
         la.skeys = sk;
         la.samps = sa;
         la.scount = scount;
-        la.dpart = dpart;
+        la.dexact = dexact;
         la.qpart = qpart;
         // overflow lists of the two table tiers: every leaf of the group can
         // overflow a tier at most once (the leaf count comes from the previous
@@ -1895,7 +1897,8 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
             gr = (unsigned)std::min<u64>((tsz + 255) / 256, (u64)c.sm_count * 8);
             SFCI_LAUNCH(c, k_big_finish<KT>, gr, 256, 0, (const KT*)bk, (const u64*)ba, (const u64*)(ba + tsz),
                         (unsigned)(tsz - 1), (const KT*)ink, (const double*)ina, (u64)ib_ie[0], (u64)ib_ie[1],
-                        la.cut, sk, sa, scount, dbig, scount + 1, qpart ? qpart + leafgrid + 1 : nullptr, la.dinst);
+                        la.cut, sk, sa, scount, dexact, scount + 1, qpart ? qpart + leafgrid + 1 : nullptr, la.dinst,
+                        la.bad);
           }
         }
         if ((st = read_words(c, scount, sizeof(u64), &scount_h))) return st;
@@ -1908,10 +1911,9 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
   c.stats[1] = T_gen;
   // 7. <v|Hv> and final selection + key sort
   tok = phase_begin(c, PH_OTHER);
-  SFCI_LAUNCH(c, k_sum_parts, 1, 32, 0, (const double*)dpart, (int)leafgrid, dpart + leafgrid);
-  double dl = 0.0;
-  if ((st = read_words(c, dpart + leafgrid, sizeof(double), &dl))) return st;
-  if ((st = read_words(c, dbig, sizeof(double), &dbig_h))) return st;
+  std::vector<u64> dx(2 + 2 * INST_MAX);
+  if ((st = read_words(c, dexact, dx.size() * sizeof(u64), dx.data()))) return st;
+  const double dl = fx_to_double(dx[0], dx[1]);
   u64 fxbad = 0;
   if ((st = read_words(c, scount + 2, sizeof(u64), &fxbad))) return st;
   phase_end(c, tok);
@@ -1940,10 +1942,10 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
     c.stats[2] = uq;
     if (uq) c.dup_est = (double)T_gen / (double)uq;
   }
-  *diag = dl + dbig_h;
+  *diag = dl;
   if (dinst) {
     c.inst_diag.assign(INST_MAX, 0.0);
-    if ((st = read_words(c, dinst, INST_MAX * sizeof(double), c.inst_diag.data()))) return st;
+    for (int i = 0; i < INST_MAX; ++i) c.inst_diag[i] = fx_to_double(dx[2 + 2 * i], dx[3 + 2 * i]);
   }
   if (qpart) {
     SFCI_LAUNCH(c, k_sum_parts, 1, 32, 0, (const double*)qpart, (int)leafgrid, qpart + leafgrid);

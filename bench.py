@@ -358,6 +358,8 @@ def run_gpu(args, rank, ws, local, dist):
     M, NE, W = sysd["M"], sysd["ne"], key_words(sysd)
     in_k, in_a = input_on_gpu(sg, path, sysd, nd)
     ctx = sg.Context(path, 2 * M, NE, Nd=nd, hpsi_cap=HPSI_CAP, mem_budget=args.mem_budget, coeff_cut=args.cut)
+    if args.class_passes is not None:
+        ctx.set_class_passes(args.class_passes)
     vin = ctx.vec_from(in_k, in_a, cap=nd)
     n_in = vin.len
     out = ctx.vec(args.out_cap or HPSI_CAP)
@@ -372,11 +374,18 @@ def run_gpu(args, rank, ws, local, dist):
     clocks.start()
     barrier(dist)
     l0 = ctx.launches()
+    if args.profile_region:  # an ncu run with --profile-from-start off captures the timed steps only
+        import torch
+        torch.cuda.synchronize()
+        torch.cuda.cudart().cudaProfilerStart()
     ctx.event_record(0)
     t0 = time.perf_counter()
     for _ in range(args.steps):
         diag = ctx.SpMVMtply_bucket(vin, out, 0.0, 1.0)
     ctx.event_record(1)
+    if args.profile_region:
+        torch.cuda.synchronize()
+        torch.cuda.cudart().cudaProfilerStop()
     ms = ctx.event_elapsed(0, 1) / args.steps
     wall = (time.perf_counter() - t0) / args.steps
     launches = ctx.launches() - l0
@@ -510,15 +519,15 @@ def _finish_gpu(args, rank, ws, dist, ctx, sysd, path, nd, M, NE, W, n_in, C, T_
 # learned excitation screen: train on logged labels, then plain vs screened
 # ---------------------------------------------------------------------------
 
-def _krylov_input(sg, ctx, sysd, nd):
+def _krylov_input(sg, ctx, sysd, nd, cap=HPSI_CAP):
     """top-nd of H (H|HF>) with the product's own cut, normalised (the sources a
     Lanczos step would multiply)."""
     hf = ctx.vec(1)
     hf.upload(hf_key(sysd), np.array([1.0]))
-    v1 = ctx.vec(HPSI_CAP)
+    v1 = ctx.vec(cap)
     ctx.SpMVMtply_bucket(hf, v1, 0.0, 1.0)
     v1.normalize()
-    w = ctx.vec(HPSI_CAP)
+    w = ctx.vec(cap)
     ctx.SpMVMtply_bucket(v1, w, 0.0, 1.0)
     v2 = ctx.vec(nd)
     v2.shrinkFrom(w)
@@ -587,8 +596,8 @@ def run_screen(args):
     scr_e.set_params(params)
     runs = []
 
-    def lanczos(thr):
-        ev.set_screen(None if thr is None else scr_e, 0.0 if thr is None else thr)
+    def lanczos(thr, guard=0.0):
+        ev.set_screen(None if thr is None else scr_e, 0.0 if thr is None else thr, guard)
         st0 = ev.screen_stats()
         v = ev.vec(args.screen_nd)
         v.upload(hf_key(sysd), np.array([1.0]))
@@ -598,7 +607,7 @@ def run_screen(args):
         tb = time.perf_counter()
         st1 = ev.screen_stats()
         d = {k: st1[k] - st0[k] for k in st1}
-        return {"threshold": thr, "seconds": tb - ta, "gsaes_energy": float(en[0]), "energy": fe,
+        return {"threshold": thr, "guard": guard, "seconds": tb - ta, "gsaes_energy": float(en[0]), "energy": fe,
                 "kept_group_fraction": d["kept_groups"] / d["groups"] if d["groups"] else 1.0,
                 "skipped_term_fraction": 1.0 - d["kept_terms"] / d["all_terms"] if d["all_terms"] else 0.0,
                 "products": d["products"], "kept_terms": d["kept_terms"], "all_double_terms": d["all_terms"]}
@@ -608,8 +617,9 @@ def run_screen(args):
     C = connected_per_det(M, NE // 2, NE // 2)
     runs.append(plain)
     best = None
-    for thr in args.screen_thresholds:
-        r = lanczos(thr)
+    for thr, guard in [(t, 0.0) for t in args.screen_thresholds] + \
+            [(args.screen_thresholds[0], gd) for gd in args.screen_guards]:
+        r = lanczos(thr, guard)
         r["dE"] = r["energy"] - plain["energy"]
         runs.append(r)
         if abs(r["dE"]) <= args.screen_tol and (best is None or r["seconds"] < best["seconds"]):
@@ -667,10 +677,11 @@ def run_mlp(args):
     sysd = SYSTEMS[1]
     path = workload_in(sysd)
     M, NE = sysd["M"], sysd["ne"]
-    ctx = sg.Context(path, 2 * M, NE, Nd=args.mlp_sources, hpsi_cap=HPSI_CAP)
-    vin = _krylov_input(sg, ctx, sysd, args.mlp_sources)
+    cap = args.out_cap or HPSI_CAP
+    ctx = sg.Context(path, 2 * M, NE, Nd=args.mlp_sources, hpsi_cap=cap, mem_budget=args.mem_budget)
+    vin = _krylov_input(sg, ctx, sysd, args.mlp_sources, cap)
     scr = sg.Screen(ctx, seed=3)
-    out = ctx.vec(HPSI_CAP)
+    out = ctx.vec(cap)
     ctx.SpMVMtply_bucket(vin, out, 0.0, 1.0)
     ne, npos = scr.log(vin, out)
     scr.predict(vin, 0.5)  # warm-up
@@ -730,8 +741,8 @@ def run_batch(args):
     Nl, R = args.batch_nl, 1
     orbs = [x["num_orb"] for x in curve]
     nes = [x["num_e"] for x in curve]
-    cap = int(sum(x["Nd"] for x in curve) * 200)
-    bc = sg.Context.batch(paths, orbs, nes, Nd=10 ** 9, hpsi_cap=min(cap, 400000000))
+    # hpsi_cap is per instance in the batched driver: the same cap as the unbatched runs
+    bc = sg.Context.batch(paths, orbs, nes, Nd=10 ** 9, hpsi_cap=HPSI_CAP)
     # autotune on the largest instance's two-step vector, in the batched context
     big = len(curve) - 1
     hf = bc.vec(1)
@@ -759,24 +770,32 @@ def run_batch(args):
     bc.batch_lanczos(start_vectors(bc, True), 2, 1)  # warm-up: scratch allocation
     vs = start_vectors(bc, True)
     l0 = bc.launches()
+    bc.profile(True)
+    bc.profile_reset()
     tb0 = time.perf_counter()
     en_b, fe_b = bc.batch_lanczos(vs, Nl, R)
     t_batched = time.perf_counter() - tb0
+    prof_b = {k: v[0] for k, v in bc.profile_read().items()}
+    bc.profile(False)
     launches_b = bc.launches() - l0
     plan_b = bc.tuning()
     bc.trim()
     # unbatched: every instance in its own context, one after another
     en_u, fe_u, t_un = [], [], 0.0
     launches_u = 0
+    prof_u = {}
     for k, inst in enumerate(curve):
         c = sg.Context(paths[k], inst["num_orb"], inst["num_e"], Nd=inst["Nd"], hpsi_cap=HPSI_CAP)
         c.set_tuning(**plan_b)
         v = c.vec(inst["Nd"])
         v.upload(sg.keys_from_ints([(1 << inst["num_e"]) - 1], c.words), np.array([1.0]))
         l0 = c.launches()
+        c.profile(True)
         ta = time.perf_counter()
         e, f = c.sparse_krylov_solve_eigenval(v, Nl, R)
         t_un += time.perf_counter() - ta
+        for kk, vv in c.profile_read().items():
+            prof_u[kk] = prof_u.get(kk, 0.0) + vv[0]
         launches_u += c.launches() - l0
         en_u.append(e)
         fe_u.append(f)
@@ -796,6 +815,7 @@ def run_batch(args):
            "max_dE_vs_unbatched": max(dE), "max_dE_gsaes": max(dG),
            "batched_seconds": t_batched, "unbatched_seconds": t_un, "speedup": t_un / t_batched,
            "gpu_launches": {"batched": launches_b, "unbatched": launches_u},
+           "product_phase_ms": {"batched": prof_b, "unbatched": prof_u},
            "autotune": {"plan": plan_b, "ms": plan_ms}, "files_seconds": t_files}
     print(json.dumps(res), flush=True)
 
@@ -814,6 +834,10 @@ def main():
     ap.add_argument("--ref-step-s", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end (host buffer) leg")
+    ap.add_argument("--class-passes", type=int, default=None, choices=[-1, 0, 1],
+                    help="generation passes by target alpha class: 0 when needed (default), 1 always, -1 never")
+    ap.add_argument("--profile-region", action="store_true",
+                    help="bracket the timed steps with cudaProfilerStart/Stop (for ncu --profile-from-start off)")
     ap.add_argument("--cut", type=float, default=1e-5,
                     help="post-merge cut of the timed product (profiling: a smaller cut gives more survivors)")
     ap.add_argument("--out-cap", type=int, default=0,
@@ -832,7 +856,9 @@ def main():
     ap.add_argument("--screen-seed", type=int, default=5)
     ap.add_argument("--screen-tol", type=float, default=1e-5)
     ap.add_argument("--screen-min-term", type=float, default=1e-8)
-    ap.add_argument("--screen-thresholds", type=float, nargs="+", default=[0.002, 0.005, 0.01, 0.02, 0.05])
+    ap.add_argument("--screen-thresholds", type=float, nargs="+", default=[0.01, 0.05])
+    ap.add_argument("--screen-guards", type=float, nargs="*", default=[1e-5, 1e-6, 1e-7, 1e-8],
+                    help="guards tried with the first threshold: groups with |c_j| max|V| >= guard always kept")
     ap.add_argument("--batch", action="store_true",
                     help="batched bond-stretch curve: 32 instances, batched vs unbatched Lanczos")
     ap.add_argument("--batch-scale", type=float, default=0.01,

@@ -232,8 +232,10 @@ int sfci_dot_noalloc(const uint64_t* x_keys, const double* x_amps, uint64_t nx, 
  * vectors of every instance at once, each by its own Hamiltonian.  Tag keys with
  * the instance before upload.  sfci_batch_lanczos runs sparse_krylov_solve_eigenval
  * (src/sparse_solver.cpp:246-548) on every instance with one batched product
- * per Krylov step; each instance's Nd is its vector's capacity; energies[i *
- * restarts + r], final_e[i] per instance. */
+ * per Krylov step; each instance's Nd is its vector's capacity, and opts.hpsi_cap
+ * caps each instance's products (not the batch's: the batched product's output
+ * grows to hold every survivor, and each instance's slice is cut to hpsi_cap by
+ * the single driver's rule); energies[i * restarts + r], final_e[i] per instance. */
 int sfci_batch_create(int n, const char* const* in_paths, const int* num_orb, const int* num_e,
                       const sfci_opts* opts, sfci_ctx** out);
 int sfci_batch_lanczos(sfci_ctx* ctx, sfci_vec* const* v, int n, int Nl, int restarts, double* energies,
@@ -304,6 +306,12 @@ int sfci_screen_params(sfci_screen* s, float* get, const float* set, uint64_t n)
 int sfci_screen_grads(sfci_screen* s, float* get, uint64_t n);
 /* Attach (s non-null) or detach the screen of the context's products. */
 int sfci_ctx_set_screen(sfci_ctx* ctx, sfci_screen* s, double threshold);
+/* Guard of the context's screened products: a group whose largest possible
+ * term, |c_j| times its two-body integral bound (the feature log|(pq|rs)|), is
+ * at least `guard` is kept whatever the network predicts; 0 switches it off
+ * (the default).  As the guard goes to 0+ the screened product becomes the
+ * plain one. */
+int sfci_ctx_set_screen_guard(sfci_ctx* ctx, double guard);
 /* groups seen, groups kept, terms kept, screened products, terms of all groups,
  * since the context was made (five counters) */
 int sfci_ctx_screen_stats(const sfci_ctx* ctx, uint64_t* out5);

@@ -114,6 +114,7 @@ def _sigs(L):
     L.sfci_screen_params.argtypes = [_vp, _vp, _vp, C.c_uint64]
     L.sfci_screen_grads.argtypes = [_vp, _vp, C.c_uint64]
     L.sfci_ctx_set_screen.argtypes = [_vp, _vp, C.c_double]
+    L.sfci_ctx_set_screen_guard.argtypes = [_vp, C.c_double]
     L.sfci_ctx_screen_stats.argtypes = [_vp, _u64p]
     return L
 
@@ -138,7 +139,7 @@ def load_library(path: str | None = None, build: bool = True):
                "sfci_add_two", "sfci_add_three", "sfci_shrink_from", "sfci_combine", "sfci_lanczos_ground",
                "sfci_minres", "sfci_gsaes", "sfci_cisd", "sfci_fci", "sfci_spmspv_linear", "sfci_res_norm",
                "sfci_krylov_linear", "sfci_shift_invert", "sfci_screen_create", "sfci_screen_train",
-               "sfci_ctx_set_screen"):
+               "sfci_ctx_set_screen", "sfci_ctx_set_screen_guard"):
         getattr(L, fn)
     _LIB = _sigs(L)
     return _LIB
@@ -252,7 +253,8 @@ class Context:
     @classmethod
     def batch(cls, in_paths, num_orbs, num_es, Nd: int = 200000, hpsi_cap: int = 60000000, **kw):
         """A batched context: one Hamiltonian per instance (<= 32 instances, <= 120 spin
-        orbitals each); keys carry their instance in their top bits (tag_keys)."""
+        orbitals each); keys carry their instance in their top bits (tag_keys).
+        In batch_lanczos, hpsi_cap caps each instance's products, as in its own run."""
         return cls(None, 128, max(num_es), Nd=Nd, hpsi_cap=hpsi_cap, _batch=(list(in_paths), num_orbs, num_es), **kw)
 
     def batch_lanczos(self, vecs, Nl: int, num_restart: int):
@@ -463,9 +465,11 @@ class Context:
         return dict(zip(names, [int(x) for x in a]))
 
     # learned excitation screen
-    def set_screen(self, screen: "Screen | None", threshold: float = 0.5):
-        """Screen this context's products (None: plain products)."""
+    def set_screen(self, screen: "Screen | None", threshold: float = 0.5, guard: float = 0.0):
+        """Screen this context's products (None: plain products).  A group whose
+        largest possible term |c_j| * max|V| reaches `guard` is always kept (0: no guard)."""
         _check(self.L.sfci_ctx_set_screen(self.h, screen.h if screen is not None else None, float(threshold)))
+        _check(self.L.sfci_ctx_set_screen_guard(self.h, float(guard)))
         self._screen = screen
 
     def screen_stats(self) -> dict:

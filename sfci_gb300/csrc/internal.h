@@ -56,6 +56,7 @@ struct Ctx {
   std::vector<cudaEvent_t> ev_pool;
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ph_pending;
   uint64_t stats[8] = {};
+  bool last_pruned = false;  // the last SpMSpV cut its survivors to the output capacity before the end
   double dup_est = 0.0;  // terms per distinct key of the last SpMSpV (sizes its leaves)
   // vectors created on this context (freed with it; their handles become orphans)
   std::set<struct Vec*> live;
@@ -81,6 +82,7 @@ struct Ctx {
   // screens created on this context (freed with it; their handles become orphans)
   std::set<struct Screen*> screens;
   double screen_thr = 0.5;
+  double screen_guard = 0.0;  // a group whose term bound |c_j| * max|V| reaches this is always kept (0: off)
   uint64_t screen_stats[5] = {};  // groups, kept groups, kept terms, screened products, terms of all groups
 };
 

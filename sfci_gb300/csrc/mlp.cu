@@ -246,6 +246,7 @@ struct FwdArgs {
   const u64* tile_start;  // training: first example of each tile (nullptr: tile t starts at 128 t)
   // inference
   float thr;
+  float lguard;           // log10 of the guard: a group with log10(|c_j| * vbound) >= lguard is kept
   uint32_t* keep;         // one bit per example
   u64* kept_terms;        // per source
   u64* kept_groups;       // per source
@@ -392,7 +393,9 @@ __global__ void __launch_bounds__(THREADS, 1) k_mlp_fwd(FwdArgs a) {
     }
     const float p = 1.f / (1.f + __expf(-logit));
     if (!TRAIN) {
-      const bool kept = valid && p >= a.thr;
+      // the guard keeps every group whose largest possible term, |c_j| times
+      // the group's integral bound, reaches it, whatever the network says
+      const bool kept = valid && (p >= a.thr || 10.f * (f.lc + f.lv) >= a.lguard);
       const unsigned m = __ballot_sync(0xffffffffu, kept);
       if (lane == 0 && e0 + 32 * warp < a.x.nex) a.keep[(e0 >> 5) + warp] = m;
       if (valid && a.prob) a.prob[e] = p;
@@ -874,8 +877,9 @@ static int check_err(Screen& s) {
 }
 
 // inference over the groups of n sources: keep bits, kept groups and terms per source
-static int screen_infer(Ctx& c, Screen& s, const u64* keys, const double* amps, u64 n, double thr, u64** goff_out,
-                        uint32_t** keep_out, u64** kterms_out, u64** kgroups_out, u64* nex_out, float* prob) {
+static int screen_infer(Ctx& c, Screen& s, const u64* keys, const double* amps, u64 n, double thr, double guard,
+                        u64** goff_out, uint32_t** keep_out, u64** kterms_out, u64** kgroups_out, u64* nex_out,
+                        float* prob) {
   int st;
   u64* goff = (u64*)scratch_get(c, "sc_goff", (n + 1) * sizeof(u64));
   if (!goff) return SFCI_ERR_NOMEM;
@@ -896,6 +900,7 @@ static int screen_infer(Ctx& c, Screen& s, const u64* keys, const double* amps, 
   a.W2img = s.W2img;
   a.ntiles = ntiles;
   a.thr = (float)thr;
+  a.lguard = guard > 0.0 ? (float)std::log10(guard) : INFINITY;
   a.keep = keep;
   a.kept_terms = kt;
   a.kept_groups = kg;
@@ -973,7 +978,8 @@ int screen_select(Ctx& c, const void* keys, const double* amps, u64 n, ScreenLis
   int st;
   u64 *goff, *kt, *kg, nex = 0;
   uint32_t* keep;
-  if ((st = screen_infer(c, s, (const u64*)keys, amps, n, c.screen_thr, &goff, &keep, &kt, &kg, &nex, nullptr)))
+  if ((st = screen_infer(c, s, (const u64*)keys, amps, n, c.screen_thr, c.screen_guard, &goff, &keep, &kt, &kg, &nex,
+                         nullptr)))
     return st;
   // offsets of the kept-group lists, the largest list, the totals
   u64* koff = (u64*)scratch_get(c, "sc_koff", (n + 1) * sizeof(u64));
@@ -1343,7 +1349,7 @@ extern "C" int sfci_screen_predict(sfci_screen* x, const sfci_vec* in, double th
     prob = (float*)scratch_get(c, "sc_prob", (ng + 1) * sizeof(float));
     if (!prob) return SFCI_ERR_NOMEM;
   }
-  if ((st = screen_infer(c, s, in->v.keys, in->v.amps, in->v.len, threshold, &goff, &keep, &kt, &kg, &nex, prob)))
+  if ((st = screen_infer(c, s, in->v.keys, in->v.amps, in->v.len, threshold, 0.0, &goff, &keep, &kt, &kg, &nex, prob)))
     return st;
   std::vector<u64> a(in->v.len), b(in->v.len);
   if ((st = read_words(c, kt, in->v.len * sizeof(u64), a.data()))) return st;
@@ -1395,6 +1401,13 @@ extern "C" int sfci_ctx_set_screen(sfci_ctx* ctx, sfci_screen* x, double thresho
   if (!(threshold >= 0.0 && threshold <= 1.0)) return set_error(SFCI_ERR_ARG, "sfci_ctx_set_screen: threshold in [0, 1]");
   ctx->c.screen = x ? &x->s : nullptr;
   ctx->c.screen_thr = threshold;
+  return SFCI_OK;
+}
+
+extern "C" int sfci_ctx_set_screen_guard(sfci_ctx* ctx, double guard) {
+  if (!ctx) return set_error(SFCI_ERR_ARG, "sfci_ctx_set_screen_guard: null context");
+  if (!(guard >= 0.0) || std::isinf(guard)) return set_error(SFCI_ERR_ARG, "sfci_ctx_set_screen_guard: guard >= 0, finite");
+  ctx->c.screen_guard = guard;
   return SFCI_OK;
 }
 

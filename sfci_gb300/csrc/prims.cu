@@ -259,24 +259,26 @@ constexpr int CP_TILE = CP_THREADS * CP_CHUNKS;
 // Ties at the threshold are kept from the end of the index order (the largest keys
 // of a key-sorted vector), as a stable ascending sort by |a| followed by "keep the
 // last k" does.
+// The magnitude tests compare the bits of |a| as integers (cut_key: -1 keeps
+// everything), which orders finite doubles as their values do and keeps these
+// passes off the FP64 pipe.
 struct KeepRule {
   int mode;
   u64 tau;
   u64 eq_skip;
-  double cut;
-  double tiny;
+  long long cut_key;   // mode 0: keep |a| > cut
+  long long tiny_key;  // mode 1: then |a| > tiny (-1: no such filter)
 };
 
 __device__ __forceinline__ bool keep_of(const KeepRule& r, double a, u64 eq_rank, bool& is_eq) {
   u64 b = abs_bits(a);
   if (r.mode == 0) {
     is_eq = false;
-    return fabs(a) > r.cut;
+    return (long long)b > r.cut_key;
   }
   is_eq = (b == r.tau);
   bool k = b > r.tau || (is_eq && eq_rank >= r.eq_skip);
-  if (k && r.tiny >= 0.0) k = fabs(a) > r.tiny;
-  return k;
+  return k && (long long)b > r.tiny_key;
 }
 
 // stage 0: per-tile count of |a| == tau
@@ -408,14 +410,14 @@ static int compact_rule(Ctx& c, const typename KeyOf<W>::T* ik, const double* ia
 template <int W>
 int compact_top(Ctx& c, const typename KeyOf<W>::T* ik, const double* ia, size_t n, u64 tau, size_t need_eq,
                 double tiny, typename KeyOf<W>::T* ok, double* oa, size_t* m) {
-  KeepRule r{1, tau, (u64)need_eq, 0.0, tiny};
+  KeepRule r{1, tau, (u64)need_eq, -1ll, cut_key(tiny)};
   return compact_rule<W>(c, ik, ia, n, r, ok, oa, m);
 }
 
 template <int W>
 int compact_cut(Ctx& c, const typename KeyOf<W>::T* ik, const double* ia, size_t n, double cut,
                 typename KeyOf<W>::T* ok, double* oa, size_t* m) {
-  KeepRule r{0, 0, 0, cut, -1.0};
+  KeepRule r{0, 0, 0, cut_key(cut), -1ll};
   return compact_rule<W>(c, ik, ia, n, r, ok, oa, m);
 }
 
@@ -427,7 +429,7 @@ int top_k_stable(Ctx& c, typename KeyOf<W>::T* ik, double* ia, size_t n, size_t 
     if (tiny >= 0.0) {
       // filter only: keep |a| > tiny (all of them pass the selection)
       // tau = 0 keeping all n ties keeps everything before the tiny filter
-      KeepRule r{1, 0ull, (u64)n, 0.0, tiny};
+      KeepRule r{1, 0ull, (u64)n, -1ll, cut_key(tiny)};
       return compact_rule<W>(c, ik, ia, n, r, ok, oa, m);
     }
     if (ok != ik) {

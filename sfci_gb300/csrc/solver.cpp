@@ -448,13 +448,20 @@ namespace sfci {
 namespace {
 struct GrowVec {
   DVec d;
-  int need(Ctx& c, uint64_t cap) {
-    if (d.v.keys && d.v.cap >= cap) return SFCI_OK;
-    if (d.v.keys) cudaFree(d.v.keys);
-    if (d.v.amps) cudaFree(d.v.amps);
-    d.v.keys = nullptr;
-    d.v.amps = nullptr;
-    return d.alloc(c, std::max<uint64_t>(cap, 1024));
+  uint64_t phys = 0;  // allocated entries
+  // room for at least `want` entries; the vector's capacity, which is what caps
+  // an axpy or a product into it, is min(allocated, limit)
+  int need(Ctx& c, uint64_t want, uint64_t limit = ~0ull) {
+    if (!d.v.keys || phys < want) {
+      if (d.v.keys) cudaFree(d.v.keys);
+      if (d.v.amps) cudaFree(d.v.amps);
+      d.v.keys = nullptr;
+      d.v.amps = nullptr;
+      TRY(d.alloc(c, std::max<uint64_t>(want, 1024)));
+      phys = d.v.cap;
+    }
+    d.v.cap = std::min(phys, limit);
+    return SFCI_OK;
   }
 };
 struct Inst {
@@ -487,13 +494,26 @@ static int batched_product(Ctx& c, std::vector<Inst>& S, const std::vector<int>&
     o += x.len;
   }
   all_in.d.v.len = tot;
-  TRY(all_out.need(c, c.opts.hpsi_cap));
+  // The product's output capacity is a cap over the whole batch, but each
+  // instance's cap is hpsi_cap, as in its own driver.  So the batch output
+  // holds every survivor (the capacity grows, and the product is redone, when
+  // the survivors outgrow it), and each instance's slice is cut to hpsi_cap by
+  // the same stable top-k rule the product's own cap applies.
+  const uint64_t hcap = c.opts.hpsi_cap;
+  uint64_t want = std::max<uint64_t>(hcap, all_out.d.v.cap);
   double dg = 0.0;
   const uint64_t Nd = c.opts.Nd;
-  c.opts.Nd = std::max<uint64_t>(Nd, tot);  // each instance is already truncated to its own Nd
-  int st = op_spmspv(c, all_in.d.v, all_out.d.v, 0.0, 1.0, &dg);
-  c.opts.Nd = Nd;
-  TRY(st);
+  for (int attempt = 0;; ++attempt) {
+    TRY(all_out.need(c, want));
+    c.opts.Nd = std::max<uint64_t>(Nd, tot);  // each instance is already truncated to its own Nd
+    int st = op_spmspv(c, all_in.d.v, all_out.d.v, 0.0, 1.0, &dg);
+    c.opts.Nd = Nd;
+    TRY(st);
+    const uint64_t surv = c.stats[3];
+    if (!c.last_pruned && surv <= all_out.d.v.cap) break;
+    if (attempt >= 8) return set_error(SFCI_ERR_NOMEM, "batched SpMSpV: survivors keep outgrowing the output");
+    want = std::max<uint64_t>(surv + surv / 4, 2 * all_out.d.v.cap);
+  }
   std::vector<u64> b(nin + 1);
   TRY(inst_bounds(c, all_out.d.v, nin, b.data()));
   for (int i : idx) {
@@ -501,14 +521,24 @@ static int batched_product(Ctx& c, std::vector<Inst>& S, const std::vector<int>&
     const uint64_t n = b[i + 1] - b[i];
     // room for the axpy that follows (at most Nd more entries), as the single
     // driver's HPsiCap-sized vectors have
-    TRY(dst.need(c, std::min<uint64_t>(c.opts.hpsi_cap, n + S[i].Nd)));
-    if (n) {
-      SFCI_CUDA(cudaMemcpyAsync(dst.d.v.keys, all_out.d.v.keys + b[i] * 2, n * 2 * sizeof(u64),
-                                cudaMemcpyDeviceToDevice, c.stream));
-      SFCI_CUDA(cudaMemcpyAsync(dst.d.v.amps, all_out.d.v.amps + b[i], n * sizeof(double), cudaMemcpyDeviceToDevice,
-                                c.stream));
+    TRY(dst.need(c, std::min<uint64_t>(hcap, n + S[i].Nd), hcap));
+    Vec slice;
+    slice.ctx = &c;
+    slice.keys = all_out.d.v.keys + b[i] * 2;
+    slice.amps = all_out.d.v.amps + b[i];
+    slice.len = slice.cap = n;
+    if (n > hcap) {
+      Vec cut = dst.d.v;
+      cut.cap = hcap;
+      TRY(op_shrink(c, cut, slice));
+      dst.d.v.len = cut.len;
+    } else {
+      if (n) {
+        SFCI_CUDA(cudaMemcpyAsync(dst.d.v.keys, slice.keys, n * 2 * sizeof(u64), cudaMemcpyDeviceToDevice, c.stream));
+        SFCI_CUDA(cudaMemcpyAsync(dst.d.v.amps, slice.amps, n * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
+      }
+      dst.d.v.len = n;
     }
-    dst.d.v.len = n;
     S[i].alpha = c.inst_diag.size() > (size_t)i ? c.inst_diag[i] : 0.0;
   }
   return SFCI_OK;
@@ -552,7 +582,7 @@ int lanczos_batched(Ctx& c, Vec* const* v, int n, int Nl, int restarts, double* 
     for (int it = 1; it < Nl; ++it) {
       for (int i : idx) {
         Inst& s = S[i];
-        TRY(s.temp.need(c, std::min<uint64_t>(c.opts.hpsi_cap, s.u.d.v.len + s.v->len)));
+        TRY(s.temp.need(c, std::min<uint64_t>(c.opts.hpsi_cap, s.u.d.v.len + s.v->len), c.opts.hpsi_cap));
         TRY(op_copy(c, s.temp.d.v, s.u.d.v));
         TRY(op_add_two(c, s.temp.d.v, *s.v, -s.alpha));
         TRY(op_shrink(c, s.v_next.v, s.temp.d.v));
@@ -573,7 +603,7 @@ int lanczos_batched(Ctx& c, Vec* const* v, int n, int Nl, int restarts, double* 
           km(it, j) = d;
         }
         TRY(op_add_two(c, s.temp_u.d.v, *s.v, -s.beta));
-        TRY(s.u.need(c, s.temp_u.d.v.len));
+        TRY(s.u.need(c, s.temp_u.d.v.len, c.opts.hpsi_cap));
         TRY(op_copy(c, s.u.d.v, s.temp_u.d.v));
         TRY(op_copy(c, *s.v, s.v_next.v));
         TRY(op_copy(c, s.KB[it]->v, *s.v));

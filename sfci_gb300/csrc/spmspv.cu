@@ -1421,6 +1421,7 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
     ns = m;
   }
   c.stats[0] = ns;
+  c.last_pruned = false;
   // extra single terms (coef * vector entries) join the generation sources
   // after the input determinants; the <v|Hv> share still covers the input only
   const KT* gen_k = src_k;
@@ -1730,8 +1731,12 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
         if (scount_h + gterms > SC && scount_h > cap) {
           int t2 = phase_begin(c, PH_SELECT);
           size_t m = 0;
+          // key order first: exact ties at the cut keep the highest keys, whatever
+          // order the leaves wrote their survivors in
+          if ((st = radix_sort_pairs<W>(c, sk, sa, scount_h, c.N))) return st;
           if ((st = top_k_stable<W>(c, sk, sa, scount_h, cap, -1.0, sk, sa, &m))) return st;
           scount_h = m;
+          c.last_pruned = true;
           SFCI_CUDA(cudaMemcpyAsync(scount, &scount_h, sizeof(u64), cudaMemcpyHostToDevice, c.stream));
           phase_end(c, t2);
         }
@@ -1922,7 +1927,13 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
                      "SpMSpV term with |amplitude| >= 2^24 or not finite: outside the merge accumulator's range");
   c.stats[3] = scount_h;
   u64 nout = scount_h;
+  tok = phase_begin(c, PH_SORT);
+  if ((st = radix_sort_pairs<W>(c, sk, sa, nout, c.N))) return st;
+  phase_end(c, tok);
   if (nout > cap) {
+    // the top cap by |amplitude| of the key-ordered survivors: a stable
+    // compaction, so the result stays in key order and exact ties at the cut
+    // keep the highest keys
     tok = phase_begin(c, PH_SELECT);
     size_t m = 0;
     if ((st = top_k_stable<W>(c, sk, sa, nout, cap, -1.0, sk, sa, &m))) return st;
@@ -1930,7 +1941,6 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
     phase_end(c, tok);
   }
   tok = phase_begin(c, PH_SORT);
-  if ((st = radix_sort_pairs<W>(c, sk, sa, nout, c.N))) return st;
   SFCI_CUDA(cudaMemcpyAsync(out.keys, sk, nout * sizeof(KT), cudaMemcpyDeviceToDevice, c.stream));
   SFCI_CUDA(cudaMemcpyAsync(out.amps, sa, nout * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
   out.len = nout;

@@ -80,18 +80,22 @@ def test_batched_product_equals_unbatched_products(curve):
         assert np.array_equal(aa[sel].view(np.uint64), want[k][1].view(np.uint64)), k
 
 
-def test_batched_lanczos_matches_unbatched_runs(curve):
+@pytest.mark.parametrize("cap", [2000000, 3000])
+def test_batched_lanczos_matches_unbatched_runs(curve, cap):
+    """cap is every instance's hpsi_cap; at 3000 it cuts each instance's
+    products, so the batched driver's per-instance cut (after a batch output
+    that grew to hold every survivor) must pick what each unbatched run keeps."""
     Nl, restarts = 8, 2
     orbs = [2 * M for M, _, _, _ in INSTANCES]
     nes = [ne for _, ne, _, _ in INSTANCES]
     ref = []
     for k, (M, ne, t, nd) in enumerate(INSTANCES):
-        c = sg.Context(curve[k], 2 * M, ne, Nd=nd, hpsi_cap=2000000)
+        c = sg.Context(curve[k], 2 * M, ne, Nd=nd, hpsi_cap=cap)
         v = c.vec(nd)
         v.upload(sg.keys_from_ints([(1 << ne) - 1], c.words), np.array([1.0]))
         en, fe = c.sparse_krylov_solve_eigenval(v, Nl, restarts)
         ref.append((en, fe))
-    bc = sg.Context.batch(curve, orbs, nes, Nd=10 ** 6, hpsi_cap=8000000)
+    bc = sg.Context.batch(curve, orbs, nes, Nd=10 ** 6, hpsi_cap=cap)
     vs = []
     for k, (M, ne, t, nd) in enumerate(INSTANCES):
         v = bc.vec(nd)

@@ -176,6 +176,43 @@ def test_threshold_zero_gives_the_plain_product(golden_in):
     assert d0 == d1
 
 
+def test_guard_keeps_groups_with_large_term_bounds(golden_in):
+    """A threshold above every probability skips every double group; a guard
+    below every group's term bound keeps them all again (the plain product bit
+    for bit), and a guard in between keeps the groups it must."""
+    g, path, c, keys, amps, _ = _setup(golden_in)
+    vin = c.vec_from(keys, amps)
+    out0 = c.vec(2000000)
+    d0 = c.SpMVMtply_bucket(vin, out0, 0.0, 1.0)
+    k0, a0 = out0.download()
+    scr = sg.Screen(c, seed=7)
+    c.set_screen(scr, 1.0, guard=1e-300)
+    out1 = c.vec(2000000)
+    d1 = c.SpMVMtply_bucket(vin, out1, 0.0, 1.0)
+    k1, a1 = out1.download()
+    st = c.screen_stats()
+    assert st["kept_groups"] == st["groups"] > 0
+    assert np.array_equal(k0, k1) and np.array_equal(a0.view(np.uint64), a1.view(np.uint64)) and d0 == d1
+    # no guard: threshold 1 keeps no double group (a sigmoid output stays below 1 here)
+    c.set_screen(scr, 1.0)
+    s0 = c.screen_stats()
+    c.SpMVMtply_bucket(vin, out1, 0.0, 1.0)
+    s1 = c.screen_stats()
+    none_kept = s1["kept_groups"] - s0["kept_groups"]
+    # a lower guard keeps at least the groups a higher one keeps
+    kept = [none_kept]
+    for gd in (1e-2, 1e-4, 1e-6):
+        c.set_screen(scr, 1.0, guard=gd)
+        a_ = c.screen_stats()
+        c.SpMVMtply_bucket(vin, out1, 0.0, 1.0)
+        b_ = c.screen_stats()
+        kept.append(b_["kept_groups"] - a_["kept_groups"])
+    assert all(x <= y for x, y in zip(kept, kept[1:])), kept
+    assert kept[-1] > kept[0], kept
+    with pytest.raises(sg.SfciError):
+        c.set_screen(scr, 0.5, guard=-1.0)
+
+
 def test_partial_screen_is_the_merge_of_the_kept_groups(golden_in, port):
     g, path, c, keys, amps, _ = _setup(golden_in, n=150, seed=5)
     N, M = 20, 10

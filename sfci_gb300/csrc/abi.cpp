@@ -36,7 +36,9 @@ void* scratch_get(Ctx& c, const char* name, size_t bytes) {
     b.p = nullptr;
     b.bytes = 0;
   }
-  size_t want = bytes + bytes / 8;  // headroom against regrowth
+  // headroom against regrowth, for buffers under 1 GiB only: the large ones
+  // are sized by the product's memory plan, which the headroom would overrun
+  size_t want = bytes < ((size_t)1 << 30) ? bytes + bytes / 8 : bytes;
   void* p = nullptr;
   if (cudaMalloc(&p, want) != cudaSuccess) {
     cudaGetLastError();

@@ -12,7 +12,7 @@ typedef unsigned long long plan_u64;
 struct MemPlan {
   plan_u64 C1 = 0;  // level-1 term capacity: the terms of one generation pass
   plan_u64 C2 = 0;  // level-2 group capacity (partition ping-pong buffer)
-  plan_u64 SC = 0;  // survivor capacity (held twice: a reduction stages through a copy)
+  plan_u64 SC = 0;  // survivor capacity (held twice: the key sort before a cut goes through a copy)
   int passes = 0;
 };
 

@@ -457,6 +457,26 @@ int top_k_stable(Ctx& c, typename KeyOf<W>::T* ik, double* ia, size_t n, size_t 
   return compact_top<W>(c, ik, ia, n, tau, need_eq, tiny, ok, oa, m);
 }
 
+template <int W>
+int select_sorted(Ctx& c, typename KeyOf<W>::T* keys, double* vals, size_t n, size_t k, size_t* m) {
+  typedef typename KeyOf<W>::T KT;
+  int st = radix_sort_pairs<W>(c, keys, vals, n, c.N);
+  if (st) return st;
+  if (n <= k) {
+    *m = n;
+    return SFCI_OK;
+  }
+  KT* tk = (KT*)scratch_get(c, "rs_keys", n * sizeof(KT));
+  double* ta = (double*)scratch_get(c, "rs_vals", n * sizeof(double));
+  if (!tk || !ta) return SFCI_ERR_NOMEM;
+  if ((st = top_k_stable<W>(c, keys, vals, n, k, -1.0, tk, ta, m))) return st;
+  SFCI_CUDA(cudaMemcpyAsync(keys, tk, *m * sizeof(KT), cudaMemcpyDeviceToDevice, c.stream));
+  SFCI_CUDA(cudaMemcpyAsync(vals, ta, *m * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
+  return SFCI_OK;
+}
+
+template int select_sorted<1>(Ctx&, u64*, double*, size_t, size_t, size_t*);
+template int select_sorted<2>(Ctx&, K128*, double*, size_t, size_t, size_t*);
 template int compact_top<1>(Ctx&, const u64*, const double*, size_t, u64, size_t, double, u64*, double*, size_t*);
 template int compact_top<2>(Ctx&, const K128*, const double*, size_t, u64, size_t, double, K128*, double*,
                             size_t*);

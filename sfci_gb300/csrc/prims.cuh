@@ -97,6 +97,13 @@ template <int W>
 int top_k_stable(Ctx& c, typename KeyOf<W>::T* ik, double* ia, size_t n, size_t k, double tiny,
                  typename KeyOf<W>::T* ok, double* oa, size_t* m);
 
+// Sort (keys, vals) by key in place, then keep the k largest |a| in key order
+// (all of them when n <= k): exact ties at the threshold keep the highest keys,
+// whatever order the pairs came in.  The compaction writes into the sort's
+// scratch and copies back, so no third n-sized buffer is needed.
+template <int W>
+int select_sorted(Ctx& c, typename KeyOf<W>::T* keys, double* vals, size_t n, size_t k, size_t* m);
+
 // deterministic FP64 sum / dot reductions
 int reduce_sum_sq(Ctx& c, const double* a, size_t n, double* out);
 

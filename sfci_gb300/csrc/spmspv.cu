@@ -1488,22 +1488,44 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
   tok = phase_begin(c, PH_OTHER);
   const size_t tb = sizeof(KT) + sizeof(double);
   const u64 cap = out.cap;
-  size_t budget = 0;
-  {
-    size_t freeb = 0, totb = 0;
-    SFCI_CUDA(cudaMemGetInfo(&freeb, &totb));
-    size_t held = 0;
-    for (const char* nm : {"sp_l1k", "sp_l1a", "sp_l2k", "sp_l2a", "sp_sk", "sp_sa", "topk_k", "topk_a"}) {
-      auto it = c.scratch.find(nm);
-      if (it != c.scratch.end()) held += it->second.bytes;
-    }
-    budget = c.opts.mem_budget ? (size_t)c.opts.mem_budget : (size_t)((freeb + held) * 0.90);
-  }
-  const u64 avail = budget / tb;
   const double dup = c.dup_est > 0.0 ? c.dup_est : 8.0;
   const int leaf_uniq = std::max(16, std::min(TW_UNIQ, c.tune_leaf_uniq));
   const int l1_bits = std::max(4, std::min(L1_BITS, c.tune_l1_bits));
   const int digit_bits = std::max(6, std::min(DIGIT_MAX, c.tune_digit_bits));
+  // 2^b leaves for `terms` generated terms: the fewest (so the fewest partition
+  // levels, each a full read and write of the terms, and the best amortised
+  // per-leaf table set-up) whose expected distinct keys stay within the leaf
+  // size, so that a warp table takes a leaf.  The distinct count is estimated
+  // from the duplication (terms per distinct key) of the previous product on
+  // this context (default 8).  At most LEAF_TERMS terms a leaf as well: with
+  // many terms per key (hot determinants) a leaf sized by distinct keys alone
+  // outgrows the warp tier's FX32_MAX_TERMS.
+  auto leaf_bits = [&](u64 terms) -> int {
+    const double uniq_est = std::max(1.0, (double)terms / std::max(1.0, dup));
+    const int b_terms = (int)std::ceil(std::log2(std::max(2.0, (double)terms / LEAF_TERMS)));
+    const int b_uniq = (int)std::ceil(std::log2(std::max(2.0, uniq_est / leaf_uniq)));
+    return std::max(1, std::min(B_MAX, std::max(b_terms, b_uniq)));
+  };
+  size_t budget = 0;
+  {
+    size_t freeb = 0, totb = 0;
+    SFCI_CUDA(cudaMemGetInfo(&freeb, &totb));
+    // the plan's buffers (replaced in place when they grow): the two term
+    // levels and the survivors; the plan also leaves room for the sort scratch
+    // the survivors go through (not counted here: whatever it holds stays held)
+    size_t held = 0;
+    for (const char* nm : {"sp_l1k", "sp_l1a", "sp_l2k", "sp_l2a", "sp_sk", "sp_sa"}) {
+      auto it = c.scratch.find(nm);
+      if (it != c.scratch.end()) held += it->second.bytes;
+    }
+    // allocations made after the plan, kept out of it: per leaf the input
+    // offsets and cursors, boundaries and overflow lists (24 B), the input
+    // grouped by leaf, and a margin for the small tables
+    const size_t reserve = ((size_t)24 << leaf_bits(T)) + (size_t)ns * tb + ((size_t)256 << 20);
+    const size_t pool = (size_t)((freeb + held) * 0.88);
+    budget = c.opts.mem_budget ? (size_t)c.opts.mem_budget : (pool > reserve ? pool - reserve : 0);
+  }
+  const u64 avail = budget / tb;
   struct OuterPass {
     unsigned lo, hi;  // class range (class passes)
     u64 terms;        // terms this outer pass generates
@@ -1598,19 +1620,8 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
       if ((st = read_words(c, doffp + ns, sizeof(u64), &Tp))) return st;
       phase_end(c, tok);
     }
-    // hash digits: level 1 (generation) d0 bits, then nlev partition levels.
-    // 2^b leaves: the fewest (so the fewest partition levels, each a full read
-    // and write of the terms, and the best amortised per-leaf table set-up) whose
-    // expected distinct keys stay within TW_UNIQ, so that a warp table takes a
-    // leaf.  The distinct count is estimated from the duplication (terms per
-    // distinct key) of the previous product on this context (default 8).
-    const double uniq_est = std::max(1.0, (double)opass.terms / std::max(1.0, dup));
-    // at most LEAF_TERMS terms a leaf as well: with many terms per key (hot
-    // determinants) a leaf sized by distinct keys alone outgrows the warp
-    // tier's FX32_MAX_TERMS
-    const int b_terms = (int)std::ceil(std::log2(std::max(2.0, (double)opass.terms / LEAF_TERMS)));
-    const int b = std::max(1, std::min(B_MAX, std::max(b_terms,
-                                                       (int)std::ceil(std::log2(std::max(2.0, uniq_est / leaf_uniq))))));
+    // hash digits: level 1 (generation) d0 bits, then nlev partition levels
+    const int b = leaf_bits(opass.terms);
     const int d0 = std::min(b, l1_bits);
     const int rem = b - d0;
     const int nlev = rem ? (rem + digit_bits - 1) / digit_bits : 0;
@@ -1733,8 +1744,7 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
           size_t m = 0;
           // key order first: exact ties at the cut keep the highest keys, whatever
           // order the leaves wrote their survivors in
-          if ((st = radix_sort_pairs<W>(c, sk, sa, scount_h, c.N))) return st;
-          if ((st = top_k_stable<W>(c, sk, sa, scount_h, cap, -1.0, sk, sa, &m))) return st;
+          if ((st = select_sorted<W>(c, sk, sa, scount_h, cap, &m))) return st;
           scount_h = m;
           c.last_pruned = true;
           SFCI_CUDA(cudaMemcpyAsync(scount, &scount_h, sizeof(u64), cudaMemcpyHostToDevice, c.stream));
@@ -1927,16 +1937,10 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
                      "SpMSpV term with |amplitude| >= 2^24 or not finite: outside the merge accumulator's range");
   c.stats[3] = scount_h;
   u64 nout = scount_h;
-  tok = phase_begin(c, PH_SORT);
-  if ((st = radix_sort_pairs<W>(c, sk, sa, nout, c.N))) return st;
-  phase_end(c, tok);
-  if (nout > cap) {
-    // the top cap by |amplitude| of the key-ordered survivors: a stable
-    // compaction, so the result stays in key order and exact ties at the cut
-    // keep the highest keys
-    tok = phase_begin(c, PH_SELECT);
+  {
+    tok = phase_begin(c, nout > cap ? PH_SELECT : PH_SORT);
     size_t m = 0;
-    if ((st = top_k_stable<W>(c, sk, sa, nout, cap, -1.0, sk, sa, &m))) return st;
+    if ((st = select_sorted<W>(c, sk, sa, nout, cap, &m))) return st;
     nout = m;
     phase_end(c, tok);
   }

@@ -465,9 +465,9 @@ def _finish_gpu(args, rank, ws, dist, ctx, sysd, path, nd, M, NE, W, n_in, C, T_
     kernels = {"scatter": "k_gen<SCATTER>", "partition": "k_part<COUNT,SCATTER>", "merge": "k_leafw",
                "count": "k_gen<COUNT>", "select": "select_threshold", "sort": "radix_sort_pairs", "other": "-"}
     # DRAM bytes per generated term measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum over
-    # every launch of a 56-orbital Nd=1e4 run with 4 generation passes), scaled here to a launch by the
-    # terms it processes
-    ncu_bytes_per_term = {"scatter": 17.79, "partition": 50.53 * levels, "merge": 16.11}
+    # the launches of one 56-orbital Nd=1e4 SpMSpV in one generation pass, 2 partition levels, 8 GB device
+    # budget: level buffers well above L2), scaled here to a launch by the terms it processes
+    ncu_bytes_per_term = {"scatter": 26.31, "partition": 38.50 * levels, "merge": 16.07}
     dom = max(prof, key=lambda k: prof[k][0])
     dms, dl = prof[dom]
     per_launch_bytes = alg[dom] / max(dl, 1)

@@ -123,12 +123,23 @@ struct DVec {
     v.cap = cap;
     v.len = 0;
     size_t n = cap ? cap : 1;
-    if (cudaMalloc(&v.keys, n * ctx.W * sizeof(u64)) != cudaSuccess ||
-        cudaMalloc(&v.amps, n * sizeof(double)) != cudaSuccess) {
+    // the products keep their scratch between calls (up to most of the
+    // device); a driver vector that finds no room releases it and retries, and
+    // the next product plans with what is left
+    for (int attempt = 0; attempt < 2; ++attempt) {
+      if (cudaMalloc(&v.keys, n * ctx.W * sizeof(u64)) == cudaSuccess &&
+          cudaMalloc(&v.amps, n * sizeof(double)) == cudaSuccess)
+        return SFCI_OK;
       cudaGetLastError();
-      return set_error(SFCI_ERR_NOMEM, "driver vector allocation failed");
+      if (v.keys) cudaFree(v.keys);
+      v.keys = nullptr;
+      v.amps = nullptr;
+      if (attempt == 0) {
+        cudaStreamSynchronize(ctx.stream);
+        scratch_free_all(ctx);
+      }
     }
-    return SFCI_OK;
+    return set_error(SFCI_ERR_NOMEM, "driver vector allocation failed");
   }
   ~DVec() {
     if (v.keys) cudaFree(v.keys);

@@ -54,6 +54,8 @@ constexpr int LC_SLOTS = 4096;
 constexpr unsigned LW_PROBE = 32;                 // probes before a warp table counts as overflowed
 constexpr unsigned LC_PROBE = 128;                // same for the second tier
 constexpr int B_MAX = 30;
+constexpr int CP_MAX = 2016;   // pairs of 64 orbitals of a spin: C(64, 2)
+constexpr int RUN_CAP = 2048;  // class passes: (occupied pair, class block) runs of spin-0 doubles per determinant
 constexpr double LEAF_TERMS = 1024.0;                 // terms a leaf is sized for (at most, on average)
 
 enum { M_COUNT = 0, M_SCATTER = 1, M_ENERGY = 2, M_PROJECT = 3, M_LABEL = 4 };
@@ -250,15 +252,25 @@ struct GenArgs {
   // each) whose class is in the pass
   int cls_on = 0;
   unsigned cls_lo = 0, cls_hi = 0;
+  int cls_k = 0;  // the pass is (cls_hi - cls_lo) >> cls_k aligned blocks of 2^cls_k classes
 };
 
+// class-pass tables of a determinant: run starts, K >> k of each occupied
+// spin-0 pair, the empty spin-0 pairs sorted by class bucket, each pair's
+// bucket, and the bucket starts
+__host__ __device__ inline size_t cls_smem_bytes() {
+  return al16(sizeof(uint32_t) * (RUN_CAP + 1)) + al16(CP_MAX) + al16(sizeof(unsigned short) * CP_MAX) + al16(CP_MAX) +
+         al16(sizeof(uint32_t) * 257);
+}
+
 template <class KT>
-__host__ __device__ inline size_t gen_smem_bytes(int mode, unsigned nbp, unsigned kl_cap = 0) {
+__host__ __device__ inline size_t gen_smem_bytes(int mode, unsigned nbp, unsigned kl_cap = 0, bool cls = false) {
   size_t s = al16(sizeof(DetInfo<KT>)) + al16(2016 * sizeof(unsigned short));
   if (mode == M_COUNT || mode == M_SCATTER) s += al16(sizeof(uint32_t) * nbp);
   if (mode == M_SCATTER)
     s += al16(sizeof(uint32_t) * nbp) + 2 * al16(sizeof(u64) * nbp) + 3 * al16(sizeof(unsigned short) * GEN_ROUND);
   s += 2 * al16(sizeof(uint32_t) * kl_cap);
+  if (cls) s += cls_smem_bytes();
   return s;
 }
 
@@ -293,7 +305,14 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
   }
   uint32_t* kst = reinterpret_cast<uint32_t*>(smem + off);  // kept groups of the current determinant
   uint32_t* kpr = kst + (al16(sizeof(uint32_t) * g.kl_cap) / sizeof(uint32_t));
-  __shared__ unsigned s_nk;
+  off += 2 * al16(sizeof(uint32_t) * g.kl_cap);
+  // class passes (see the class-pass set-up below)
+  uint32_t* rpre = reinterpret_cast<uint32_t*>(smem + off);
+  unsigned char* kop = smem + off + al16(sizeof(uint32_t) * (RUN_CAP + 1));
+  unsigned short* cperm = reinterpret_cast<unsigned short*>(kop + al16(CP_MAX));
+  unsigned char* cbq = reinterpret_cast<unsigned char*>(cperm) + al16(sizeof(unsigned short) * CP_MAX);
+  uint32_t* cboff = reinterpret_cast<uint32_t*>(cbq + al16(CP_MAX));
+  __shared__ unsigned s_nk, s_n2;
   __shared__ u64 s_det;
   __shared__ unsigned s_nsq;
   __shared__ double s_red[GEN_THREADS / 32];
@@ -402,43 +421,122 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
     if (det < g.nmain) det_fill_singles(d, tid, GEN_THREADS);  // (term 0 needs no tables)
     __syncthreads();
     if (cls_pass) {
-      // the pass's blocks of this determinant, in term order: [0, c[3]) always,
-      // the spin-1 doubles when the determinant's class is in the pass, then the
-      // opposite-spin blocks of the spin-0 singles whose class is
-      const unsigned lo = g.cls_lo, hi = g.cls_hi;
-      const bool own = d.h.acls >= lo && d.h.acls < hi;
-      const unsigned nx = d.h.na[0] * d.h.nv[0], nsb = d.h.nsb;
-      if (tid == 0) {
-        kst[0] = 0;
-        kpr[0] = 0;
-        if (own) {
-          kst[1] = d.h.c[3];
-          kpr[1] = d.h.c[3];
+      // The pass owns the aligned class blocks P0 .. P0 + nblk - 1 (of 2^kb
+      // classes each).  Its index space for this determinant, in order:
+      //   [0, c[2])  the diagonal and the singles, filtered term by term;
+      //   runs       the spin-0 doubles whose target class is in the pass: for
+      //              the occupied pair op the target class is K_op ^ g(u, v)
+      //              (K_op = class ^ bytes of the pair, g = bytes of the empty
+      //              pair), so it lies in block P0 + j exactly when g >> kb is
+      //              bucket (P0 + j) ^ (K_op >> kb); with the empty pairs sorted
+      //              by bucket, run (op, j) is one contiguous stretch;
+      //   the spin-1 doubles when the determinant's own class is in the pass;
+      //   the opposite-spin blocks of the spin-0 singles whose class is.
+      const unsigned kb = (unsigned)g.cls_k, nb = 256u >> kb, P0 = g.cls_lo >> kb;
+      const unsigned nblk = (g.cls_hi - g.cls_lo) >> kb;
+      const bool own = d.h.acls >= g.cls_lo && d.h.acls < g.cls_hi;
+      const unsigned nv0 = d.h.nv[0], nvp0 = d.h.nvp[0], nop = c2(d.h.na[0]);
+      const unsigned nx = d.h.na[0] * nv0, nsb = d.h.nsb;
+      const unsigned lt = (1u << lane) - 1u;
+      // (1) bucket of every empty spin-0 pair, bucket sizes
+      for (unsigned bk = tid; bk <= nb; bk += GEN_THREADS) cboff[bk] = 0;
+      __syncthreads();
+      for (unsigned q = tid; q < nvp0; q += GEN_THREADS) {
+        unsigned u, v;
+        pair_of(pt, q, u, v);
+        const unsigned bk = (unsigned)(d.hx[u] ^ d.hx[v]) >> kb;  // row 0 of hx: the occupied byte cancels
+        cbq[q] = (unsigned char)bk;
+        atomicAdd(&cboff[bk], 1u);
+      }
+      for (unsigned op = tid; op < nop; op += GEN_THREADS) {
+        unsigned x, y;
+        pair_of(pt, op, x, y);
+        kop[op] = (unsigned char)((d.h.acls ^ d.hx[x * nv0] ^ d.hx[y * nv0]) >> kb);  // the empty byte cancels
+      }
+      __syncthreads();
+      // (2) bucket starts (nb <= 256 <= GEN_THREADS)
+      {
+        uint32_t tot;
+        const uint32_t ex = block_excl_scan<uint32_t, GEN_THREADS>(tid < (int)nb ? cboff[tid] : 0u, &tot, s_scan);
+        if (tid < (int)nb) cboff[tid] = ex;
+        if (tid == 0) cboff[nb] = tot;
+      }
+      __syncthreads();
+      // (3) the empty pairs by bucket, ascending within a bucket (a fixed order:
+      // the count sweep and the generation pass must see the same index space)
+      for (unsigned bk = tid >> 5; bk < nb; bk += GEN_THREADS / 32) {
+        unsigned pos = cboff[bk];
+        const unsigned end = cboff[bk + 1];
+        for (unsigned q0 = 0; q0 < nvp0 && pos < end; q0 += 32) {
+          const unsigned q = q0 + lane;
+          const bool m = q < nvp0 && cbq[q] == bk;
+          const unsigned bal = __ballot_sync(0xffffffffu, m);
+          if (m) cperm[pos + __popc(bal & lt)] = (unsigned short)q;
+          pos += __popc(bal);
         }
       }
-      const unsigned e0 = own ? 2u : 1u, p0 = own ? d.h.c[4] : d.h.c[3];
+      // (4) run starts, op-major
+      const unsigned nrun = nop * nblk;  // <= RUN_CAP (the plan bounds nblk by the occupied pairs)
       unsigned run = 0;
+      for (unsigned r0 = 0; r0 < nrun; r0 += GEN_THREADS) {
+        const unsigned r = r0 + tid;
+        unsigned sz = 0;
+        if (r < nrun) {
+          const unsigned op = r / nblk, j = r - op * nblk, bk = (P0 + j) ^ kop[op];
+          sz = cboff[bk + 1] - cboff[bk];
+        }
+        uint32_t t2;
+        const uint32_t e2 = block_excl_scan<uint32_t, GEN_THREADS>(sz, &t2, s_scan);
+        if (r < nrun) rpre[r] = run + e2;
+        run += t2;
+      }
+      // (5) the tail's blocks
+      const unsigned p0 = d.h.c[2] + run;
+      if (tid == 0) {
+        rpre[nrun] = run;
+        s_n2 = run;
+        if (own) {
+          kst[0] = d.h.c[3];
+          kpr[0] = p0;
+        }
+      }
+      const unsigned e0 = own ? 1u : 0u, p1 = p0 + (own ? d.h.c[4] - d.h.c[3] : 0u);
+      unsigned runk = 0;
       for (unsigned xb = 0; xb < nx; xb += GEN_THREADS) {
         const unsigned x = xb + tid;
         const unsigned cx = x < nx ? (d.h.acls ^ d.hx[x]) : 0u;
-        const bool keep = x < nx && cx >= lo && cx < hi && nsb > 0;
+        const bool keep = x < nx && cx >= g.cls_lo && cx < g.cls_hi && nsb > 0;
         uint32_t tot;
         const uint32_t ex = block_excl_scan<uint32_t, GEN_THREADS>(keep ? 1u : 0u, &tot, s_scan);
         if (keep) {
-          kst[e0 + run + ex] = d.h.c[4] + x * nsb;
-          kpr[e0 + run + ex] = p0 + (run + ex) * nsb;
+          kst[e0 + runk + ex] = d.h.c[4] + x * nsb;
+          kpr[e0 + runk + ex] = p1 + (runk + ex) * nsb;
         }
-        run += tot;
+        runk += tot;
       }
-      if (tid == 0) s_nk = e0 + run;
+      if (tid == 0) s_nk = e0 + runk;
       __syncthreads();
     }
     const DetHead<KT> dh = d.h;
     const unsigned nk = screened ? s_nk : 0u;
-    // screened term index -> full term index: group 0 maps to itself, then a
-    // binary search over the kept groups' screened starts
+    const unsigned n2 = cls_pass ? s_n2 : 0u;
+    const unsigned c_nblk = cls_pass ? (g.cls_hi - g.cls_lo) >> g.cls_k : 1u, c_P0 = g.cls_lo >> g.cls_k;
+    const unsigned c_nrun = cls_pass ? c2(dh.na[0]) * c_nblk : 0u;
+    // screened term index -> full term index: group 0 (the diagonal and the
+    // singles) maps to itself; in a class pass the spin-0 double runs come
+    // next; then a binary search over the kept blocks' screened starts
     auto remap = [&](unsigned l) -> unsigned {
-      if (!screened || l < (cls_pass ? dh.c[3] : dh.c[2])) return l;
+      if (!screened || l < dh.c[2]) return l;
+      if (cls_pass && l - dh.c[2] < n2) {
+        const unsigned r = l - dh.c[2];
+        unsigned lo = 0, hi = c_nrun;  // the last run starting at or before r
+        while (hi - lo > 1) {
+          const unsigned mid = (lo + hi) >> 1;
+          if (rpre[mid] <= r) lo = mid; else hi = mid;
+        }
+        const unsigned op = lo / c_nblk, bk = (c_P0 + (lo - op * c_nblk)) ^ kop[op];
+        return dh.c[2] + op * dh.nvp[0] + cperm[cboff[bk] + (r - rpre[lo])];
+      }
       unsigned lo = 0, hi = nk;
       while (hi - lo > 1) {
         const unsigned mid = (lo + hi) >> 1;
@@ -446,9 +544,10 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
       }
       return kst[lo] + (l - kpr[lo]);
     };
-    // class pass: is the target of (full) term index lf in the pass?
+    // class pass: is the target of (full) term index lf in the pass?  Only the
+    // diagonal and the singles are filtered; everything after was chosen whole
     auto in_pass = [&](unsigned lf) -> bool {
-      if (!cls_pass || lf >= dh.c[3]) return true;  // blocks past c[3] were chosen whole
+      if (!cls_pass || lf >= dh.c[2]) return true;
       const unsigned cl = term_class(dh, d, pt, lf);
       return cl >= g.cls_lo && cl < g.cls_hi;
     };
@@ -1200,7 +1299,7 @@ static HamView ham_view(Ctx& c) {
 template <int W, int MODE>
 static int launch_gen(Ctx& c, const GenArgs<typename KeyOf<W>::T>& g, unsigned grid, unsigned nbp) {
   typedef typename KeyOf<W>::T KT;
-  size_t sm = gen_smem_bytes<KT>(MODE, nbp, g.kl_cap);
+  size_t sm = gen_smem_bytes<KT>(MODE, nbp, g.kl_cap, g.cls_on != 0);
   static size_t configured = 0;
   // opt in whenever the size grows: static shared memory (the projection's
   // per-warp sums) counts against the same 48 KB default
@@ -1299,29 +1398,54 @@ __global__ void __launch_bounds__(256) k_class_hist(const KT* __restrict__ keys,
     if (sh[i]) atomicAdd(hist + i, sh[i]);
 }
 
-// index-space size of every determinant in the class pass [lo, hi): [0, c[3]),
-// the spin-1 doubles when its class is in the pass, and nsb per spin-0 single
-// whose class is (the generator's class-pass index space)
+// index-space size of every determinant in the class pass [lo, hi) of aligned
+// blocks of 2^kb classes (the generator's class-pass index space): [0, c[2]),
+// the spin-0 doubles whose target class is in the pass, the spin-1 doubles
+// when its own class is, and nsb per spin-0 single whose class is
 template <class KT>
 __global__ void __launch_bounds__(256) k_pass_counts(const KT* __restrict__ keys, u64 n, int N, int M, unsigned lo,
-                                                     unsigned hi, u64* __restrict__ cnt) {
+                                                     unsigned hi, int kb, u64* __restrict__ cnt) {
   __shared__ unsigned char s_oc[8][64], s_vc[8][64];
+  __shared__ unsigned s_bc[8][256];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned nb = 256u >> kb, P0 = lo >> kb, nblk = (hi - lo) >> kb;
+  unsigned* bc = s_bc[warp];
   for (u64 j = ((u64)blockIdx.x * blockDim.x + threadIdx.x) >> 5; j < n; j += ((u64)gridDim.x * blockDim.x) >> 5) {
     unsigned na[2], nv[2];
+    const unsigned char* oc = s_oc[warp];
+    const unsigned char* vc = s_vc[warp];
     const unsigned ac = class_lists(keys[j], N, M, s_oc[warp], s_vc[warp], na, nv);
     const u64 nsb = (u64)na[1] * nv[1];
     unsigned kept = 0;
     for (unsigned x = lane; x < na[0] * nv[0]; x += 32) {
       const unsigned ii = x / nv[0], aa = x - ii * nv[0];
-      const unsigned cx = ac ^ s_oc[warp][ii] ^ s_vc[warp][aa];
+      const unsigned cx = ac ^ oc[ii] ^ vc[aa];
       kept += (cx >= lo && cx < hi) ? 1u : 0u;
     }
     kept = warp_sum(kept);
+    // spin-0 doubles: buckets of the empty pairs, then per occupied pair the
+    // buckets its target classes in the pass need
+    for (unsigned bk = lane; bk < nb; bk += 32) bc[bk] = 0;
+    __syncwarp();
+    const unsigned nvp = c2(nv[0]), nop = c2(na[0]);
+    for (unsigned q = lane; q < nvp; q += 32) {
+      unsigned u, v;
+      unrank_pair(q, u, v);
+      atomicAdd(&bc[(unsigned)(vc[u] ^ vc[v]) >> kb], 1u);
+    }
+    __syncwarp();
+    u64 n2 = 0;
+    for (unsigned op = lane; op < nop; op += 32) {
+      unsigned x, y;
+      unrank_pair(op, x, y);
+      const unsigned K = (unsigned)(ac ^ oc[x] ^ oc[y]) >> kb;
+      for (unsigned jb = 0; jb < nblk; ++jb) n2 += bc[(P0 + jb) ^ K];
+    }
+    n2 = warp_sum(n2);
     if (lane == 0) {
-      const u64 c3 = 1ull + (u64)na[0] * nv[0] + nsb + (u64)c2(na[0]) * c2(nv[0]);
+      const u64 cs2 = 1ull + (u64)na[0] * nv[0] + nsb;
       const bool own = ac >= lo && ac < hi;
-      cnt[j] = c3 + (own ? (u64)c2(na[1]) * c2(nv[1]) : 0ull) + (u64)kept * nsb;
+      cnt[j] = cs2 + n2 + (own ? (u64)c2(na[1]) * c2(nv[1]) : 0ull) + (u64)kept * nsb;
     }
     __syncwarp();
   }
@@ -1527,8 +1651,9 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
   }
   const u64 avail = budget / tb;
   struct OuterPass {
-    unsigned lo, hi;  // class range (class passes)
+    unsigned lo, hi;  // class range (class passes): aligned blocks of 2^k classes
     u64 terms;        // terms this outer pass generates
+    int k;
   };
   std::vector<OuterPass> outer;
   bool cls_mode = false;
@@ -1553,22 +1678,43 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
       }
       if (tot != T) return set_error(SFCI_ERR_NUMERIC, "SpMSpV class histogram disagrees with term offsets");
       (void)big;
-      // consecutive classes while they fit one pass; a class larger than a pass
-      // is an outer pass of its own, split further into bin passes that
-      // regenerate that class's terms only
+      // Passes are runs of aligned blocks of 2^kc classes (the generator
+      // enumerates a pass's spin-0 doubles block by block): kc two bits below
+      // the widest block size whose blocks all fit a pass, consecutive blocks
+      // while they fit and while their runs (occupied spin-0 pairs x blocks)
+      // fit the generator's table.  A class larger than a pass is an outer pass
+      // of its own, split further into bin passes that regenerate that class's
+      // terms only.
       cls_mode = true;
+      auto block_sum = [&](unsigned lo, int kb) {
+        u64 t = 0;
+        for (unsigned cc = lo; cc < lo + (1u << kb); ++cc) t += hh[cc];
+        return t;
+      };
+      int kfit = -1;
+      for (int kb = 8; kb >= 0 && kfit < 0; --kb) {
+        bool fits = true;
+        for (unsigned lo = 0; lo < (unsigned)CLS_N && fits; lo += 1u << kb) fits = block_sum(lo, kb) <= cmp.C1;
+        if (fits) kfit = kb;
+      }
+      const int kc = std::max(0, kfit - 2);
+      const unsigned nop_max = std::max(1u, c2((unsigned)std::min(c.ne, c.M)));
+      const unsigned nblk_cap = std::max(1u, (unsigned)RUN_CAP / nop_max);
       unsigned lo = 0;
       while (lo < (unsigned)CLS_N) {
-        unsigned hi = lo + 1;
-        u64 sum = hh[lo];
-        while (hi < (unsigned)CLS_N && sum + hh[hi] <= cmp.C1) sum += hh[hi++];
-        if (sum) outer.push_back({lo, hi, sum});
+        unsigned hi = lo + (1u << kc);
+        u64 sum = block_sum(lo, kc);
+        while (hi < (unsigned)CLS_N && ((hi - lo) >> kc) < nblk_cap && sum + block_sum(hi, kc) <= cmp.C1) {
+          sum += block_sum(hi, kc);
+          hi += 1u << kc;
+        }
+        if (sum) outer.push_back({lo, hi, sum, kc});
         lo = hi;
       }
       cmp.passes = (int)outer.size();
     }
   }
-  if (!cls_mode) outer.push_back({0u, 0u, T});
+  if (!cls_mode) outer.push_back({0u, 0u, T, 0});
   phase_end(c, tok);
   // [0] survivors, [1] distinct, [2] fixed-point range flag
   u64* scount = (u64*)scratch_get(c, "sp_scount", 4 * sizeof(u64));
@@ -1615,7 +1761,7 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
       doffp = (u64*)scratch_get(c, "sp_pdoff", (ns + 1) * sizeof(u64));
       if (!doffp) return SFCI_ERR_NOMEM;
       const unsigned gr = (unsigned)std::min<u64>((ns * 32 + 255) / 256, (u64)c.sm_count * 16);
-      SFCI_LAUNCH(c, k_pass_counts<KT>, gr, 256, 0, src_k, ns, c.N, c.M, opass.lo, opass.hi, doffp);
+      SFCI_LAUNCH(c, k_pass_counts<KT>, gr, 256, 0, src_k, ns, c.N, c.M, opass.lo, opass.hi, opass.k, doffp);
       if ((st = scan_excl(c, doffp, doffp, ns))) return st;
       if ((st = read_words(c, doffp + ns, sizeof(u64), &Tp))) return st;
       phase_end(c, tok);
@@ -1657,6 +1803,7 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
       g.cls_on = 1;
       g.cls_lo = opass.lo;
       g.cls_hi = opass.hi;
+      g.cls_k = opass.k;
       g.kl_cap = 3 + (unsigned)(c.M * c.M / 4);  // [0, c3), spin-1 doubles, na0 * nv0 <= M^2 / 4 blocks
     }
     if ((st = launch_gen<W, M_COUNT>(c, g, G, NB1))) return st;

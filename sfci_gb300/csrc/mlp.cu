@@ -62,15 +62,18 @@ constexpr uint32_t T256_BYTES = HID * TILE * 2;      // 65536: a 256 x 128 trans
 constexpr uint32_t XT_BYTES = KIN * TILE * 2;        // 147456: the 576 x 128 transposed input tile
 constexpr uint32_t MASK_WORDS = TILE * HID / 32;     // relu'(z1) bits of a tile
 constexpr int MAX_SYSTEMS = 64;                      // Hamiltonians one training set may mix
-// inference: layer 1's one-hot inputs (occupancy, p, q, r: rows 0..511 of W1)
-// go through the tensor cores in K chunks of 64 streamed by bulk copies
-constexpr int K1 = 512;                              // one-hot input rows of W1 taken by the MMA
-constexpr int KC = 64;                               // K chunk
-constexpr int NCH = K1 / KC;                         // 8 chunks per tile
-constexpr uint32_t W1C_BYTES = HID * KC * 2;         // 32768: K-major image of a 256 x 64 chunk of W1^T
-constexpr uint32_t AC_BYTES = TILE * KC * 2;         // 16384: a 128 x 64 input chunk
-constexpr uint32_t STAGE_BYTES = W1C_BYTES + AC_BYTES;
-constexpr int INF_STAGES = 2;
+// inference: the one-hot rows p, q, r of W1 (rows 128..511) and all of W2 go
+// through the tensor cores as B operands streamed by bulk copies, in K chunks
+// of 32 through a ring of shared-memory stages
+constexpr int IKC = 32;                              // K chunk
+constexpr int NCH1 = (IN_R + 128 - IN_P) / IKC;      // 12 chunks of W1^T (inputs 128..511)
+constexpr int NCH2 = HID / IKC;                      // 8 chunks of W2
+constexpr int NCHT = NCH1 + NCH2;                    // chunks per tile
+constexpr uint32_t IB_BYTES = HID * IKC * 2;         // 16384: K-major image of a 256 x 32 B chunk
+constexpr uint32_t IA_BYTES = TILE * IKC * 2;        // 8192: a 128 x 32 input chunk
+constexpr uint32_t ISTAGE = IB_BYTES + IA_BYTES;
+constexpr int ISTAGES = 6;
+constexpr int INF_THREADS = 160;                     // four row warps and one copy warp
 
 }  // namespace mlp
 
@@ -256,7 +259,7 @@ struct FwdArgs {
   const __nv_bfloat16* W1b;
   const float* params;   // FP32 masters: b1, b2, w3, b3 read from here
   const uint8_t* W2img;  // K-major image of W2 (B = W2, N = out, K = in)
-  const uint8_t* W1img;  // inference: NCH K-major images of 256 x 64 chunks of W1^T (B = W1^T, N = hidden, K = input)
+  const uint8_t* Wc;     // inference: NCHT K-major 256 x 32 chunks, W1^T rows 128..511 then W2
   unsigned ntiles;
   const u64* tile_start;  // training: first example of each tile (nullptr: tile t starts at 128 t)
   // inference
@@ -480,220 +483,276 @@ __global__ void __launch_bounds__(THREADS, 1) k_mlp_fwd(FwdArgs a) {
 // ---------------------------------------------------------------------------
 // inference: both hidden layers on the tensor cores
 // ---------------------------------------------------------------------------
-// Layer 1's one-hot rows (occupancy bits, p, q, r: W1 rows 0..511) are an MMA
-// of the tile's 0/1 input rows with W1^T, in eight K chunks of 64 that cycle
-// through two shared-memory stages: a bulk copy brings the W1^T chunk while
-// the 128 threads write their rows' input chunk, and one thread issues the
-// chunk's four MMAs into TMEM columns 0..255.  The epilogue adds the rows of
-// b1, the class one-hot and the two scalar features (BF16 weights, FP32
-// values), applies the ReLU and writes the BF16 layer-2 operand over the
-// stages; layer 2 (resident W2 image) accumulates into TMEM columns 256..511;
-// layer 3 and the sigmoid are the last epilogue.  The same function as the
-// training forward (layer1_row), summed in another order.
+// Warps 0-3 hold one group (row) of the tile each thread; warp 4 is a copy
+// warp.  Every tile takes the same 20 B-operand chunks (256 x 32, 16 KB): 12 of
+// W1^T for the one-hot inputs p, q, r (W1 rows 128..511) and 8 of W2, through
+// a ring of 6 stages.  The copy warp streams them ahead of use, across tile
+// boundaries and through the epilogues.  Layer 1: per W1 chunk the row warps
+// write the tile's 0/1 input chunk into the stage and one thread issues its two
+// MMAs into TMEM columns 0..255.  The layer-1 epilogue adds b1, the source's
+// occupancy rows (summed once per source on CUDA cores), the class row and the
+// two scalar rows, applies the ReLU and writes the BF16 layer-2 operand (64 KB);
+// layer 2 accumulates into TMEM columns 256..511; layer 3 and the sigmoid are
+// the last epilogue.  The same function as the training forward (layer1_row),
+// summed in another order.
 //
-// Barrier phases: stage s holds chunks g = s, s + 2, ... of the CTA's chunk
-// sequence; its use u = g / 2 completes `full` (copy landed) and, after the
-// MMAs that read it, `freed` (tcgen05.commit), both with parity u & 1.
+// Barrier phases: chunk g of the CTA's sequence uses stage g % 6; its use
+// u = g / 6 completes `full` (copy landed) and, after the MMAs that read the
+// stage, `freed` (tcgen05.commit), both with parity u & 1.  The row warps sync
+// among themselves on named barrier 1.  Every wait is bounded; a timeout sets
+// a shared flag that both roles poll, and the CTA drains what it started.
+__device__ __forceinline__ void rows_sync() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+// named barrier 1 over the row warps that also ORs a flag across them
+__device__ __forceinline__ bool rows_or(bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "setp.ne.u32 p, %1, 0;\n\t"
+      "bar.red.or.pred q, 1, 128, p;\n\t"
+      "selp.u32 %0, 1, 0, q;\n\t}"
+      : "=r"(r)
+      : "r"((uint32_t)v)
+      : "memory");
+  return r != 0;
+}
+
 template <class KT>
-__global__ void __launch_bounds__(THREADS, 1) k_mlp_infer(FwdArgs a) {
+__global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(FwdArgs a) {
   extern __shared__ __align__(1024) uint8_t smem[];
-  uint8_t* sW2 = smem;                  // 128 KB
-  uint8_t* sStage = smem + W2_BYTES;    // 2 x (32 KB W1^T chunk + 16 KB input chunk)
-  uint8_t* sA2 = sStage;                // layer-2 operand (64 KB) over the stages once layer 1 is done
-  __shared__ __align__(8) uint64_t bar_w2, bar_full[INF_STAGES], bar_free[INF_STAGES], bar_done, bar_fin;
+  uint8_t* sA2 = smem;                                      // 64 KB layer-2 operand
+  uint8_t* sStg = smem + A_BYTES;                           // ISTAGES x (B chunk, input chunk)
+  float* su = reinterpret_cast<float*>(sStg + ISTAGES * ISTAGE);  // [2][256] occupancy sums
+  __shared__ __align__(8) uint64_t bar_full[ISTAGES], bar_free[ISTAGES], bar_done, bar_fin;
   __shared__ uint32_t tmem_slot;
-  __shared__ u64 s_src0;
+  __shared__ u64 s_src[2];
+  __shared__ volatile int s_fail;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid == 0) {
-    umma::mbar_init(&bar_w2, 1);
-    for (int i = 0; i < INF_STAGES; ++i) {
+    for (int i = 0; i < ISTAGES; ++i) {
       umma::mbar_init(&bar_full[i], 1);
       umma::mbar_init(&bar_free[i], 1);
     }
     umma::mbar_init(&bar_done, 1);
     umma::mbar_init(&bar_fin, 1);
     umma::fence_mbar_init();
+    s_fail = 0;
   }
   __syncthreads();
   if (warp == 0) umma::tmem_alloc(&tmem_slot, 512);
-  if (tid == 0) {
-    umma::mbar_arrive_expect_tx(&bar_w2, W2_BYTES);
-    for (uint32_t o = 0; o < W2_BYTES; o += 16384) umma::bulk_g2s(sW2 + o, a.W2img + o, 16384, &bar_w2);
-  }
   umma::tc_fence_before();
   __syncthreads();
   umma::tc_fence_after();
   const uint32_t tmem = tmem_slot;
-  bool failed = __syncthreads_or(!umma::mbar_wait(&bar_w2, 0)) != 0;
-  const float b3 = a.params[OFF_B3];
-  const uint32_t idesc = umma::idesc_bf16_f32(TILE, HID);
-  const uint32_t trow = tmem + ((uint32_t)(32 * warp) << 16);
-  const uint16_t ONE = 0x3f80;  // BF16 1.0
-  uint32_t g = 0;               // chunks this CTA has started
-  uint32_t done_phase = 0;
-  const int N = a.x.N;
-  const u64 nmask0 = N >= 64 ? ~0ull : ((1ull << N) - 1ull);
-  const u64 nmask1 = N >= 128 ? ~0ull : (N > 64 ? ((1ull << (N - 64)) - 1ull) : 0ull);
 
-  for (unsigned t = blockIdx.x; t < a.ntiles && !failed; t += gridDim.x) {
-    const u64 e0 = (u64)t * TILE;
-    const u64 e = e0 + tid;
-    const bool valid = e < a.x.nex;
-    if (tid == 0) s_src0 = source_of(a.x, e0 < a.x.nex ? e0 : a.x.nex - 1);
-    __syncthreads();
-    u64 j = 0;
-    Feat f{};
-    u64 occ[2] = {0ull, 0ull};
-    if (valid) {
-      // sources are in example order: walk forward from the tile's first one
-      j = s_src0;
-      while (j + 1 < a.x.nsrc && __ldg(a.x.goff + j + 1) <= e) ++j;
-      const KT key = load_key<KT>(a.x.keys, j);
-      f = example_feat(a.x, key, a.x.cc[j], (unsigned)(e - a.x.goff[j]) + 1u, j);
-      occ[0] = kword(key, 0) & nmask0;
-      if (sizeof(KT) > 8) occ[1] = kword(key, 1) & nmask1;
-    }
-    // ---- layer 1, one-hot part: NCH chunks through the two stages
-    for (int c = 0; c < NCH && !failed; ++c, ++g) {
-      const uint32_t st = g & 1u, use = g >> 1;
-      uint8_t* sB = sStage + st * STAGE_BYTES;
-      uint8_t* sX = sB + W1C_BYTES;
-      if (use > 0) failed = __syncthreads_or(!umma::mbar_wait(&bar_free[st], (use - 1) & 1u)) != 0;
-      if (failed) break;
-      if (tid == 0) {
-        umma::mbar_arrive_expect_tx(&bar_full[st], W1C_BYTES);
-        const uint8_t* src = a.W1img + (size_t)c * W1C_BYTES;
-        umma::bulk_g2s(sB, src, 16384, &bar_full[st]);
-        umma::bulk_g2s(sB + 16384, src + 16384, 16384, &bar_full[st]);
-      }
-      // this row's 64 inputs of chunk c: occupancy bits (c = 0, 1) or a one-hot index
-      u64 bits = 0;
-      if (valid) {
-        if (c < 2) {
-          bits = occ[c];
-        } else {
-          const int idx = c < 4 ? f.p : (c < 6 ? f.q : f.r);
-          const int lo = 64 * ((c - 2) & 1);
-          if (idx >= lo && idx < lo + 64) bits = 1ull << (idx - lo);
+  if (warp == 4) {
+    // ---- copy warp: the B chunks of every tile, in order, ISTAGES ahead
+    if (lane == 0) {
+      uint32_t g = 0;
+      for (unsigned t = blockIdx.x; t < a.ntiles && !s_fail; t += gridDim.x) {
+        for (int c = 0; c < NCHT; ++c) {
+          const uint32_t st = g % ISTAGES, use = g / ISTAGES;
+          if (use > 0 && !umma::mbar_wait(&bar_free[st], (use - 1) & 1u)) s_fail = 1;
+          if (s_fail) break;
+          umma::mbar_arrive_expect_tx(&bar_full[st], IB_BYTES);
+          umma::bulk_g2s(sStg + st * ISTAGE, a.Wc + (size_t)c * IB_BYTES, IB_BYTES, &bar_full[st]);
+          ++g;
         }
       }
+      // the copies this warp started have landed (the row warps waited for
+      // them already unless a wait timed out)
+      for (uint32_t st = 0; st < (uint32_t)ISTAGES; ++st) {
+        const uint32_t uses = g / ISTAGES + (st < g % ISTAGES ? 1u : 0u);
+        if (uses) umma::mbar_wait(&bar_full[st], (uses - 1) & 1u);
+      }
+    }
+  } else {
+    // ---- row warps
+    const float b3 = a.params[OFF_B3];
+    const uint32_t idesc = umma::idesc_bf16_f32(TILE, HID);
+    const uint32_t trow = tmem + ((uint32_t)(32 * warp) << 16);
+    const uint16_t ONE = 0x3f80;  // BF16 1.0
+    uint32_t g = 0, done_phase = 0;
+    bool fail = false;  // this thread's; every decision takes it through rows_or
+    for (unsigned t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
+      const u64 e0 = (u64)t * TILE;
+      const u64 e = e0 + tid;
+      const bool valid = e < a.x.nex;
+      // the tile's first and last sources: their occupancy sums are shared
+      if (tid == 0) s_src[0] = source_of(a.x, e0 < a.x.nex ? e0 : a.x.nex - 1);
+      if (tid == 1) s_src[1] = source_of(a.x, e0 + TILE - 1 < a.x.nex ? e0 + TILE - 1 : a.x.nex - 1);
+      rows_sync();
+      occ_sum(load_key<KT>(a.x.keys, s_src[0]), a.x.N, a.W1b, su);
+      if (s_src[1] != s_src[0]) occ_sum(load_key<KT>(a.x.keys, s_src[1]), a.x.N, a.W1b, su + HID);
+      u64 j = 0;
+      Feat f{};
+      KT key{};
+      if (valid) {
+        // sources are in example order: walk forward from the tile's first one
+        j = s_src[0];
+        while (j + 1 < a.x.nsrc && __ldg(a.x.goff + j + 1) <= e) ++j;
+        key = load_key<KT>(a.x.keys, j);
+        f = example_feat(a.x, key, a.x.cc[j], (unsigned)(e - a.x.goff[j]) + 1u, j);
+      }
+      // ---- layer 1, one-hot part: NCH1 chunks
+      for (int c = 0; c < NCH1; ++c, ++g) {
+        const uint32_t st = g % ISTAGES, use = g / ISTAGES;
+        uint8_t* sB = sStg + st * ISTAGE;
+        uint8_t* sX = sB + IB_BYTES;
+        if (use > 0 && !umma::mbar_wait(&bar_free[st], (use - 1) & 1u)) fail = true;
+        // this row's 32 inputs of chunk c: p (c < 4), q (c < 8) or r as a one-hot index
+        unsigned bits = 0;
+        if (valid) {
+          const int idx = c < 4 ? f.p : (c < 8 ? f.q : f.r);
+          const int lo = IKC * (c & 3);
+          if (idx >= lo && idx < lo + IKC) bits = 1u << (idx - lo);
+        }
 #pragma unroll
-      for (int q = 0; q < KC / 8; ++q) {
-        const unsigned by = (unsigned)(bits >> (8 * q)) & 0xffu;
-        uint32_t w[4];
+        for (int q = 0; q < IKC / 8; ++q) {
+          const unsigned by = (bits >> (8 * q)) & 0xffu;
+          uint32_t w[4];
 #pragma unroll
-        for (int h = 0; h < 4; ++h)
-          w[h] = ((by >> (2 * h)) & 1u ? ONE : 0u) | (((by >> (2 * h + 1)) & 1u ? ONE : 0u) << 16);
-        *reinterpret_cast<uint4*>(sX + umma::tile_offset(tid, 8 * q, KC)) = make_uint4(w[0], w[1], w[2], w[3]);
+          for (int h = 0; h < 4; ++h)
+            w[h] = ((by >> (2 * h)) & 1u ? ONE : 0u) | (((by >> (2 * h + 1)) & 1u ? ONE : 0u) << 16);
+          *reinterpret_cast<uint4*>(sX + umma::tile_offset(tid, 8 * q, IKC)) = make_uint4(w[0], w[1], w[2], w[3]);
+        }
+        umma::fence_async_smem();
+        umma::tc_fence_before();
+        if (rows_or(fail)) {
+          fail = true;
+          break;
+        }
+        if (tid == 0) {
+          umma::tc_fence_after();
+          if (umma::mbar_wait(&bar_full[st], use & 1u))
+            umma::gemm_tile(tmem, umma::smem_u32(sX), umma::smem_u32(sB), IKC, idesc, c > 0);
+          else
+            fail = true;
+          umma::mma_commit(&bar_free[st]);
+          if (c == NCH1 - 1) umma::mma_commit(&bar_done);
+        }
+      }
+      if (rows_or(fail)) {
+        fail = true;
+        break;
+      }
+      // ---- layer-1 epilogue: + b1 + occupancy + class row + scalar rows, ReLU, BF16
+      if (!umma::mbar_wait(&bar_done, done_phase)) fail = true;
+      done_phase ^= 1u;
+      if (rows_or(fail)) {
+        fail = true;
+        break;
+      }
+      umma::tc_fence_after();
+      {
+        const float* u = su;
+        float ubuf[HID];
+        if (valid && j == s_src[1] && j != s_src[0]) u = su + HID;
+        if (valid && j != s_src[0] && j != s_src[1]) {  // a source strictly inside the tile: its own sum
+          for (int cc = 0; cc < HID; ++cc) ubuf[cc] = 0.f;
+          for (int o = 0; o < a.x.N; ++o)
+            if (key_test(key, o))
+              for (int cc = 0; cc < HID; ++cc) ubuf[cc] += __bfloat162float(a.W1b[(size_t)(IN_OCC + o) * HID + cc]);
+          u = ubuf;
+        }
+        const __nv_bfloat16* rc = a.W1b + (size_t)(IN_CLS + (valid ? f.cls : 0)) * HID;
+        const __nv_bfloat16* rl = a.W1b + (size_t)IN_LC * HID;
+        const __nv_bfloat16* rv = a.W1b + (size_t)IN_LV * HID;
+        const float* b1 = a.params + OFF_B1;
+        for (int k = 0; k < HID / 32; ++k) {
+          float z[32];
+          umma::tmem_ld32(trow + 32 * k, z);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const int c0 = 32 * k + 8 * q;
+            float acc[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) acc[i] = z[8 * q + i] + __ldg(b1 + c0 + i) + u[c0 + i];
+            add_row8(acc, rc + c0, 1.f);
+            add_row8(acc, rl + c0, f.lc);
+            add_row8(acc, rv + c0, f.lv);
+            uint4 o;
+            o.x = pack_bf16(valid ? fmaxf(acc[0], 0.f) : 0.f, valid ? fmaxf(acc[1], 0.f) : 0.f);
+            o.y = pack_bf16(valid ? fmaxf(acc[2], 0.f) : 0.f, valid ? fmaxf(acc[3], 0.f) : 0.f);
+            o.z = pack_bf16(valid ? fmaxf(acc[4], 0.f) : 0.f, valid ? fmaxf(acc[5], 0.f) : 0.f);
+            o.w = pack_bf16(valid ? fmaxf(acc[6], 0.f) : 0.f, valid ? fmaxf(acc[7], 0.f) : 0.f);
+            *reinterpret_cast<uint4*>(sA2 + umma::tile_offset(tid, c0, HID)) = o;
+          }
+        }
       }
       umma::fence_async_smem();
       umma::tc_fence_before();
-      __syncthreads();
+      rows_sync();
+      // ---- layer 2: NCH2 chunks of W2 against the K stripes of the operand
       if (tid == 0) {
         umma::tc_fence_after();
-        if (umma::mbar_wait(&bar_full[st], use & 1u)) {
-          umma::gemm_tile(tmem, umma::smem_u32(sX), umma::smem_u32(sB), KC, idesc, c > 0);
-        } else {
-          failed = true;
+        for (int c = 0; c < NCH2; ++c) {
+          const uint32_t gg = g + (uint32_t)c, st = gg % ISTAGES, use = gg / ISTAGES;
+          if (!fail && umma::mbar_wait(&bar_full[st], use & 1u)) {
+            const uint32_t sB = umma::smem_u32(sStg + st * ISTAGE), sa = umma::smem_u32(sA2);
+#pragma unroll
+            for (int k = 0; k < IKC; k += 16)
+              umma::mma_bf16(tmem + HID, umma::sdesc(sa + ((IKC * c + k) >> 3) * umma::CORE_BYTES, HID),
+                             umma::sdesc(sB + (k >> 3) * umma::CORE_BYTES, IKC), idesc, c > 0 || k > 0);
+          } else {
+            fail = true;
+          }
+          umma::mma_commit(&bar_free[st]);
         }
-        umma::mma_commit(&bar_free[st]);
-        if (c == NCH - 1) umma::mma_commit(&bar_done);
+        umma::mma_commit(&bar_done);
       }
-      failed = __syncthreads_or(failed) != 0;
-    }
-    if (failed) break;
-    // ---- layer-1 epilogue: + b1 + class row + scalar rows, ReLU, BF16 operand of layer 2
-    failed = __syncthreads_or(!umma::mbar_wait(&bar_done, done_phase)) != 0;
-    done_phase ^= 1u;
-    if (failed) break;
-    umma::tc_fence_after();
-    {
-      const __nv_bfloat16* rc = a.W1b + (size_t)(IN_CLS + (valid ? f.cls : 0)) * HID;
-      const __nv_bfloat16* rl = a.W1b + (size_t)IN_LC * HID;
-      const __nv_bfloat16* rv = a.W1b + (size_t)IN_LV * HID;
-      const float* b1 = a.params + OFF_B1;
+      g += NCH2;
+      if (!umma::mbar_wait(&bar_done, done_phase)) fail = true;
+      done_phase ^= 1u;
+      if (rows_or(fail)) {
+        fail = true;
+        break;
+      }
+      umma::tc_fence_after();
+      // ---- layer 3, sigmoid, keep decisions
+      float logit = b3;
       for (int k = 0; k < HID / 32; ++k) {
         float z[32];
-        umma::tmem_ld32(trow + 32 * k, z);
+        umma::tmem_ld32(trow + HID + 32 * k, z);
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int c0 = 32 * k + 8 * q;
-          float acc[8];
-#pragma unroll
-          for (int i = 0; i < 8; ++i) acc[i] = z[8 * q + i] + __ldg(b1 + c0 + i);
-          add_row8(acc, rc + c0, 1.f);
-          add_row8(acc, rl + c0, f.lc);
-          add_row8(acc, rv + c0, f.lv);
-          uint4 o;
-          o.x = pack_bf16(valid ? fmaxf(acc[0], 0.f) : 0.f, valid ? fmaxf(acc[1], 0.f) : 0.f);
-          o.y = pack_bf16(valid ? fmaxf(acc[2], 0.f) : 0.f, valid ? fmaxf(acc[3], 0.f) : 0.f);
-          o.z = pack_bf16(valid ? fmaxf(acc[4], 0.f) : 0.f, valid ? fmaxf(acc[5], 0.f) : 0.f);
-          o.w = pack_bf16(valid ? fmaxf(acc[6], 0.f) : 0.f, valid ? fmaxf(acc[7], 0.f) : 0.f);
-          *reinterpret_cast<uint4*>(sA2 + umma::tile_offset(tid, c0, HID)) = o;
+        for (int i = 0; i < 32; ++i)
+          logit += fmaxf(z[i] + __ldg(a.params + OFF_B2 + 32 * k + i), 0.f) * __ldg(a.params + OFF_W3 + 32 * k + i);
+      }
+      const float p = 1.f / (1.f + __expf(-logit));
+      // the guard keeps every group whose largest possible term, |c_j| times the
+      // group's integral bound, reaches it, whatever the network says
+      const bool kept = valid && (p >= a.thr || 10.f * (f.lc + f.lv) >= a.lguard);
+      const unsigned m = __ballot_sync(0xffffffffu, kept);
+      if (lane == 0 && e0 + 32 * warp < a.x.nex) a.keep[(e0 >> 5) + warp] = m;
+      if (valid && a.prob) a.prob[e] = p;
+      const u64 jj = valid ? j : ~0ull;
+      const unsigned same = __match_any_sync(0xffffffffu, jj);
+      const unsigned nt = kept ? f.gsize : 0u, ng = kept ? 1u : 0u;
+      if (a.all_terms) {
+        const unsigned at = warp_sum(valid ? f.gsize : 0u);
+        if (lane == 0 && at) atomicAdd(a.all_terms, (u64)at);
+      }
+      if (same == 0xffffffffu) {
+        const unsigned sm_ = warp_sum(nt), sg = warp_sum(ng);
+        if (lane == 0 && valid && sm_) {
+          atomicAdd(a.kept_terms + j, (u64)sm_);
+          atomicAdd(a.kept_groups + j, (u64)sg);
         }
+      } else if (valid && kept) {
+        atomicAdd(a.kept_terms + j, (u64)nt);
+        atomicAdd(a.kept_groups + j, (u64)ng);
       }
-    }
-    umma::fence_async_smem();
-    umma::tc_fence_before();
-    __syncthreads();
-    if (tid == 0) {
+      umma::tc_fence_before();
+      rows_sync();  // the operand, the occupancy sums and TMEM are rewritten by the next tile
       umma::tc_fence_after();
-      umma::gemm_tile(tmem + HID, umma::smem_u32(sA2), umma::smem_u32(sW2), HID, idesc, false);
-      umma::mma_commit(&bar_done);
     }
-    failed = __syncthreads_or(!umma::mbar_wait(&bar_done, done_phase)) != 0;
-    done_phase ^= 1u;
-    if (failed) break;
-    umma::tc_fence_after();
-    // ---- layer 3, sigmoid, keep decisions
-    float logit = b3;
-    for (int k = 0; k < HID / 32; ++k) {
-      float z[32];
-      umma::tmem_ld32(trow + HID + 32 * k, z);
-#pragma unroll
-      for (int i = 0; i < 32; ++i)
-        logit += fmaxf(z[i] + __ldg(a.params + OFF_B2 + 32 * k + i), 0.f) * __ldg(a.params + OFF_W3 + 32 * k + i);
-    }
-    const float p = 1.f / (1.f + __expf(-logit));
-    // the guard keeps every group whose largest possible term, |c_j| times the
-    // group's integral bound, reaches it, whatever the network says
-    const bool kept = valid && (p >= a.thr || 10.f * (f.lc + f.lv) >= a.lguard);
-    const unsigned m = __ballot_sync(0xffffffffu, kept);
-    if (lane == 0 && e0 + 32 * warp < a.x.nex) a.keep[(e0 >> 5) + warp] = m;
-    if (valid && a.prob) a.prob[e] = p;
-    const u64 jj = valid ? j : ~0ull;
-    const unsigned same = __match_any_sync(0xffffffffu, jj);
-    const unsigned nt = kept ? f.gsize : 0u, ng = kept ? 1u : 0u;
-    if (a.all_terms) {
-      const unsigned at = warp_sum(valid ? f.gsize : 0u);
-      if (lane == 0 && at) atomicAdd(a.all_terms, (u64)at);
-    }
-    if (same == 0xffffffffu) {
-      const unsigned st = warp_sum(nt), sg = warp_sum(ng);
-      if (lane == 0 && valid && st) {
-        atomicAdd(a.kept_terms + j, (u64)st);
-        atomicAdd(a.kept_groups + j, (u64)sg);
+    if (fail) {
+      s_fail = 1;  // stops the copy warp
+      if (tid == 0) {
+        atomicOr(a.err, 1u);
+        umma::mma_commit(&bar_fin);  // arrives once every MMA issued before has completed
+        umma::mbar_wait(&bar_fin, 0);
       }
-    } else if (valid && kept) {
-      atomicAdd(a.kept_terms + j, (u64)nt);
-      atomicAdd(a.kept_groups + j, (u64)ng);
     }
-    umma::tc_fence_before();
-    __syncthreads();  // the stages and TMEM are rewritten by the next tile
-    umma::tc_fence_after();
-  }
-  if (failed) {
-    // let the copies and MMAs this CTA started finish before its shared memory
-    // and TMEM go away (each wait bounded as well)
-    if (tid == 0) {
-      atomicOr(a.err, 1u);
-      umma::mma_commit(&bar_fin);  // arrives once every MMA issued before has completed
-    }
-    for (int i = 0; i < INF_STAGES; ++i) {
-      const uint32_t uses = (g + (uint32_t)(INF_STAGES - 1 - i)) / INF_STAGES;  // stage i got uses 0 .. uses-1
-      if (uses) umma::mbar_wait(&bar_full[i], (uses - 1) & 1u);
-    }
-    umma::mbar_wait(&bar_fin, 0);
   }
   umma::tc_fence_before();
   __syncthreads();
@@ -896,24 +955,29 @@ __global__ void k_mlp_adam(float* p, const float* g, float* m, float* v, size_t 
   }
 }
 
-__global__ void k_mlp_images(const float* p, __nv_bfloat16* W1b, uint8_t* W2img, uint8_t* W2Timg, uint8_t* W1img) {
+__global__ void k_mlp_images(const float* p, __nv_bfloat16* W1b, uint8_t* W2img, uint8_t* W2Timg, uint8_t* Wc) {
   const size_t n1 = (size_t)KIN * HID;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n1 + (size_t)HID * HID;
        i += (size_t)gridDim.x * blockDim.x) {
     if (i < n1) {
       const __nv_bfloat16 w = __float2bfloat16(p[OFF_W1 + i]);
       W1b[i] = w;
-      // W1 row `in` (an input), column `h` (a hidden unit): element (h, in % KC)
-      // of chunk in / KC of the K-major W1^T images
+      // W1 row `in` (an input), column `h` (a hidden unit): element (h, in % IKC)
+      // of the inference chunk (in - IN_P) / IKC
       const unsigned in = (unsigned)(i / HID), h = (unsigned)(i % HID);
-      if (in < (unsigned)K1)
-        *reinterpret_cast<__nv_bfloat16*>(W1img + (size_t)(in / KC) * W1C_BYTES + umma::tile_offset(h, in % KC, KC)) = w;
+      if (in >= (unsigned)IN_P && in < (unsigned)(IN_P + NCH1 * IKC)) {
+        const unsigned r = in - IN_P;
+        *reinterpret_cast<__nv_bfloat16*>(Wc + (size_t)(r / IKC) * IB_BYTES + umma::tile_offset(h, r % IKC, IKC)) = w;
+      }
     } else {
       const size_t k = i - n1;
       const unsigned o = (unsigned)(k / HID), in = (unsigned)(k % HID);
       const __nv_bfloat16 w = __float2bfloat16(p[OFF_W2 + k]);
       *reinterpret_cast<__nv_bfloat16*>(W2img + umma::tile_offset(o, in, HID)) = w;
       *reinterpret_cast<__nv_bfloat16*>(W2Timg + umma::tile_offset(in, o, HID)) = w;
+      // inference chunk NCH1 + in / IKC: element (o, in % IKC)
+      *reinterpret_cast<__nv_bfloat16*>(Wc + (size_t)(NCH1 + in / IKC) * IB_BYTES +
+                                        umma::tile_offset(o, in % IKC, IKC)) = w;
     }
   }
 }
@@ -951,7 +1015,7 @@ struct Screen {
   __nv_bfloat16* W1b = nullptr;
   uint8_t* W2img = nullptr;
   uint8_t* W2Timg = nullptr;
-  uint8_t* W1img = nullptr;  // NCH chunks of W1^T for the inference MMAs
+  uint8_t* Wc = nullptr;     // NCHT B-operand chunks of the inference MMAs
   float* vmax = nullptr;     // this context's table (system 0)
   std::vector<float*> vmaxs;  // one per logged system; [0] = vmax
   float** d_vmaxs = nullptr;  // device copy of the pointers
@@ -1002,12 +1066,12 @@ static double gauss(uint64_t& x) {
 
 static int screen_images(Screen& s) {
   Ctx& c = s.ctx[0];
-  SFCI_LAUNCH(c, k_mlp_images, c.sm_count * 4, 256, 0, (const float*)s.params, s.W1b, s.W2img, s.W2Timg, s.W1img);
+  SFCI_LAUNCH(c, k_mlp_images, c.sm_count * 4, 256, 0, (const float*)s.params, s.W1b, s.W2img, s.W2Timg, s.Wc);
   return SFCI_OK;
 }
 
 static int fwd_smem_bytes() { return (int)(W2_BYTES + A_BYTES + 6 * HID * sizeof(float)); }
-static int infer_smem_bytes() { return (int)(W2_BYTES + INF_STAGES * STAGE_BYTES); }
+static int infer_smem_bytes() { return (int)(A_BYTES + ISTAGES * ISTAGE + 2 * HID * sizeof(float)); }
 static int bwd_smem_bytes() { return (int)(W2_BYTES + A_BYTES + HID * sizeof(float)); }
 static int grad_smem_bytes() { return (int)(2 * T256_BYTES); }
 
@@ -1034,11 +1098,11 @@ static int screen_init(Screen& s, uint64_t seed) {
   s.grads = s.params + NPARAM;
   s.am = s.grads + NPARAM;
   s.av = s.am + NPARAM;
-  if ((st = dev_alloc(s, &p, (size_t)KIN * HID * 2 + 2 * (size_t)W2_BYTES + (size_t)NCH * W1C_BYTES))) return st;
+  if ((st = dev_alloc(s, &p, (size_t)KIN * HID * 2 + 2 * (size_t)W2_BYTES + (size_t)NCHT * IB_BYTES))) return st;
   s.W1b = (__nv_bfloat16*)p;
   s.W2img = (uint8_t*)p + (size_t)KIN * HID * 2;
   s.W2Timg = s.W2img + W2_BYTES;
-  s.W1img = s.W2Timg + W2_BYTES;
+  s.Wc = s.W2Timg + W2_BYTES;
   if ((st = dev_alloc(s, &p, (size_t)4 * c.P * c.M * sizeof(float)))) return st;
   s.vmax = (float*)p;
   s.vmaxs.push_back(s.vmax);
@@ -1119,7 +1183,7 @@ static int screen_infer(Ctx& c, Screen& s, const u64* keys, const double* amps, 
   a.W1b = s.W1b;
   a.params = s.params;
   a.W2img = s.W2img;
-  a.W1img = s.W1img;
+  a.Wc = s.Wc;
   a.ntiles = ntiles;
   a.thr = (float)thr;
   a.lguard = guard > 0.0 ? (float)std::log10(guard) : INFINITY;
@@ -1132,9 +1196,9 @@ static int screen_infer(Ctx& c, Screen& s, const u64* keys, const double* amps, 
   if (ntiles) {
     const unsigned grid = std::min<unsigned>(ntiles, (unsigned)c.sm_count);
     if (c.W == 1)
-      SFCI_LAUNCH(c, k_mlp_infer<u64>, grid, THREADS, infer_smem_bytes(), a);
+      SFCI_LAUNCH(c, k_mlp_infer<u64>, grid, INF_THREADS, infer_smem_bytes(), a);
     else
-      SFCI_LAUNCH(c, k_mlp_infer<K128>, grid, THREADS, infer_smem_bytes(), a);
+      SFCI_LAUNCH(c, k_mlp_infer<K128>, grid, INF_THREADS, infer_smem_bytes(), a);
   }
   *goff_out = goff;
   *keep_out = keep;

@@ -73,7 +73,8 @@ constexpr uint32_t IB_BYTES = HID * IKC * 2;         // 16384: K-major image of 
 constexpr uint32_t IA_BYTES = TILE * IKC * 2;        // 8192: a 128 x 32 input chunk
 constexpr uint32_t ISTAGE = IB_BYTES + IA_BYTES;
 constexpr int ISTAGES = 6;
-constexpr int INF_THREADS = 160;                     // four row warps and one copy warp
+constexpr int ROW_THREADS = 256;                     // inference: 8 row warps, two per row quarter of TMEM lanes
+constexpr int INF_THREADS = ROW_THREADS + 32;        // and one copy warp
 
 }  // namespace mlp
 
@@ -483,45 +484,64 @@ __global__ void __launch_bounds__(THREADS, 1) k_mlp_fwd(FwdArgs a) {
 // ---------------------------------------------------------------------------
 // inference: both hidden layers on the tensor cores
 // ---------------------------------------------------------------------------
-// Warps 0-3 hold one group (row) of the tile each thread; warp 4 is a copy
-// warp.  Every tile takes the same 20 B-operand chunks (256 x 32, 16 KB): 12 of
-// W1^T for the one-hot inputs p, q, r (W1 rows 128..511) and 8 of W2, through
-// a ring of 6 stages.  The copy warp streams them ahead of use, across tile
-// boundaries and through the epilogues.  Layer 1: per W1 chunk the row warps
-// write the tile's 0/1 input chunk into the stage and one thread issues its two
-// MMAs into TMEM columns 0..255.  The layer-1 epilogue adds b1, the source's
-// occupancy rows (summed once per source on CUDA cores), the class row and the
-// two scalar rows, applies the ReLU and writes the BF16 layer-2 operand (64 KB);
-// layer 2 accumulates into TMEM columns 256..511; layer 3 and the sigmoid are
-// the last epilogue.  The same function as the training forward (layer1_row),
-// summed in another order.
+// Warps 0-7 are row warps: warp w holds rows 32 (w % 4) .. + 31 of the tile
+// (the TMEM lane quarter it may read) and the column half w / 4 of every
+// 256-wide epilogue, so two warps share each row and each scheduler has two.
+// Warp 8 is a copy warp.  Every tile takes the same 20 B-operand chunks (256 x
+// 32, 16 KB): 12 of W1^T for the one-hot inputs p, q, r (W1 rows 128..511) and
+// 8 of W2, through a ring of 6 stages; the copy warp streams them ahead of use,
+// across tile boundaries and through the epilogues.  Layer 1: per W1 chunk the
+// row warps write the tile's 0/1 input chunk into the stage and one thread
+// issues its two MMAs into TMEM columns 0..255.  The layer-1 epilogue adds the
+// source's bias (b1 plus its occupancy rows, summed once per source), the class
+// row and the two scalar rows (kept in shared memory as FP32 copies of the BF16
+// weights), applies the ReLU and writes the BF16 layer-2 operand (64 KB); layer
+// 2 accumulates into TMEM columns 256..511; layer 3 and the sigmoid are the last
+// epilogue, its two column halves added through shared memory.  The same
+// function as the training forward (layer1_row), summed in another order.
 //
 // Barrier phases: chunk g of the CTA's sequence uses stage g % 6; its use
 // u = g / 6 completes `full` (copy landed) and, after the MMAs that read the
 // stage, `freed` (tcgen05.commit), both with parity u & 1.  The row warps sync
-// among themselves on named barrier 1.  Every wait is bounded; a timeout sets
-// a shared flag that both roles poll, and the CTA drains what it started.
-__device__ __forceinline__ void rows_sync() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+// among themselves on named barrier 1 and vote on failures with bar.red.or, so
+// every branch is uniform; every mbarrier wait is bounded.
+__device__ __forceinline__ void rows_sync() { asm volatile("bar.sync 1, %0;" ::"r"(ROW_THREADS) : "memory"); }
 // named barrier 1 over the row warps that also ORs a flag across them
 __device__ __forceinline__ bool rows_or(bool v) {
   uint32_t r;
   asm volatile(
       "{\n\t.reg .pred p, q;\n\t"
       "setp.ne.u32 p, %1, 0;\n\t"
-      "bar.red.or.pred q, 1, 128, p;\n\t"
+      "bar.red.or.pred q, 1, %2, p;\n\t"
       "selp.u32 %0, 1, 0, q;\n\t}"
       : "=r"(r)
-      : "r"((uint32_t)v)
+      : "r"((uint32_t)v), "r"(ROW_THREADS)
       : "memory");
   return r != 0;
+}
+
+// b1 plus the occupancy rows of a key, column c of 256 (one column per thread)
+template <class KT>
+__device__ __forceinline__ float src_bias(const KT& key, int N, const __nv_bfloat16* __restrict__ W1b,
+                                          const float* __restrict__ b1, int c) {
+  float s = __ldg(b1 + c);
+  for (int o = 0; o < N; ++o)
+    if (key_test(key, o)) s += __bfloat162float(W1b[(size_t)(IN_OCC + o) * HID + c]);
+  return s;
 }
 
 template <class KT>
 __global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(FwdArgs a) {
   extern __shared__ __align__(1024) uint8_t smem[];
-  uint8_t* sA2 = smem;                                      // 64 KB layer-2 operand
-  uint8_t* sStg = smem + A_BYTES;                           // ISTAGES x (B chunk, input chunk)
-  float* su = reinterpret_cast<float*>(sStg + ISTAGES * ISTAGE);  // [2][256] occupancy sums
+  uint8_t* sA2 = smem;                                                  // 64 KB layer-2 operand
+  uint8_t* sStg = smem + A_BYTES;                                       // ISTAGES x (B chunk, input chunk)
+  float* sbias = reinterpret_cast<float*>(sStg + ISTAGES * ISTAGE);     // [2][256] per-source bias
+  float* scls = sbias + 2 * HID;                                        // [4][256] class rows
+  float* slc = scls + 4 * HID;                                          // [256] log|c| row
+  float* slv = slc + HID;                                               // [256] log bound row
+  float* sb2 = slv + HID;                                               // [256]
+  float* sw3 = sb2 + HID;                                               // [256]
+  float* slog = sw3 + HID;                                              // [128] second-half logits
   __shared__ __align__(8) uint64_t bar_full[ISTAGES], bar_free[ISTAGES], bar_done, bar_fin;
   __shared__ uint32_t tmem_slot;
   __shared__ u64 s_src[2];
@@ -537,6 +557,13 @@ __global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(FwdArgs a) {
     umma::fence_mbar_init();
     s_fail = 0;
   }
+  for (int i = tid; i < HID; i += INF_THREADS) {
+    for (int k = 0; k < 4; ++k) scls[k * HID + i] = __bfloat162float(a.W1b[(size_t)(IN_CLS + k) * HID + i]);
+    slc[i] = __bfloat162float(a.W1b[(size_t)IN_LC * HID + i]);
+    slv[i] = __bfloat162float(a.W1b[(size_t)IN_LV * HID + i]);
+    sb2[i] = a.params[OFF_B2 + i];
+    sw3[i] = a.params[OFF_W3 + i];
+  }
   __syncthreads();
   if (warp == 0) umma::tmem_alloc(&tmem_slot, 512);
   umma::tc_fence_before();
@@ -544,7 +571,7 @@ __global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(FwdArgs a) {
   umma::tc_fence_after();
   const uint32_t tmem = tmem_slot;
 
-  if (warp == 4) {
+  if (warp == ROW_THREADS / 32) {
     // ---- copy warp: the B chunks of every tile, in order, ISTAGES ahead
     if (lane == 0) {
       uint32_t g = 0;
@@ -567,22 +594,25 @@ __global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(FwdArgs a) {
     }
   } else {
     // ---- row warps
+    const int row = 32 * (warp & 3) + lane, half = warp >> 2, c0h = 128 * half;
     const float b3 = a.params[OFF_B3];
     const uint32_t idesc = umma::idesc_bf16_f32(TILE, HID);
-    const uint32_t trow = tmem + ((uint32_t)(32 * warp) << 16);
+    const uint32_t trow = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
     const uint16_t ONE = 0x3f80;  // BF16 1.0
     uint32_t g = 0, done_phase = 0;
     bool fail = false;  // this thread's; every decision takes it through rows_or
     for (unsigned t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
       const u64 e0 = (u64)t * TILE;
-      const u64 e = e0 + tid;
+      const u64 e = e0 + row;
       const bool valid = e < a.x.nex;
-      // the tile's first and last sources: their occupancy sums are shared
+      // the tile's first and last sources: their biases are shared
       if (tid == 0) s_src[0] = source_of(a.x, e0 < a.x.nex ? e0 : a.x.nex - 1);
       if (tid == 1) s_src[1] = source_of(a.x, e0 + TILE - 1 < a.x.nex ? e0 + TILE - 1 : a.x.nex - 1);
       rows_sync();
-      occ_sum(load_key<KT>(a.x.keys, s_src[0]), a.x.N, a.W1b, su);
-      if (s_src[1] != s_src[0]) occ_sum(load_key<KT>(a.x.keys, s_src[1]), a.x.N, a.W1b, su + HID);
+      sbias[tid] = src_bias(load_key<KT>(a.x.keys, s_src[0]), a.x.N, a.W1b, a.params + OFF_B1, tid);
+      sbias[HID + tid] = s_src[1] != s_src[0]
+                             ? src_bias(load_key<KT>(a.x.keys, s_src[1]), a.x.N, a.W1b, a.params + OFF_B1, tid)
+                             : sbias[tid];
       u64 j = 0;
       Feat f{};
       KT key{};
@@ -599,7 +629,8 @@ __global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(FwdArgs a) {
         uint8_t* sB = sStg + st * ISTAGE;
         uint8_t* sX = sB + IB_BYTES;
         if (use > 0 && !umma::mbar_wait(&bar_free[st], (use - 1) & 1u)) fail = true;
-        // this row's 32 inputs of chunk c: p (c < 4), q (c < 8) or r as a one-hot index
+        // this row's 32 inputs of chunk c: p (c < 4), q (c < 8) or r as a one-hot
+        // index; each of the row's two threads writes 16 of them
         unsigned bits = 0;
         if (valid) {
           const int idx = c < 4 ? f.p : (c < 8 ? f.q : f.r);
@@ -607,13 +638,14 @@ __global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(FwdArgs a) {
           if (idx >= lo && idx < lo + IKC) bits = 1u << (idx - lo);
         }
 #pragma unroll
-        for (int q = 0; q < IKC / 8; ++q) {
+        for (int qq = 0; qq < IKC / 16; ++qq) {
+          const int q = 2 * half + qq;
           const unsigned by = (bits >> (8 * q)) & 0xffu;
           uint32_t w[4];
 #pragma unroll
           for (int h = 0; h < 4; ++h)
             w[h] = ((by >> (2 * h)) & 1u ? ONE : 0u) | (((by >> (2 * h + 1)) & 1u ? ONE : 0u) << 16);
-          *reinterpret_cast<uint4*>(sX + umma::tile_offset(tid, 8 * q, IKC)) = make_uint4(w[0], w[1], w[2], w[3]);
+          *reinterpret_cast<uint4*>(sX + umma::tile_offset(row, 8 * q, IKC)) = make_uint4(w[0], w[1], w[2], w[3]);
         }
         umma::fence_async_smem();
         umma::tc_fence_before();
@@ -635,7 +667,7 @@ __global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(FwdArgs a) {
         fail = true;
         break;
       }
-      // ---- layer-1 epilogue: + b1 + occupancy + class row + scalar rows, ReLU, BF16
+      // ---- layer-1 epilogue, this thread's 128 columns
       if (!umma::mbar_wait(&bar_done, done_phase)) fail = true;
       done_phase ^= 1u;
       if (rows_or(fail)) {
@@ -644,38 +676,33 @@ __global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(FwdArgs a) {
       }
       umma::tc_fence_after();
       {
-        const float* u = su;
-        float ubuf[HID];
-        if (valid && j == s_src[1] && j != s_src[0]) u = su + HID;
-        if (valid && j != s_src[0] && j != s_src[1]) {  // a source strictly inside the tile: its own sum
-          for (int cc = 0; cc < HID; ++cc) ubuf[cc] = 0.f;
-          for (int o = 0; o < a.x.N; ++o)
-            if (key_test(key, o))
-              for (int cc = 0; cc < HID; ++cc) ubuf[cc] += __bfloat162float(a.W1b[(size_t)(IN_OCC + o) * HID + cc]);
-          u = ubuf;
+        const float* u = sbias;
+        float ubuf[HID / 2];
+        if (valid && j == s_src[1] && j != s_src[0]) u = sbias + HID;
+        if (valid && j != s_src[0] && j != s_src[1]) {  // a source strictly inside the tile: its own bias
+          for (int cc = 0; cc < HID / 2; ++cc) ubuf[cc] = src_bias(key, a.x.N, a.W1b, a.params + OFF_B1, c0h + cc);
+          u = ubuf - c0h;
         }
-        const __nv_bfloat16* rc = a.W1b + (size_t)(IN_CLS + (valid ? f.cls : 0)) * HID;
-        const __nv_bfloat16* rl = a.W1b + (size_t)IN_LC * HID;
-        const __nv_bfloat16* rv = a.W1b + (size_t)IN_LV * HID;
-        const float* b1 = a.params + OFF_B1;
-        for (int k = 0; k < HID / 32; ++k) {
+        const float* rc = scls + (valid ? f.cls : 0) * HID;
+        for (int k = 0; k < HID / 64; ++k) {
+          const int cb = c0h + 32 * k;
           float z[32];
-          umma::tmem_ld32(trow + 32 * k, z);
+          umma::tmem_ld32(trow + cb, z);
 #pragma unroll
           for (int q = 0; q < 4; ++q) {
-            const int c0 = 32 * k + 8 * q;
-            float acc[8];
+            const int c8 = cb + 8 * q;
+            float h[8];
 #pragma unroll
-            for (int i = 0; i < 8; ++i) acc[i] = z[8 * q + i] + __ldg(b1 + c0 + i) + u[c0 + i];
-            add_row8(acc, rc + c0, 1.f);
-            add_row8(acc, rl + c0, f.lc);
-            add_row8(acc, rv + c0, f.lv);
+            for (int i = 0; i < 8; ++i) {
+              const float x = z[8 * q + i] + u[c8 + i] + rc[c8 + i] + f.lc * slc[c8 + i] + f.lv * slv[c8 + i];
+              h[i] = valid ? fmaxf(x, 0.f) : 0.f;
+            }
             uint4 o;
-            o.x = pack_bf16(valid ? fmaxf(acc[0], 0.f) : 0.f, valid ? fmaxf(acc[1], 0.f) : 0.f);
-            o.y = pack_bf16(valid ? fmaxf(acc[2], 0.f) : 0.f, valid ? fmaxf(acc[3], 0.f) : 0.f);
-            o.z = pack_bf16(valid ? fmaxf(acc[4], 0.f) : 0.f, valid ? fmaxf(acc[5], 0.f) : 0.f);
-            o.w = pack_bf16(valid ? fmaxf(acc[6], 0.f) : 0.f, valid ? fmaxf(acc[7], 0.f) : 0.f);
-            *reinterpret_cast<uint4*>(sA2 + umma::tile_offset(tid, c0, HID)) = o;
+            o.x = pack_bf16(h[0], h[1]);
+            o.y = pack_bf16(h[2], h[3]);
+            o.z = pack_bf16(h[4], h[5]);
+            o.w = pack_bf16(h[6], h[7]);
+            *reinterpret_cast<uint4*>(sA2 + umma::tile_offset(row, c8, HID)) = o;
           }
         }
       }
@@ -708,41 +735,46 @@ __global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(FwdArgs a) {
         break;
       }
       umma::tc_fence_after();
-      // ---- layer 3, sigmoid, keep decisions
-      float logit = b3;
-      for (int k = 0; k < HID / 32; ++k) {
+      // ---- layer 3: each half's 128 columns, the second half's sum through shared memory
+      float logit = 0.f;
+      for (int k = 0; k < HID / 64; ++k) {
+        const int cb = c0h + 32 * k;
         float z[32];
-        umma::tmem_ld32(trow + HID + 32 * k, z);
+        umma::tmem_ld32(trow + HID + cb, z);
 #pragma unroll
-        for (int i = 0; i < 32; ++i)
-          logit += fmaxf(z[i] + __ldg(a.params + OFF_B2 + 32 * k + i), 0.f) * __ldg(a.params + OFF_W3 + 32 * k + i);
+        for (int i = 0; i < 32; ++i) logit += fmaxf(z[i] + sb2[cb + i], 0.f) * sw3[cb + i];
       }
-      const float p = 1.f / (1.f + __expf(-logit));
-      // the guard keeps every group whose largest possible term, |c_j| times the
-      // group's integral bound, reaches it, whatever the network says
-      const bool kept = valid && (p >= a.thr || 10.f * (f.lc + f.lv) >= a.lguard);
-      const unsigned m = __ballot_sync(0xffffffffu, kept);
-      if (lane == 0 && e0 + 32 * warp < a.x.nex) a.keep[(e0 >> 5) + warp] = m;
-      if (valid && a.prob) a.prob[e] = p;
-      const u64 jj = valid ? j : ~0ull;
-      const unsigned same = __match_any_sync(0xffffffffu, jj);
-      const unsigned nt = kept ? f.gsize : 0u, ng = kept ? 1u : 0u;
-      if (a.all_terms) {
-        const unsigned at = warp_sum(valid ? f.gsize : 0u);
-        if (lane == 0 && at) atomicAdd(a.all_terms, (u64)at);
-      }
-      if (same == 0xffffffffu) {
-        const unsigned sm_ = warp_sum(nt), sg = warp_sum(ng);
-        if (lane == 0 && valid && sm_) {
-          atomicAdd(a.kept_terms + j, (u64)sm_);
-          atomicAdd(a.kept_groups + j, (u64)sg);
+      if (half) slog[row] = logit;
+      rows_sync();
+      if (!half) {
+        logit += slog[row] + b3;
+        const float p = 1.f / (1.f + __expf(-logit));
+        // the guard keeps every group whose largest possible term, |c_j| times
+        // the group's integral bound, reaches it, whatever the network says
+        const bool kept = valid && (p >= a.thr || 10.f * (f.lc + f.lv) >= a.lguard);
+        const unsigned m = __ballot_sync(0xffffffffu, kept);
+        if (lane == 0 && e0 + 32 * warp < a.x.nex) a.keep[(e0 >> 5) + warp] = m;
+        if (valid && a.prob) a.prob[e] = p;
+        const u64 jj = valid ? j : ~0ull;
+        const unsigned same = __match_any_sync(0xffffffffu, jj);
+        const unsigned nt = kept ? f.gsize : 0u, ng = kept ? 1u : 0u;
+        if (a.all_terms) {
+          const unsigned at = warp_sum(valid ? f.gsize : 0u);
+          if (lane == 0 && at) atomicAdd(a.all_terms, (u64)at);
         }
-      } else if (valid && kept) {
-        atomicAdd(a.kept_terms + j, (u64)nt);
-        atomicAdd(a.kept_groups + j, (u64)ng);
+        if (same == 0xffffffffu) {
+          const unsigned sm_ = warp_sum(nt), sg = warp_sum(ng);
+          if (lane == 0 && valid && sm_) {
+            atomicAdd(a.kept_terms + j, (u64)sm_);
+            atomicAdd(a.kept_groups + j, (u64)sg);
+          }
+        } else if (valid && kept) {
+          atomicAdd(a.kept_terms + j, (u64)nt);
+          atomicAdd(a.kept_groups + j, (u64)ng);
+        }
       }
       umma::tc_fence_before();
-      rows_sync();  // the operand, the occupancy sums and TMEM are rewritten by the next tile
+      rows_sync();  // the operand, the biases, the logits and TMEM are rewritten by the next tile
       umma::tc_fence_after();
     }
     if (fail) {
@@ -1071,7 +1103,7 @@ static int screen_images(Screen& s) {
 }
 
 static int fwd_smem_bytes() { return (int)(W2_BYTES + A_BYTES + 6 * HID * sizeof(float)); }
-static int infer_smem_bytes() { return (int)(A_BYTES + ISTAGES * ISTAGE + 2 * HID * sizeof(float)); }
+static int infer_smem_bytes() { return (int)(A_BYTES + ISTAGES * ISTAGE + (10 * HID + TILE) * sizeof(float)); }
 static int bwd_smem_bytes() { return (int)(W2_BYTES + A_BYTES + HID * sizeof(float)); }
 static int grad_smem_bytes() { return (int)(2 * T256_BYTES); }
 

@@ -1679,7 +1679,7 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
       if (tot != T) return set_error(SFCI_ERR_NUMERIC, "SpMSpV class histogram disagrees with term offsets");
       (void)big;
       // Passes are runs of aligned blocks of 2^kc classes (the generator
-      // enumerates a pass's spin-0 doubles block by block): kc two bits below
+      // enumerates a pass's spin-0 doubles block by block): kc three bits below
       // the widest block size whose blocks all fit a pass, consecutive blocks
       // while they fit and while their runs (occupied spin-0 pairs x blocks)
       // fit the generator's table.  A class larger than a pass is an outer pass
@@ -1697,7 +1697,7 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
         for (unsigned lo = 0; lo < (unsigned)CLS_N && fits; lo += 1u << kb) fits = block_sum(lo, kb) <= cmp.C1;
         if (fits) kfit = kb;
       }
-      const int kc = std::max(0, kfit - 2);
+      const int kc = std::max(0, kfit - 3);
       const unsigned nop_max = std::max(1u, c2((unsigned)std::min(c.ne, c.M)));
       const unsigned nblk_cap = std::max(1u, (unsigned)RUN_CAP / nop_max);
       unsigned lo = 0;

@@ -669,9 +669,10 @@ def run_mlp(args):
     """Throughput of the screen's tensor-core kernels on the 56-spin-orbital
     system: inference over every term group of a Krylov vector's top
     --mlp-sources determinants (1,870 groups each), and Adam training steps on
-    the groups' labels.  Tensor FLOPs: 2 x 256 x 256 per group for inference;
-    per training example the forward and backward 256 x 256 products and the
-    weight-gradient products of both layers (2 x 256 x (256 + 256 + 576))."""
+    the groups' labels.  Tensor FLOPs as the MMAs execute them: per group for
+    inference 2 x 256 x (384 + 256) (layer 1's one-hot p, q, r rows and layer
+    2); per training example the forward and backward 256 x 256 products and
+    the weight-gradient products of both layers (2 x 256 x (256 + 256 + 576))."""
     import sfci_gb300 as sg
     sg.load_library()
     sysd = SYSTEMS[1]
@@ -697,7 +698,7 @@ def run_mlp(args):
     scr.train(steps, batch_tiles=args.mlp_batch_tiles, lr=1e-3)
     t_tr = (time.perf_counter() - t0) / steps
     B = args.mlp_batch_tiles * 128
-    f_inf = 2.0 * 256 * 256 * groups
+    f_inf = 2.0 * 256 * (384 + 256) * groups
     f_tr = 2.0 * 256 * (256 + 256 + 256 + 576) * B
     peak = None
     try:

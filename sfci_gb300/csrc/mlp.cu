@@ -261,6 +261,7 @@ struct FwdArgs {
   const float* params;   // FP32 masters: b1, b2, w3, b3 read from here
   const uint8_t* W2img;  // K-major image of W2 (B = W2, N = out, K = in)
   const uint8_t* Wc;     // inference: NCHT K-major 256 x 32 chunks, W1^T rows 128..511 then W2
+  const u64* tile_src;   // inference: sources of each tile's first and last example
   unsigned ntiles;
   const u64* tile_start;  // training: first example of each tile (nullptr: tile t starts at 128 t)
   // inference
@@ -481,6 +482,16 @@ __global__ void __launch_bounds__(THREADS, 1) k_mlp_fwd(FwdArgs a) {
   if (warp == 0) umma::tmem_dealloc(tmem, 256);
 }
 
+// sources of the first and last example of every inference tile (one binary
+// search per tile, all tiles in parallel)
+__global__ void k_tile_src(ExView x, unsigned ntiles, u64* __restrict__ out) {
+  for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < ntiles; t += gridDim.x * blockDim.x) {
+    const u64 e0 = (u64)t * TILE, e1 = e0 + TILE - 1;
+    out[2 * t] = source_of(x, e0 < x.nex ? e0 : x.nex - 1);
+    out[2 * t + 1] = source_of(x, e1 < x.nex ? e1 : x.nex - 1);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // inference: both hidden layers on the tensor cores
 // ---------------------------------------------------------------------------
@@ -606,8 +617,7 @@ __global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(FwdArgs a) {
       const u64 e = e0 + row;
       const bool valid = e < a.x.nex;
       // the tile's first and last sources: their biases are shared
-      if (tid == 0) s_src[0] = source_of(a.x, e0 < a.x.nex ? e0 : a.x.nex - 1);
-      if (tid == 1) s_src[1] = source_of(a.x, e0 + TILE - 1 < a.x.nex ? e0 + TILE - 1 : a.x.nex - 1);
+      if (tid < 2) s_src[tid] = __ldg(a.tile_src + 2 * t + tid);
       rows_sync();
       sbias[tid] = src_bias(load_key<KT>(a.x.keys, s_src[0]), a.x.N, a.W1b, a.params + OFF_B1, tid);
       sbias[HID + tid] = s_src[1] != s_src[0]
@@ -1206,7 +1216,8 @@ static int screen_infer(Ctx& c, Screen& s, const u64* keys, const double* amps, 
   const unsigned ntiles = (unsigned)((nex + TILE - 1) / TILE);
   uint32_t* keep = (uint32_t*)scratch_get(c, "sc_keep", ((size_t)ntiles * TILE / 32 + 1) * sizeof(uint32_t));
   u64* kt = (u64*)scratch_get(c, "sc_kterms", (2 * (n + 1) + 1) * sizeof(u64));
-  if (!keep || !kt) return SFCI_ERR_NOMEM;
+  u64* tsrc = (u64*)scratch_get(c, "sc_tsrc", (2 * (size_t)ntiles + 2) * sizeof(u64));
+  if (!keep || !kt || !tsrc) return SFCI_ERR_NOMEM;
   u64* kg = kt + (n + 1);
   u64* allt = kg + (n + 1);
   SFCI_CUDA(cudaMemsetAsync(kt, 0, (2 * (n + 1) + 1) * sizeof(u64), c.stream));
@@ -1216,6 +1227,7 @@ static int screen_infer(Ctx& c, Screen& s, const u64* keys, const double* amps, 
   a.params = s.params;
   a.W2img = s.W2img;
   a.Wc = s.Wc;
+  a.tile_src = tsrc;
   a.ntiles = ntiles;
   a.thr = (float)thr;
   a.lguard = guard > 0.0 ? (float)std::log10(guard) : INFINITY;
@@ -1226,6 +1238,8 @@ static int screen_infer(Ctx& c, Screen& s, const u64* keys, const double* amps, 
   a.prob = prob;
   a.err = s.err;
   if (ntiles) {
+    SFCI_LAUNCH(c, k_tile_src, std::min<unsigned>((ntiles + 255) / 256, (unsigned)c.sm_count * 4), 256, 0, a.x,
+                ntiles, tsrc);
     const unsigned grid = std::min<unsigned>(ntiles, (unsigned)c.sm_count);
     if (c.W == 1)
       SFCI_LAUNCH(c, k_mlp_infer<u64>, grid, INF_THREADS, infer_smem_bytes(), a);

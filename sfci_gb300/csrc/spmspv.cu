@@ -260,7 +260,7 @@ struct GenArgs {
 // bucket, and the bucket starts
 __host__ __device__ inline size_t cls_smem_bytes() {
   return al16(sizeof(uint32_t) * (RUN_CAP + 1)) + al16(CP_MAX) + al16(sizeof(unsigned short) * CP_MAX) + al16(CP_MAX) +
-         al16(sizeof(uint32_t) * 257);
+         2 * al16(sizeof(uint32_t) * 257);
 }
 
 template <class KT>
@@ -311,7 +311,8 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
   unsigned char* kop = smem + off + al16(sizeof(uint32_t) * (RUN_CAP + 1));
   unsigned short* cperm = reinterpret_cast<unsigned short*>(kop + al16(CP_MAX));
   unsigned char* cbq = reinterpret_cast<unsigned char*>(cperm) + al16(sizeof(unsigned short) * CP_MAX);
-  uint32_t* cboff = reinterpret_cast<uint32_t*>(cbq + al16(CP_MAX));
+  uint32_t* cbcnt = reinterpret_cast<uint32_t*>(cbq + al16(CP_MAX));  // bucket sizes
+  uint32_t* cboff = cbcnt + al16(sizeof(uint32_t) * 257) / sizeof(uint32_t);  // bucket starts
   __shared__ unsigned s_nk, s_n2;
   __shared__ u64 s_det;
   __shared__ unsigned s_nsq;
@@ -419,6 +420,8 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
     }
     __syncthreads();
     if (det < g.nmain) det_fill_singles(d, tid, GEN_THREADS);  // (term 0 needs no tables)
+    if (cls_pass)
+      for (unsigned bk = tid; bk <= (256u >> g.cls_k); bk += GEN_THREADS) cbcnt[bk] = 0;
     __syncthreads();
     if (cls_pass) {
       // The pass owns the aligned class blocks P0 .. P0 + nblk - 1 (of 2^kb
@@ -437,34 +440,92 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
       const bool own = d.h.acls >= g.cls_lo && d.h.acls < g.cls_hi;
       const unsigned nv0 = d.h.nv[0], nvp0 = d.h.nvp[0], nop = c2(d.h.na[0]);
       const unsigned nx = d.h.na[0] * nv0, nsb = d.h.nsb;
-      const unsigned lt = (1u << lane) - 1u;
-      // (1) bucket of every empty spin-0 pair, bucket sizes
-      for (unsigned bk = tid; bk <= nb; bk += GEN_THREADS) cboff[bk] = 0;
-      __syncthreads();
+      const unsigned lt = (1u << lane) - 1u, warp = tid >> 5;
+      const unsigned nrun = nop * nblk;  // <= RUN_CAP (the plan bounds nblk by the occupied pairs)
+      // Three barriers: (1) bucket sizes and K_op >> kb (all threads), the tail
+      // block list (the last warp); (2) bucket starts (warp 0) and run starts
+      // (warp 1), both warp scans; (3) the empty pairs by bucket (all warps).
       for (unsigned q = tid; q < nvp0; q += GEN_THREADS) {
         unsigned u, v;
         pair_of(pt, q, u, v);
         const unsigned bk = (unsigned)(d.hx[u] ^ d.hx[v]) >> kb;  // row 0 of hx: the occupied byte cancels
         cbq[q] = (unsigned char)bk;
-        atomicAdd(&cboff[bk], 1u);
+        atomicAdd(&cbcnt[bk], 1u);
       }
       for (unsigned op = tid; op < nop; op += GEN_THREADS) {
         unsigned x, y;
         pair_of(pt, op, x, y);
         kop[op] = (unsigned char)((d.h.acls ^ d.hx[x * nv0] ^ d.hx[y * nv0]) >> kb);  // the empty byte cancels
       }
-      __syncthreads();
-      // (2) bucket starts (nb <= 256 <= GEN_THREADS)
-      {
-        uint32_t tot;
-        const uint32_t ex = block_excl_scan<uint32_t, GEN_THREADS>(tid < (int)nb ? cboff[tid] : 0u, &tot, s_scan);
-        if (tid < (int)nb) cboff[tid] = ex;
-        if (tid == 0) cboff[nb] = tot;
+      if (warp == GEN_THREADS / 32 - 1) {
+        // the tail's blocks, screened starts relative to the tail: the spin-1
+        // doubles when the determinant's own class is in the pass, then the
+        // opposite-spin blocks of the spin-0 singles whose class is
+        const unsigned e0 = own ? 1u : 0u, r1 = own ? d.h.c[4] - d.h.c[3] : 0u;
+        if (lane == 0 && own) {
+          kst[0] = d.h.c[3];
+          kpr[0] = 0;
+        }
+        unsigned runk = 0;
+        for (unsigned xb = 0; xb < nx; xb += 32) {
+          const unsigned x = xb + lane;
+          const unsigned cx = x < nx ? (d.h.acls ^ d.hx[x]) : 0u;
+          const bool keep = x < nx && cx >= g.cls_lo && cx < g.cls_hi && nsb > 0;
+          const unsigned bal = __ballot_sync(0xffffffffu, keep);
+          if (keep) {
+            const unsigned r = runk + __popc(bal & lt);
+            kst[e0 + r] = d.h.c[4] + x * nsb;
+            kpr[e0 + r] = r1 + r * nsb;
+          }
+          runk += __popc(bal);
+        }
+        if (lane == 0) s_nk = e0 + runk;
       }
       __syncthreads();
-      // (3) the empty pairs by bucket, ascending within a bucket (a fixed order:
-      // the count sweep and the generation pass must see the same index space)
-      for (unsigned bk = tid >> 5; bk < nb; bk += GEN_THREADS / 32) {
+      if (warp == 0) {
+        // bucket starts
+        unsigned carry = 0;
+        for (unsigned b0 = 0; b0 < nb; b0 += 32) {
+          const unsigned bk = b0 + lane;
+          const unsigned v = bk < nb ? cbcnt[bk] : 0u;
+          unsigned x = v;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+          }
+          if (bk < nb) cboff[bk] = carry + x - v;
+          carry += __shfl_sync(0xffffffffu, x, 31);
+        }
+        if (lane == 0) cboff[nb] = carry;
+      } else if (warp == 1) {
+        // run starts, op-major: run (op, j) holds the empty pairs of bucket (P0 + j) ^ kop[op]
+        unsigned carry = 0;
+        for (unsigned r0 = 0; r0 < nrun; r0 += 32) {
+          const unsigned r = r0 + lane;
+          unsigned v = 0;
+          if (r < nrun) {
+            const unsigned op = r / nblk, j = r - op * nblk;
+            v = cbcnt[(P0 + j) ^ kop[op]];
+          }
+          unsigned x = v;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+          }
+          if (r < nrun) rpre[r] = carry + x - v;
+          carry += __shfl_sync(0xffffffffu, x, 31);
+        }
+        if (lane == 0) {
+          rpre[nrun] = carry;
+          s_n2 = carry;
+        }
+      }
+      __syncthreads();
+      // the empty pairs by bucket, ascending within a bucket (a fixed order: the
+      // count sweep and the generation pass must see the same index space)
+      for (unsigned bk = warp; bk < nb; bk += GEN_THREADS / 32) {
         unsigned pos = cboff[bk];
         const unsigned end = cboff[bk + 1];
         for (unsigned q0 = 0; q0 < nvp0 && pos < end; q0 += 32) {
@@ -475,46 +536,6 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
           pos += __popc(bal);
         }
       }
-      // (4) run starts, op-major
-      const unsigned nrun = nop * nblk;  // <= RUN_CAP (the plan bounds nblk by the occupied pairs)
-      unsigned run = 0;
-      for (unsigned r0 = 0; r0 < nrun; r0 += GEN_THREADS) {
-        const unsigned r = r0 + tid;
-        unsigned sz = 0;
-        if (r < nrun) {
-          const unsigned op = r / nblk, j = r - op * nblk, bk = (P0 + j) ^ kop[op];
-          sz = cboff[bk + 1] - cboff[bk];
-        }
-        uint32_t t2;
-        const uint32_t e2 = block_excl_scan<uint32_t, GEN_THREADS>(sz, &t2, s_scan);
-        if (r < nrun) rpre[r] = run + e2;
-        run += t2;
-      }
-      // (5) the tail's blocks
-      const unsigned p0 = d.h.c[2] + run;
-      if (tid == 0) {
-        rpre[nrun] = run;
-        s_n2 = run;
-        if (own) {
-          kst[0] = d.h.c[3];
-          kpr[0] = p0;
-        }
-      }
-      const unsigned e0 = own ? 1u : 0u, p1 = p0 + (own ? d.h.c[4] - d.h.c[3] : 0u);
-      unsigned runk = 0;
-      for (unsigned xb = 0; xb < nx; xb += GEN_THREADS) {
-        const unsigned x = xb + tid;
-        const unsigned cx = x < nx ? (d.h.acls ^ d.hx[x]) : 0u;
-        const bool keep = x < nx && cx >= g.cls_lo && cx < g.cls_hi && nsb > 0;
-        uint32_t tot;
-        const uint32_t ex = block_excl_scan<uint32_t, GEN_THREADS>(keep ? 1u : 0u, &tot, s_scan);
-        if (keep) {
-          kst[e0 + runk + ex] = d.h.c[4] + x * nsb;
-          kpr[e0 + runk + ex] = p1 + (runk + ex) * nsb;
-        }
-        runk += tot;
-      }
-      if (tid == 0) s_nk = e0 + runk;
       __syncthreads();
     }
     const DetHead<KT> dh = d.h;
@@ -527,15 +548,18 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
     // next; then a binary search over the kept blocks' screened starts
     auto remap = [&](unsigned l) -> unsigned {
       if (!screened || l < dh.c[2]) return l;
-      if (cls_pass && l - dh.c[2] < n2) {
+      if (cls_pass) {
         const unsigned r = l - dh.c[2];
-        unsigned lo = 0, hi = c_nrun;  // the last run starting at or before r
-        while (hi - lo > 1) {
-          const unsigned mid = (lo + hi) >> 1;
-          if (rpre[mid] <= r) lo = mid; else hi = mid;
+        if (r < n2) {
+          unsigned lo = 0, hi = c_nrun;  // the last run starting at or before r
+          while (hi - lo > 1) {
+            const unsigned mid = (lo + hi) >> 1;
+            if (rpre[mid] <= r) lo = mid; else hi = mid;
+          }
+          const unsigned op = lo / c_nblk, bk = (c_P0 + (lo - op * c_nblk)) ^ kop[op];
+          return dh.c[2] + op * dh.nvp[0] + cperm[cboff[bk] + (r - rpre[lo])];
         }
-        const unsigned op = lo / c_nblk, bk = (c_P0 + (lo - op * c_nblk)) ^ kop[op];
-        return dh.c[2] + op * dh.nvp[0] + cperm[cboff[bk] + (r - rpre[lo])];
+        l = r - n2;  // the tail's blocks have screened starts relative to the tail
       }
       unsigned lo = 0, hi = nk;
       while (hi - lo > 1) {

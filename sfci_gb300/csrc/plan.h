@@ -32,13 +32,13 @@ inline int plan_passes(const std::vector<plan_u64>& binoff, unsigned nb1, plan_u
 // buffer and the survivors (cap = output capacity, at most T).  Every generation
 // pass regenerates all T terms, so the plan takes the fewest passes first; among
 // plans with that many, the largest level-2 groups (fewer, fuller partition and
-// merge launches: 1/16 to 1/64 of the budget, at least 2^20 terms).  Without
+// merge launches: 1/16 to 1/128 of the budget, at least 2^20 terms).  Without
 // partition levels the level-2 buffer is one group buffer of 1/6 of the budget.
 // false: the budget cannot hold a single level-1 bin.
 inline bool plan_memory(const std::vector<plan_u64>& binoff, unsigned nb1, plan_u64 T, plan_u64 avail, plan_u64 cap,
                         plan_u64 maxbin, bool partition, MemPlan& out) {
   out = MemPlan();
-  for (const int div : {6, 16, 24, 32, 48, 64}) {
+  for (const int div : {6, 16, 24, 32, 48, 64, 96, 128}) {
     if (partition == (div == 6)) continue;
     const plan_u64 share = partition ? std::max<plan_u64>(avail / div, 1ull << 20) : avail / div;
     const plan_u64 c2 = std::max<plan_u64>(maxbin, std::min<plan_u64>(T, share));

@@ -327,15 +327,27 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
   if (MODE == M_SCATTER)
     for (unsigned b = tid; b < nbp; b += GEN_THREADS)
       cur[b] = g.basem[(u64)(g.bin_lo + b) * G + blockIdx.x] - g.pass_base;
-  u64 t0 = (u64)((unsigned __int128)g.T * blockIdx.x / G);
-  u64 t1 = (u64)((unsigned __int128)g.T * (blockIdx.x + 1) / G);
-  if (tid == 0 && t0 < t1) {
-    u64 lo = 0, hi = g.ndet;  // largest i with doff[i] <= t0
-    while (hi - lo > 1) {
-      u64 mid = (lo + hi) >> 1;
-      if (g.doff[mid] <= t0) lo = mid; else hi = mid;
+  // Each CTA owns a slice of the term index space: an even share of it, or, in
+  // a class pass, whole determinants (an even share of them), so that the order
+  // of a determinant's terms never decides which CTA counts and writes them.
+  u64 t0, t1;
+  if (g.cls_on) {
+    const u64 d0 = (u64)((unsigned __int128)g.nmain * blockIdx.x / G);
+    const u64 d1 = (u64)((unsigned __int128)g.nmain * (blockIdx.x + 1) / G);
+    t0 = g.doff[d0];
+    t1 = g.doff[d1];
+    if (tid == 0) s_det = d0;
+  } else {
+    t0 = (u64)((unsigned __int128)g.T * blockIdx.x / G);
+    t1 = (u64)((unsigned __int128)g.T * (blockIdx.x + 1) / G);
+    if (tid == 0 && t0 < t1) {
+      u64 lo = 0, hi = g.ndet;  // largest i with doff[i] <= t0
+      while (hi - lo > 1) {
+        u64 mid = (lo + hi) >> 1;
+        if (g.doff[mid] <= t0) lo = mid; else hi = mid;
+      }
+      s_det = lo;
     }
-    s_det = lo;
   }
   __syncthreads();
   double eacc = 0.0;
@@ -444,7 +456,7 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
       const unsigned nrun = nop * nblk;  // <= RUN_CAP (the plan bounds nblk by the occupied pairs)
       // Three barriers: (1) bucket sizes and K_op >> kb (all threads), the tail
       // block list (the last warp); (2) bucket starts (warp 0) and run starts
-      // (warp 1), both warp scans; (3) the empty pairs by bucket (all warps).
+      // (warp 1), both warp scans; (3) the empty pairs by bucket (all threads).
       for (unsigned q = tid; q < nvp0; q += GEN_THREADS) {
         unsigned u, v;
         pair_of(pt, q, u, v);
@@ -523,18 +535,13 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
         }
       }
       __syncthreads();
-      // the empty pairs by bucket, ascending within a bucket (a fixed order: the
-      // count sweep and the generation pass must see the same index space)
-      for (unsigned bk = warp; bk < nb; bk += GEN_THREADS / 32) {
-        unsigned pos = cboff[bk];
-        const unsigned end = cboff[bk + 1];
-        for (unsigned q0 = 0; q0 < nvp0 && pos < end; q0 += 32) {
-          const unsigned q = q0 + lane;
-          const bool m = q < nvp0 && cbq[q] == bk;
-          const unsigned bal = __ballot_sync(0xffffffffu, m);
-          if (m) cperm[pos + __popc(bal & lt)] = (unsigned short)q;
-          pos += __popc(bal);
-        }
+      // the empty pairs by bucket, in any order within a bucket: a CTA owns
+      // whole determinants in a class pass, so the order decides nothing that
+      // the count sweep and the generation pass could disagree on (the bucket
+      // sizes count down to zero, ready for the next determinant)
+      for (unsigned q = tid; q < nvp0; q += GEN_THREADS) {
+        const unsigned bk = cbq[q];
+        cperm[cboff[bk] + atomicSub(&cbcnt[bk], 1u) - 1u] = (unsigned short)q;
       }
       __syncthreads();
     }
@@ -1670,7 +1677,7 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
     // offsets and cursors, boundaries and overflow lists (24 B), the input
     // grouped by leaf, and a margin for the small tables
     const size_t reserve = ((size_t)24 << leaf_bits(T)) + (size_t)ns * tb + ((size_t)256 << 20);
-    const size_t pool = (size_t)((freeb + held) * 0.88);
+    const size_t pool = (size_t)((freeb + held) * 0.90);
     budget = c.opts.mem_budget ? (size_t)c.opts.mem_budget : (pool > reserve ? pool - reserve : 0);
   }
   const u64 avail = budget / tb;

@@ -1677,7 +1677,9 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
     // offsets and cursors, boundaries and overflow lists (24 B), the input
     // grouped by leaf, and a margin for the small tables
     const size_t reserve = ((size_t)24 << leaf_bits(T)) + (size_t)ns * tb + ((size_t)256 << 20);
-    const size_t pool = (size_t)((freeb + held) * 0.90);
+    // a batched context's driver keeps growing per-instance vectors between
+    // products, so its products leave it a larger margin
+    const size_t pool = (size_t)((freeb + held) * (c.ninst ? 0.85 : 0.90));
     budget = c.opts.mem_budget ? (size_t)c.opts.mem_budget : (pool > reserve ? pool - reserve : 0);
   }
   const u64 avail = budget / tb;

@@ -538,9 +538,10 @@ def _krylov_input(sg, ctx, sysd, nd, cap=HPSI_CAP):
 def run_screen(args):
     """Screen study: labels from plain products on 112-spin-orbital, 18-electron
     synthetic RHF systems of seeds 6-9, Adam training of the MLP on them, then the
-    truncated Lanczos driver on the seed-5 system with and without the screen.
-    The energy of every run is judged by the unscreened calc_energy of its final
-    vector; the screened run is accepted when it is within tol of the plain one."""
+    truncated Lanczos driver on the seed-5 system with and without the screen
+    (threshold, guard, and floor at the labels' minimum term).  The energy of
+    every run is judged by the unscreened calc_energy of its final vector; a
+    screened run is accepted when it is within tol of the plain one."""
     import sfci_gb300 as sg
     sg.load_library()
     M, NE = 56, 18
@@ -596,8 +597,8 @@ def run_screen(args):
     scr_e.set_params(params)
     runs = []
 
-    def lanczos(thr, guard=0.0):
-        ev.set_screen(None if thr is None else scr_e, 0.0 if thr is None else thr, guard)
+    def lanczos(thr, guard=0.0, floor=0.0):
+        ev.set_screen(None if thr is None else scr_e, 0.0 if thr is None else thr, guard, floor)
         st0 = ev.screen_stats()
         v = ev.vec(args.screen_nd)
         v.upload(hf_key(sysd), np.array([1.0]))
@@ -607,7 +608,8 @@ def run_screen(args):
         tb = time.perf_counter()
         st1 = ev.screen_stats()
         d = {k: st1[k] - st0[k] for k in st1}
-        return {"threshold": thr, "guard": guard, "seconds": tb - ta, "gsaes_energy": float(en[0]), "energy": fe,
+        return {"threshold": thr, "guard": guard, "floor": floor, "seconds": tb - ta, "gsaes_energy": float(en[0]),
+                "energy": fe,
                 "kept_group_fraction": d["kept_groups"] / d["groups"] if d["groups"] else 1.0,
                 "skipped_term_fraction": 1.0 - d["kept_terms"] / d["all_terms"] if d["all_terms"] else 0.0,
                 "products": d["products"], "kept_terms": d["kept_terms"], "all_double_terms": d["all_terms"]}
@@ -617,9 +619,11 @@ def run_screen(args):
     C = connected_per_det(M, NE // 2, NE // 2)
     runs.append(plain)
     best = None
-    for thr, guard in [(t, 0.0) for t in args.screen_thresholds] + \
-            [(args.screen_thresholds[0], gd) for gd in args.screen_guards]:
-        r = lanczos(thr, guard)
+    t0_ = args.screen_thresholds[0]
+    grid = [(t, 0.0, 0.0) for t in args.screen_thresholds] + [(t0_, gd, 0.0) for gd in args.screen_guards] + \
+        [(t0_, gd, args.screen_min_term) for gd in args.screen_guards if gd > args.screen_min_term]
+    for thr, guard, floor in grid:
+        r = lanczos(thr, guard, floor)
         r["dE"] = r["energy"] - plain["energy"]
         runs.append(r)
         if abs(r["dE"]) <= args.screen_tol and (best is None or r["seconds"] < best["seconds"]):
@@ -857,9 +861,10 @@ def main():
     ap.add_argument("--screen-seed", type=int, default=5)
     ap.add_argument("--screen-tol", type=float, default=1e-5)
     ap.add_argument("--screen-min-term", type=float, default=1e-8)
-    ap.add_argument("--screen-thresholds", type=float, nargs="+", default=[0.01, 0.05])
-    ap.add_argument("--screen-guards", type=float, nargs="*", default=[1e-5, 1e-6, 1e-7, 1e-8],
-                    help="guards tried with the first threshold: groups with |c_j| max|V| >= guard always kept")
+    ap.add_argument("--screen-thresholds", type=float, nargs="+", default=[0.01])
+    ap.add_argument("--screen-guards", type=float, nargs="*", default=[1e-5, 1e-6, 1e-7],
+                    help="guards tried with the first threshold: groups with |c_j| max|V| >= guard always kept; "
+                         "each is tried again with the floor at the labels' minimum term")
     ap.add_argument("--batch", action="store_true",
                     help="batched bond-stretch curve: 32 instances, batched vs unbatched Lanczos")
     ap.add_argument("--batch-scale", type=float, default=0.01,

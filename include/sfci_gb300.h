@@ -312,6 +312,11 @@ int sfci_ctx_set_screen(sfci_ctx* ctx, sfci_screen* s, double threshold);
  * (the default).  As the guard goes to 0+ the screened product becomes the
  * plain one. */
 int sfci_ctx_set_screen_guard(sfci_ctx* ctx, double guard);
+/* Floor of the context's screened products: a group whose largest possible
+ * term is below `floor` is skipped without running the network (0 switches it
+ * off, the default).  With the floor at the training labels' minimum term
+ * (sfci_screen_log's min_term) it skips only groups the labels call dead. */
+int sfci_ctx_set_screen_floor(sfci_ctx* ctx, double floor_);
 /* groups seen, groups kept, terms kept, screened products, terms of all groups,
  * since the context was made (five counters) */
 int sfci_ctx_screen_stats(const sfci_ctx* ctx, uint64_t* out5);

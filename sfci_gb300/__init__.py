@@ -115,6 +115,7 @@ def _sigs(L):
     L.sfci_screen_grads.argtypes = [_vp, _vp, C.c_uint64]
     L.sfci_ctx_set_screen.argtypes = [_vp, _vp, C.c_double]
     L.sfci_ctx_set_screen_guard.argtypes = [_vp, C.c_double]
+    L.sfci_ctx_set_screen_floor.argtypes = [_vp, C.c_double]
     L.sfci_ctx_screen_stats.argtypes = [_vp, _u64p]
     return L
 
@@ -139,7 +140,7 @@ def load_library(path: str | None = None, build: bool = True):
                "sfci_add_two", "sfci_add_three", "sfci_shrink_from", "sfci_combine", "sfci_lanczos_ground",
                "sfci_minres", "sfci_gsaes", "sfci_cisd", "sfci_fci", "sfci_spmspv_linear", "sfci_res_norm",
                "sfci_krylov_linear", "sfci_shift_invert", "sfci_screen_create", "sfci_screen_train",
-               "sfci_ctx_set_screen", "sfci_ctx_set_screen_guard"):
+               "sfci_ctx_set_screen", "sfci_ctx_set_screen_guard", "sfci_ctx_set_screen_floor"):
         getattr(L, fn)
     _LIB = _sigs(L)
     return _LIB
@@ -465,11 +466,13 @@ class Context:
         return dict(zip(names, [int(x) for x in a]))
 
     # learned excitation screen
-    def set_screen(self, screen: "Screen | None", threshold: float = 0.5, guard: float = 0.0):
+    def set_screen(self, screen: "Screen | None", threshold: float = 0.5, guard: float = 0.0, floor: float = 0.0):
         """Screen this context's products (None: plain products).  A group whose
-        largest possible term |c_j| * max|V| reaches `guard` is always kept (0: no guard)."""
+        largest possible term |c_j| * max|V| reaches `guard` is always kept, one
+        below `floor` is skipped without the network (0: neither)."""
         _check(self.L.sfci_ctx_set_screen(self.h, screen.h if screen is not None else None, float(threshold)))
         _check(self.L.sfci_ctx_set_screen_guard(self.h, float(guard)))
+        _check(self.L.sfci_ctx_set_screen_floor(self.h, float(floor)))
         self._screen = screen
 
     def screen_stats(self) -> dict:

@@ -83,6 +83,7 @@ struct Ctx {
   std::set<struct Screen*> screens;
   double screen_thr = 0.5;
   double screen_guard = 0.0;  // a group whose term bound |c_j| * max|V| reaches this is always kept (0: off)
+  double screen_floor = 0.0;  // a group whose term bound is below this is skipped without the network (0: off)
   uint64_t screen_stats[5] = {};  // groups, kept groups, kept terms, screened products, terms of all groups
 };
 

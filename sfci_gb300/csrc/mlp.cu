@@ -62,11 +62,11 @@ constexpr uint32_t T256_BYTES = HID * TILE * 2;      // 65536: a 256 x 128 trans
 constexpr uint32_t XT_BYTES = KIN * TILE * 2;        // 147456: the 576 x 128 transposed input tile
 constexpr uint32_t MASK_WORDS = TILE * HID / 32;     // relu'(z1) bits of a tile
 constexpr int MAX_SYSTEMS = 64;                      // Hamiltonians one training set may mix
-// inference: the one-hot rows p, q, r of W1 (rows 128..511) and all of W2 go
-// through the tensor cores as B operands streamed by bulk copies, in K chunks
-// of 32 through a ring of shared-memory stages
+// inference: the 0/1 rows of W1 (occupancy, p, q, r: rows 0..511) and all of
+// W2 go through the tensor cores as B operands streamed by bulk copies, in K
+// chunks of 32 through a ring of shared-memory stages
 constexpr int IKC = 32;                              // K chunk
-constexpr int NCH1 = (IN_R + 128 - IN_P) / IKC;      // 12 chunks of W1^T (inputs 128..511)
+constexpr int NCH1 = (IN_R + 128 - IN_OCC) / IKC;    // 16 chunks of W1^T (inputs 0..511: occupancy, p, q, r)
 constexpr int NCH2 = HID / IKC;                      // 8 chunks of W2
 constexpr int NCHT = NCH1 + NCH2;                    // chunks per tile
 constexpr uint32_t IB_BYTES = HID * IKC * 2;         // 16384: K-major image of a 256 x 32 B chunk
@@ -260,13 +260,16 @@ struct FwdArgs {
   const __nv_bfloat16* W1b;
   const float* params;   // FP32 masters: b1, b2, w3, b3 read from here
   const uint8_t* W2img;  // K-major image of W2 (B = W2, N = out, K = in)
-  const uint8_t* Wc;     // inference: NCHT K-major 256 x 32 chunks, W1^T rows 128..511 then W2
-  const u64* tile_src;   // inference: sources of each tile's first and last example
+  const uint8_t* Wc;     // inference: NCHT K-major 256 x 32 chunks, W1^T rows 0..511 then W2
+  const u64* list_e;     // inference: the examples the network decides (in any order) ...
+  const uint32_t* list_j;  // ... and their sources
+  u64 nlist;
   unsigned ntiles;
   const u64* tile_start;  // training: first example of each tile (nullptr: tile t starts at 128 t)
   // inference
   float thr;
   float lguard;           // log10 of the guard: a group with log10(|c_j| * vbound) >= lguard is kept
+  float lfloor;           // log10 of the floor: a group with log10(|c_j| * vbound) < lfloor is skipped
   uint32_t* keep;         // one bit per example
   u64* kept_terms;        // per source
   u64* kept_groups;       // per source
@@ -482,13 +485,93 @@ __global__ void __launch_bounds__(THREADS, 1) k_mlp_fwd(FwdArgs a) {
   if (warp == 0) umma::tmem_dealloc(tmem, 256);
 }
 
-// sources of the first and last example of every inference tile (one binary
-// search per tile, all tiles in parallel)
-__global__ void k_tile_src(ExView x, unsigned ntiles, u64* __restrict__ out) {
-  for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < ntiles; t += gridDim.x * blockDim.x) {
-    const u64 e0 = (u64)t * TILE, e1 = e0 + TILE - 1;
-    out[2 * t] = source_of(x, e0 < x.nex ? e0 : x.nex - 1);
-    out[2 * t + 1] = source_of(x, e1 < x.nex ? e1 : x.nex - 1);
+// Decides the groups the network need not see: a group whose largest possible
+// term, |c_j| times its integral bound, reaches the guard is kept; one below the
+// floor is skipped (the training labels call a group alive only through a term
+// above their minimum, so a floor at that minimum skips only groups the labels
+// call dead); the rest join the network's list (example and source), in any
+// order.  Writes every keep word (the guard's bits), the guard-kept groups and
+// terms per source and the terms of all groups.  A warp takes CW consecutive
+// keep words (32 examples each) per round, one lane per example; one atomic per
+// block round claims the list positions.
+constexpr int CW = 4;
+template <class KT>
+__global__ void __launch_bounds__(256) k_screen_classify(FwdArgs a, u64 wbeg, u64 nwords, u64* __restrict__ list_e,
+                                                         uint32_t* __restrict__ list_j, u64* __restrict__ nlist) {
+  __shared__ unsigned s_cnt[8];
+  __shared__ u64 s_base;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned lt = (1u << lane) - 1u;
+  const u64 step = (u64)gridDim.x * 8 * CW;
+  for (u64 wb = wbeg + (u64)blockIdx.x * 8 * CW; wb < nwords; wb += step) {
+    const u64 w0 = wb + (u64)warp * CW;
+    unsigned unsure_bits = 0, total = 0;
+    u64 js[CW];
+    for (int k = 0; k < CW; ++k) {
+      const u64 w = w0 + k;
+      js[k] = 0;
+      if (w >= nwords) continue;  // warp-uniform
+      const u64 e = (w << 5) + lane;
+      const bool valid = e < a.x.nex;
+      u64 j = 0;
+      if (lane == 0) j = source_of(a.x, w << 5);
+      j = __shfl_sync(0xffffffffu, j, 0);
+      Feat f{};
+      if (valid) {
+        while (j + 1 < a.x.nsrc && __ldg(a.x.goff + j + 1) <= e) ++j;
+        f = example_feat(a.x, load_key<KT>(a.x.keys, j), a.x.cc[j], (unsigned)(e - a.x.goff[j]) + 1u, j);
+      }
+      js[k] = j;
+      const float lb = 10.f * (f.lc + f.lv);
+      const bool gk = valid && lb >= a.lguard;
+      const bool unsure = valid && !gk && lb >= a.lfloor;
+      const unsigned m = __ballot_sync(0xffffffffu, gk);
+      if (lane == 0) a.keep[w] = m;
+      const unsigned at = warp_sum(valid ? f.gsize : 0u);
+      if (lane == 0 && at) atomicAdd(a.all_terms, (u64)at);
+      const u64 jj = valid ? j : ~0ull;
+      const unsigned same = __match_any_sync(0xffffffffu, jj);
+      const unsigned nt = gk ? f.gsize : 0u, ng = gk ? 1u : 0u;
+      if (same == 0xffffffffu) {
+        const unsigned st = warp_sum(nt), sg = warp_sum(ng);
+        if (lane == 0 && st) {
+          atomicAdd(a.kept_terms + j, (u64)st);
+          atomicAdd(a.kept_groups + j, (u64)sg);
+        }
+      } else if (gk) {
+        atomicAdd(a.kept_terms + j, (u64)nt);
+        atomicAdd(a.kept_groups + j, (u64)ng);
+      }
+      const unsigned bu = __ballot_sync(0xffffffffu, unsure);
+      if (unsure) unsure_bits |= 1u << k;
+      total += __popc(bu);
+    }
+    if (lane == 0) s_cnt[warp] = total;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      unsigned t = 0;
+      for (int i = 0; i < 8; ++i) {
+        const unsigned c = s_cnt[i];
+        s_cnt[i] = t;
+        t += c;
+      }
+      s_base = t ? atomicAdd(nlist, (u64)t) : 0ull;
+    }
+    __syncthreads();
+    u64 pos = s_base + s_cnt[warp];
+    for (int k = 0; k < CW; ++k) {
+      const u64 w = w0 + k;
+      if (w >= nwords) break;  // warp-uniform
+      const bool unsure = (unsure_bits >> k) & 1u;
+      const unsigned bu = __ballot_sync(0xffffffffu, unsure);
+      if (unsure) {
+        const u64 q = pos + __popc(bu & lt);
+        list_e[q] = (w << 5) + lane;
+        list_j[q] = (uint32_t)js[k];
+      }
+      pos += __popc(bu);
+    }
+    __syncthreads();  // s_cnt and s_base are rewritten next round
   }
 }
 
@@ -531,23 +614,13 @@ __device__ __forceinline__ bool rows_or(bool v) {
   return r != 0;
 }
 
-// b1 plus the occupancy rows of a key, column c of 256 (one column per thread)
-template <class KT>
-__device__ __forceinline__ float src_bias(const KT& key, int N, const __nv_bfloat16* __restrict__ W1b,
-                                          const float* __restrict__ b1, int c) {
-  float s = __ldg(b1 + c);
-  for (int o = 0; o < N; ++o)
-    if (key_test(key, o)) s += __bfloat162float(W1b[(size_t)(IN_OCC + o) * HID + c]);
-  return s;
-}
-
 template <class KT>
 __global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(FwdArgs a) {
   extern __shared__ __align__(1024) uint8_t smem[];
   uint8_t* sA2 = smem;                                                  // 64 KB layer-2 operand
   uint8_t* sStg = smem + A_BYTES;                                       // ISTAGES x (B chunk, input chunk)
-  float* sbias = reinterpret_cast<float*>(sStg + ISTAGES * ISTAGE);     // [2][256] per-source bias
-  float* scls = sbias + 2 * HID;                                        // [4][256] class rows
+  float* sb1 = reinterpret_cast<float*>(sStg + ISTAGES * ISTAGE);       // [256] b1
+  float* scls = sb1 + 2 * HID;                                          // [4][256] class rows
   float* slc = scls + 4 * HID;                                          // [256] log|c| row
   float* slv = slc + HID;                                               // [256] log bound row
   float* sb2 = slv + HID;                                               // [256]
@@ -555,7 +628,6 @@ __global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(FwdArgs a) {
   float* slog = sw3 + HID;                                              // [128] second-half logits
   __shared__ __align__(8) uint64_t bar_full[ISTAGES], bar_free[ISTAGES], bar_done, bar_fin;
   __shared__ uint32_t tmem_slot;
-  __shared__ u64 s_src[2];
   __shared__ volatile int s_fail;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid == 0) {
@@ -569,6 +641,7 @@ __global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(FwdArgs a) {
     s_fail = 0;
   }
   for (int i = tid; i < HID; i += INF_THREADS) {
+    sb1[i] = a.params[OFF_B1 + i];
     for (int k = 0; k < 4; ++k) scls[k * HID + i] = __bfloat162float(a.W1b[(size_t)(IN_CLS + k) * HID + i]);
     slc[i] = __bfloat162float(a.W1b[(size_t)IN_LC * HID + i]);
     slv[i] = __bfloat162float(a.W1b[(size_t)IN_LV * HID + i]);
@@ -612,26 +685,23 @@ __global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(FwdArgs a) {
     const uint16_t ONE = 0x3f80;  // BF16 1.0
     uint32_t g = 0, done_phase = 0;
     bool fail = false;  // this thread's; every decision takes it through rows_or
+    const int N = a.x.N;
+    const u64 nmask0 = N >= 64 ? ~0ull : ((1ull << N) - 1ull);
+    const u64 nmask1 = N >= 128 ? ~0ull : (N > 64 ? ((1ull << (N - 64)) - 1ull) : 0ull);
     for (unsigned t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
-      const u64 e0 = (u64)t * TILE;
-      const u64 e = e0 + row;
-      const bool valid = e < a.x.nex;
-      // the tile's first and last sources: their biases are shared
-      if (tid < 2) s_src[tid] = __ldg(a.tile_src + 2 * t + tid);
-      rows_sync();
-      sbias[tid] = src_bias(load_key<KT>(a.x.keys, s_src[0]), a.x.N, a.W1b, a.params + OFF_B1, tid);
-      sbias[HID + tid] = s_src[1] != s_src[0]
-                             ? src_bias(load_key<KT>(a.x.keys, s_src[1]), a.x.N, a.W1b, a.params + OFF_B1, tid)
-                             : sbias[tid];
-      u64 j = 0;
+      // row `row` of the tile: an entry of the network's list (example, source)
+      const u64 idx = (u64)t * TILE + row;
+      const bool valid = idx < a.nlist;
+      u64 e = 0, j = 0;
       Feat f{};
-      KT key{};
+      u64 occ[2] = {0ull, 0ull};
       if (valid) {
-        // sources are in example order: walk forward from the tile's first one
-        j = s_src[0];
-        while (j + 1 < a.x.nsrc && __ldg(a.x.goff + j + 1) <= e) ++j;
-        key = load_key<KT>(a.x.keys, j);
+        e = __ldg(a.list_e + idx);
+        j = __ldg(a.list_j + idx);
+        const KT key = load_key<KT>(a.x.keys, j);
         f = example_feat(a.x, key, a.x.cc[j], (unsigned)(e - a.x.goff[j]) + 1u, j);
+        occ[0] = kword(key, 0) & nmask0;
+        if (sizeof(KT) > 8) occ[1] = kword(key, 1) & nmask1;
       }
       // ---- layer 1, one-hot part: NCH1 chunks
       for (int c = 0; c < NCH1; ++c, ++g) {
@@ -639,13 +709,18 @@ __global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(FwdArgs a) {
         uint8_t* sB = sStg + st * ISTAGE;
         uint8_t* sX = sB + IB_BYTES;
         if (use > 0 && !umma::mbar_wait(&bar_free[st], (use - 1) & 1u)) fail = true;
-        // this row's 32 inputs of chunk c: p (c < 4), q (c < 8) or r as a one-hot
-        // index; each of the row's two threads writes 16 of them
+        // this row's 32 inputs of chunk c: occupancy bits (c < 4), then p, q or r
+        // as a one-hot index; each of the row's two threads writes 16 of them
         unsigned bits = 0;
         if (valid) {
-          const int idx = c < 4 ? f.p : (c < 8 ? f.q : f.r);
-          const int lo = IKC * (c & 3);
-          if (idx >= lo && idx < lo + IKC) bits = 1u << (idx - lo);
+          if (c < 4) {
+            bits = (unsigned)(occ[c >> 1] >> (32 * (c & 1)));
+          } else {
+            const int cc = c - 4;
+            const int oh = cc < 4 ? f.p : (cc < 8 ? f.q : f.r);
+            const int lo = IKC * (cc & 3);
+            if (oh >= lo && oh < lo + IKC) bits = 1u << (oh - lo);
+          }
         }
 #pragma unroll
         for (int qq = 0; qq < IKC / 16; ++qq) {
@@ -686,13 +761,7 @@ __global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(FwdArgs a) {
       }
       umma::tc_fence_after();
       {
-        const float* u = sbias;
-        float ubuf[HID / 2];
-        if (valid && j == s_src[1] && j != s_src[0]) u = sbias + HID;
-        if (valid && j != s_src[0] && j != s_src[1]) {  // a source strictly inside the tile: its own bias
-          for (int cc = 0; cc < HID / 2; ++cc) ubuf[cc] = src_bias(key, a.x.N, a.W1b, a.params + OFF_B1, c0h + cc);
-          u = ubuf - c0h;
-        }
+        const float* u = sb1;
         const float* rc = scls + (valid ? f.cls : 0) * HID;
         for (int k = 0; k < HID / 64; ++k) {
           const int cb = c0h + 32 * k;
@@ -759,19 +828,12 @@ __global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(FwdArgs a) {
       if (!half) {
         logit += slog[row] + b3;
         const float p = 1.f / (1.f + __expf(-logit));
-        // the guard keeps every group whose largest possible term, |c_j| times
-        // the group's integral bound, reaches it, whatever the network says
-        const bool kept = valid && (p >= a.thr || 10.f * (f.lc + f.lv) >= a.lguard);
-        const unsigned m = __ballot_sync(0xffffffffu, kept);
-        if (lane == 0 && e0 + 32 * warp < a.x.nex) a.keep[(e0 >> 5) + warp] = m;
+        const bool kept = valid && p >= a.thr;
+        if (kept) atomicOr(a.keep + (e >> 5), 1u << (e & 31));
         if (valid && a.prob) a.prob[e] = p;
         const u64 jj = valid ? j : ~0ull;
         const unsigned same = __match_any_sync(0xffffffffu, jj);
         const unsigned nt = kept ? f.gsize : 0u, ng = kept ? 1u : 0u;
-        if (a.all_terms) {
-          const unsigned at = warp_sum(valid ? f.gsize : 0u);
-          if (lane == 0 && at) atomicAdd(a.all_terms, (u64)at);
-        }
         if (same == 0xffffffffu) {
           const unsigned sm_ = warp_sum(nt), sg = warp_sum(ng);
           if (lane == 0 && valid && sm_) {
@@ -784,7 +846,7 @@ __global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(FwdArgs a) {
         }
       }
       umma::tc_fence_before();
-      rows_sync();  // the operand, the biases, the logits and TMEM are rewritten by the next tile
+      rows_sync();  // the operand, the logits and TMEM are rewritten by the next tile
       umma::tc_fence_after();
     }
     if (fail) {
@@ -1005,10 +1067,10 @@ __global__ void k_mlp_images(const float* p, __nv_bfloat16* W1b, uint8_t* W2img,
       const __nv_bfloat16 w = __float2bfloat16(p[OFF_W1 + i]);
       W1b[i] = w;
       // W1 row `in` (an input), column `h` (a hidden unit): element (h, in % IKC)
-      // of the inference chunk (in - IN_P) / IKC
+      // of the inference chunk in / IKC
       const unsigned in = (unsigned)(i / HID), h = (unsigned)(i % HID);
-      if (in >= (unsigned)IN_P && in < (unsigned)(IN_P + NCH1 * IKC)) {
-        const unsigned r = in - IN_P;
+      if (in < (unsigned)(IN_OCC + NCH1 * IKC)) {
+        const unsigned r = in - IN_OCC;
         *reinterpret_cast<__nv_bfloat16*>(Wc + (size_t)(r / IKC) * IB_BYTES + umma::tile_offset(h, r % IKC, IKC)) = w;
       }
     } else {
@@ -1205,19 +1267,24 @@ static int check_err(Screen& s) {
 
 // inference over the groups of n sources: keep bits, kept groups and terms per source
 static int screen_infer(Ctx& c, Screen& s, const u64* keys, const double* amps, u64 n, double thr, double guard,
-                        u64** goff_out, uint32_t** keep_out, u64** kterms_out, u64** kgroups_out, u64* nex_out,
-                        float* prob) {
+                        double floor_, u64** goff_out, uint32_t** keep_out, u64** kterms_out, u64** kgroups_out,
+                        u64* nex_out, float* prob) {
   int st;
   u64* goff = (u64*)scratch_get(c, "sc_goff", (n + 1) * sizeof(u64));
   if (!goff) return SFCI_ERR_NOMEM;
   if ((st = c.W == 1 ? group_offsets<1>(c, keys, n, goff) : group_offsets<2>(c, keys, n, goff))) return st;
   u64 nex = 0;
   if ((st = read_words(c, goff + n, sizeof(u64), &nex))) return st;
-  const unsigned ntiles = (unsigned)((nex + TILE - 1) / TILE);
-  uint32_t* keep = (uint32_t*)scratch_get(c, "sc_keep", ((size_t)ntiles * TILE / 32 + 1) * sizeof(uint32_t));
+  const u64 nwords = (nex + 31) / 32;
+  // the network's list is built and run in chunks of examples (whole keep words)
+  const u64 CHW = (1ull << 26) / 32;
+  const u64 chunk = std::min<u64>(nwords, CHW) * 32;
+  uint32_t* keep = (uint32_t*)scratch_get(c, "sc_keep", (nwords + 1) * sizeof(uint32_t));
   u64* kt = (u64*)scratch_get(c, "sc_kterms", (2 * (n + 1) + 1) * sizeof(u64));
-  u64* tsrc = (u64*)scratch_get(c, "sc_tsrc", (2 * (size_t)ntiles + 2) * sizeof(u64));
-  if (!keep || !kt || !tsrc) return SFCI_ERR_NOMEM;
+  u64* le = (u64*)scratch_get(c, "sc_le", (chunk + 1) * sizeof(u64));
+  uint32_t* lj = (uint32_t*)scratch_get(c, "sc_lj", (chunk + 1) * sizeof(uint32_t));
+  u64* nl = (u64*)scratch_get(c, "sc_nl", sizeof(u64));
+  if (!keep || !kt || !le || !lj || !nl) return SFCI_ERR_NOMEM;
   u64* kg = kt + (n + 1);
   u64* allt = kg + (n + 1);
   SFCI_CUDA(cudaMemsetAsync(kt, 0, (2 * (n + 1) + 1) * sizeof(u64), c.stream));
@@ -1227,20 +1294,31 @@ static int screen_infer(Ctx& c, Screen& s, const u64* keys, const double* amps, 
   a.params = s.params;
   a.W2img = s.W2img;
   a.Wc = s.Wc;
-  a.tile_src = tsrc;
-  a.ntiles = ntiles;
   a.thr = (float)thr;
   a.lguard = guard > 0.0 ? (float)std::log10(guard) : INFINITY;
+  a.lfloor = floor_ > 0.0 ? (float)std::log10(floor_) : -INFINITY;
   a.keep = keep;
   a.kept_terms = kt;
   a.kept_groups = kg;
   a.all_terms = allt;
   a.prob = prob;
   a.err = s.err;
-  if (ntiles) {
-    SFCI_LAUNCH(c, k_tile_src, std::min<unsigned>((ntiles + 255) / 256, (unsigned)c.sm_count * 4), 256, 0, a.x,
-                ntiles, tsrc);
-    const unsigned grid = std::min<unsigned>(ntiles, (unsigned)c.sm_count);
+  a.list_e = le;
+  a.list_j = lj;
+  for (u64 w0 = 0; w0 < nwords; w0 += CHW) {
+    const u64 w1 = std::min<u64>(nwords, w0 + CHW);
+    SFCI_CUDA(cudaMemsetAsync(nl, 0, sizeof(u64), c.stream));
+    const unsigned cg = (unsigned)std::min<u64>((w1 - w0 + 8 * CW - 1) / (8 * CW), (u64)c.sm_count * 8);
+    if (c.W == 1)
+      SFCI_LAUNCH(c, k_screen_classify<u64>, cg, 256, 0, a, w0, w1, le, lj, nl);
+    else
+      SFCI_LAUNCH(c, k_screen_classify<K128>, cg, 256, 0, a, w0, w1, le, lj, nl);
+    u64 nlist = 0;
+    if ((st = read_words(c, nl, sizeof(u64), &nlist))) return st;
+    if (!nlist) continue;
+    a.nlist = nlist;
+    a.ntiles = (unsigned)((nlist + TILE - 1) / TILE);
+    const unsigned grid = std::min<unsigned>(a.ntiles, (unsigned)c.sm_count);
     if (c.W == 1)
       SFCI_LAUNCH(c, k_mlp_infer<u64>, grid, INF_THREADS, infer_smem_bytes(), a);
     else
@@ -1310,8 +1388,8 @@ int screen_select(Ctx& c, const void* keys, const double* amps, u64 n, ScreenLis
   int st;
   u64 *goff, *kt, *kg, nex = 0;
   uint32_t* keep;
-  if ((st = screen_infer(c, s, (const u64*)keys, amps, n, c.screen_thr, c.screen_guard, &goff, &keep, &kt, &kg, &nex,
-                         nullptr)))
+  if ((st = screen_infer(c, s, (const u64*)keys, amps, n, c.screen_thr, c.screen_guard, c.screen_floor, &goff, &keep,
+                         &kt, &kg, &nex, nullptr)))
     return st;
   // offsets of the kept-group lists, the largest list, the totals
   u64* koff = (u64*)scratch_get(c, "sc_koff", (n + 1) * sizeof(u64));
@@ -1681,7 +1759,8 @@ extern "C" int sfci_screen_predict(sfci_screen* x, const sfci_vec* in, double th
     prob = (float*)scratch_get(c, "sc_prob", (ng + 1) * sizeof(float));
     if (!prob) return SFCI_ERR_NOMEM;
   }
-  if ((st = screen_infer(c, s, in->v.keys, in->v.amps, in->v.len, threshold, 0.0, &goff, &keep, &kt, &kg, &nex, prob)))
+  if ((st = screen_infer(c, s, in->v.keys, in->v.amps, in->v.len, threshold, 0.0, 0.0, &goff, &keep, &kt, &kg, &nex,
+                         prob)))
     return st;
   std::vector<u64> a(in->v.len), b(in->v.len);
   if ((st = read_words(c, kt, in->v.len * sizeof(u64), a.data()))) return st;
@@ -1740,6 +1819,13 @@ extern "C" int sfci_ctx_set_screen_guard(sfci_ctx* ctx, double guard) {
   if (!ctx) return set_error(SFCI_ERR_ARG, "sfci_ctx_set_screen_guard: null context");
   if (!(guard >= 0.0) || std::isinf(guard)) return set_error(SFCI_ERR_ARG, "sfci_ctx_set_screen_guard: guard >= 0, finite");
   ctx->c.screen_guard = guard;
+  return SFCI_OK;
+}
+
+extern "C" int sfci_ctx_set_screen_floor(sfci_ctx* ctx, double floor_) {
+  if (!ctx) return set_error(SFCI_ERR_ARG, "sfci_ctx_set_screen_floor: null context");
+  if (!(floor_ >= 0.0) || std::isinf(floor_)) return set_error(SFCI_ERR_ARG, "sfci_ctx_set_screen_floor: floor >= 0, finite");
+  ctx->c.screen_floor = floor_;
   return SFCI_OK;
 }
 

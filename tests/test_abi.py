@@ -107,6 +107,7 @@ def test_solver_entry_points_reject_null_arguments():
     assert name(L.sfci_cisd(None, None, 0, 1, None, None, None, C.byref(n))) == "SFCI_ERR_ARG"
     assert name(L.sfci_fci(None, 1, None, None, None, C.byref(n))) == "SFCI_ERR_ARG"
     assert name(L.sfci_ctx_set_screen_guard(None, 1e-6)) == "SFCI_ERR_ARG"
+    assert name(L.sfci_ctx_set_screen_floor(None, 1e-8)) == "SFCI_ERR_ARG"
 
 
 def test_dot_noalloc_rejects_bad_arguments_without_a_device_call():

@@ -209,6 +209,17 @@ def test_guard_keeps_groups_with_large_term_bounds(golden_in):
         kept.append(b_["kept_groups"] - a_["kept_groups"])
     assert all(x <= y for x, y in zip(kept, kept[1:])), kept
     assert kept[-1] > kept[0], kept
+    # a floor above every bound skips every double group without the network;
+    # one below every bound changes nothing (threshold 0 keeps the rest)
+    c.set_screen(scr, 0.0, floor=1e300)
+    a_ = c.screen_stats()
+    c.SpMVMtply_bucket(vin, out1, 0.0, 1.0)
+    b_ = c.screen_stats()
+    assert b_["kept_groups"] == a_["kept_groups"] and b_["groups"] > a_["groups"]
+    c.set_screen(scr, 0.0, floor=1e-300)
+    d2 = c.SpMVMtply_bucket(vin, out1, 0.0, 1.0)
+    k2, a2 = out1.download()
+    assert np.array_equal(k0, k2) and np.array_equal(a0.view(np.uint64), a2.view(np.uint64)) and d0 == d2
     with pytest.raises(sg.SfciError):
         c.set_screen(scr, 0.5, guard=-1.0)
 

@@ -61,4 +61,49 @@ inline bool plan_memory(const std::vector<plan_u64>& binoff, unsigned nb1, plan_
   return out.passes > 0;
 }
 
+// Class passes: the 256 alpha classes' term counts hh, the level-1 capacity c1.
+// Passes are runs of aligned blocks of 2^k classes (the generator enumerates a
+// pass's spin-0 doubles block by block): k three bits below the widest block
+// size whose blocks all fit c1 (0 when even single classes do not), consecutive
+// blocks while they fit and while their runs (occupied spin-0 pairs x blocks,
+// at most nop_max x blocks) fit run_cap.  A block larger than c1 is a pass of
+// its own (the caller splits it further into bin passes).  Empty passes are
+// dropped.
+struct ClassPass {
+  unsigned lo, hi;  // classes [lo, hi): aligned blocks of 2^k
+  plan_u64 terms;
+  int k;
+};
+
+inline std::vector<ClassPass> plan_class_passes(const std::vector<plan_u64>& hh, plan_u64 c1, unsigned nop_max,
+                                                unsigned run_cap) {
+  const unsigned NC = 256;
+  auto block_sum = [&](unsigned lo, int kb) {
+    plan_u64 t = 0;
+    for (unsigned cc = lo; cc < lo + (1u << kb); ++cc) t += hh[cc];
+    return t;
+  };
+  int kfit = -1;
+  for (int kb = 8; kb >= 0 && kfit < 0; --kb) {
+    bool fits = true;
+    for (unsigned lo = 0; lo < NC && fits; lo += 1u << kb) fits = block_sum(lo, kb) <= c1;
+    if (fits) kfit = kb;
+  }
+  const int kc = std::max(0, kfit - 3);
+  const unsigned nblk_cap = std::max(1u, run_cap / std::max(1u, nop_max));
+  std::vector<ClassPass> out;
+  unsigned lo = 0;
+  while (lo < NC) {
+    unsigned hi = lo + (1u << kc);
+    plan_u64 sum = block_sum(lo, kc);
+    while (hi < NC && ((hi - lo) >> kc) < nblk_cap && sum + block_sum(hi, kc) <= c1) {
+      sum += block_sum(hi, kc);
+      hi += 1u << kc;
+    }
+    if (sum) out.push_back({lo, hi, sum, kc});
+    lo = hi;
+  }
+  return out;
+}
+
 }  // namespace sfci

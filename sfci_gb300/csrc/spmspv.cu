@@ -1711,39 +1711,11 @@ int spmspv_impl(Ctx& c, const Vec& in, Vec& out, double lambda, double coeff, do
       }
       if (tot != T) return set_error(SFCI_ERR_NUMERIC, "SpMSpV class histogram disagrees with term offsets");
       (void)big;
-      // Passes are runs of aligned blocks of 2^kc classes (the generator
-      // enumerates a pass's spin-0 doubles block by block): kc three bits below
-      // the widest block size whose blocks all fit a pass, consecutive blocks
-      // while they fit and while their runs (occupied spin-0 pairs x blocks)
-      // fit the generator's table.  A class larger than a pass is an outer pass
-      // of its own, split further into bin passes that regenerate that class's
-      // terms only.
+      // runs of aligned class blocks (plan_class_passes, plan.h)
       cls_mode = true;
-      auto block_sum = [&](unsigned lo, int kb) {
-        u64 t = 0;
-        for (unsigned cc = lo; cc < lo + (1u << kb); ++cc) t += hh[cc];
-        return t;
-      };
-      int kfit = -1;
-      for (int kb = 8; kb >= 0 && kfit < 0; --kb) {
-        bool fits = true;
-        for (unsigned lo = 0; lo < (unsigned)CLS_N && fits; lo += 1u << kb) fits = block_sum(lo, kb) <= cmp.C1;
-        if (fits) kfit = kb;
-      }
-      const int kc = std::max(0, kfit - 3);
       const unsigned nop_max = std::max(1u, c2((unsigned)std::min(c.ne, c.M)));
-      const unsigned nblk_cap = std::max(1u, (unsigned)RUN_CAP / nop_max);
-      unsigned lo = 0;
-      while (lo < (unsigned)CLS_N) {
-        unsigned hi = lo + (1u << kc);
-        u64 sum = block_sum(lo, kc);
-        while (hi < (unsigned)CLS_N && ((hi - lo) >> kc) < nblk_cap && sum + block_sum(hi, kc) <= cmp.C1) {
-          sum += block_sum(hi, kc);
-          hi += 1u << kc;
-        }
-        if (sum) outer.push_back({lo, hi, sum, kc});
-        lo = hi;
-      }
+      for (const ClassPass& cp : plan_class_passes(hh, cmp.C1, nop_max, (unsigned)RUN_CAP))
+        outer.push_back({cp.lo, cp.hi, cp.terms, cp.k});
       cmp.passes = (int)outer.size();
     }
   }

@@ -24,6 +24,7 @@ def pl(tmp_path_factory):
     L = C.CDLL(so)
     L.pl_plan.argtypes = [_u, C.c_uint, C.c_uint64, C.c_uint64, C.c_uint64, C.c_uint64, C.c_int, _u]
     L.pl_passes.argtypes = [_u, C.c_uint, C.c_uint64]
+    L.pl_class.argtypes = [_u, C.c_uint64, C.c_uint, C.c_uint, _u, C.c_int]
     return L
 
 
@@ -110,3 +111,35 @@ def test_random_plans_fit_and_minimise_passes(pl, seed):
         c1 = T if T + c2 + 2 * sc <= avail else avail - c2 - 2 * sc
         if avail >= c2 + 2 * sc + max(sizes) and c1 >= max(sizes):
             assert pl.pl_passes(binoff, nb, c1) >= passes
+
+
+def _class_plan(pl, hh, c1, nop_max, run_cap=2048):
+    out = np.zeros(4 * 512, np.uint64)
+    n = pl.pl_class(np.asarray(hh, np.uint64), int(c1), nop_max, run_cap, out, 512)
+    return [tuple(int(x) for x in out[4 * i:4 * i + 4]) for i in range(n)]
+
+
+@pytest.mark.parametrize("seed,scale,frac", [(0, 1e9, 1 / 24), (1, 1e6, 1 / 5), (2, 3e10, 1 / 60), (3, 1e4, 1.0)])
+def test_class_passes_cover_every_class_in_aligned_fitting_blocks(pl, seed, scale, frac):
+    """Class passes (plan_class_passes): every class with terms lies in exactly one
+    pass, in order; a pass is whole aligned blocks of 2^k classes, holds at most
+    c1 terms unless it is a single block, and its runs (occupied pairs x blocks)
+    fit the generator's table."""
+    rng = np.random.default_rng(seed)
+    hh = (rng.uniform(0.7, 1.3, 256) * scale).astype(np.uint64)
+    hh[rng.integers(0, 256, 5)] = 0  # a few empty classes
+    c1 = int(max(int(hh.sum() * frac), int(hh.max())))
+    nop_max = 45
+    passes = _class_plan(pl, hh, c1, nop_max)
+    covered = np.zeros(256, bool)
+    prev = 0
+    for lo, hi, terms, k in passes:
+        assert lo >= prev and lo % (1 << k) == 0 and hi % (1 << k) == 0 and hi > lo
+        assert terms == int(hh[lo:hi].sum()) > 0
+        assert terms <= c1 or hi - lo == (1 << k)
+        assert nop_max * ((hi - lo) >> k) <= 2048
+        covered[lo:hi] = True
+        prev = hi
+    assert covered[hh > 0].all()
+    # close to the fewest passes the capacity allows
+    assert len(passes) <= 2 * max(1, -(-int(hh.sum()) // c1)) + 1

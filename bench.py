@@ -674,9 +674,10 @@ def run_mlp(args):
     system: inference over every term group of a Krylov vector's top
     --mlp-sources determinants (1,870 groups each), and Adam training steps on
     the groups' labels.  Tensor FLOPs as the MMAs execute them: per group for
-    inference 2 x 256 x (384 + 256) (layer 1's one-hot p, q, r rows and layer
-    2); per training example the forward and backward 256 x 256 products and
-    the weight-gradient products of both layers (2 x 256 x (256 + 256 + 576))."""
+    inference 2 x 256 x (512 + 256) (layer 1's 0/1 rows: occupancy, p, q, r;
+    and layer 2); per training example the forward and backward 256 x 256
+    products and the weight-gradient products of both layers
+    (2 x 256 x (256 + 256 + 576))."""
     import sfci_gb300 as sg
     sg.load_library()
     sysd = SYSTEMS[1]
@@ -702,7 +703,7 @@ def run_mlp(args):
     scr.train(steps, batch_tiles=args.mlp_batch_tiles, lr=1e-3)
     t_tr = (time.perf_counter() - t0) / steps
     B = args.mlp_batch_tiles * 128
-    f_inf = 2.0 * 256 * (384 + 256) * groups
+    f_inf = 2.0 * 256 * (512 + 256) * groups
     f_tr = 2.0 * 256 * (256 + 256 + 256 + 576) * B
     peak = None
     try:

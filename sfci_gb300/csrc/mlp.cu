@@ -262,7 +262,8 @@ struct FwdArgs {
   const uint8_t* W2img;  // K-major image of W2 (B = W2, N = out, K = in)
   const uint8_t* Wc;     // inference: NCHT K-major 256 x 32 chunks, W1^T rows 0..511 then W2
   const u64* list_e;     // inference: the examples the network decides (in any order) ...
-  const uint32_t* list_j;  // ... and their sources
+  const uint32_t* list_j;  // ... their sources ...
+  const uint4* list_f;     // ... and their features (ListFeat)
   u64 nlist;
   unsigned ntiles;
   const u64* tile_start;  // training: first example of each tile (nullptr: tile t starts at 128 t)
@@ -495,9 +496,28 @@ __global__ void __launch_bounds__(THREADS, 1) k_mlp_fwd(FwdArgs a) {
 // keep words (32 examples each) per round, one lane per example; one atomic per
 // block round claims the list positions.
 constexpr int CW = 4;
+// a list entry's features, 16 bytes: p | q << 7 | r << 14 | class << 21, log|c|, log bound, terms
+__device__ __forceinline__ uint4 pack_feat(const Feat& f) {
+  return make_uint4((unsigned)f.p | ((unsigned)f.q << 7) | ((unsigned)f.r << 14) | ((unsigned)f.cls << 21),
+                    __float_as_uint(f.lc), __float_as_uint(f.lv), f.gsize);
+}
+__device__ __forceinline__ Feat unpack_feat(const uint4 v) {
+  Feat f;
+  f.p = (int)(v.x & 127u);
+  f.q = (int)((v.x >> 7) & 127u);
+  f.r = (int)((v.x >> 14) & 127u);
+  f.cls = (int)((v.x >> 21) & 3u);
+  f.lc = __uint_as_float(v.y);
+  f.lv = __uint_as_float(v.z);
+  f.gstart = 0;
+  f.gsize = v.w;
+  return f;
+}
+
 template <class KT>
 __global__ void __launch_bounds__(256) k_screen_classify(FwdArgs a, u64 wbeg, u64 nwords, u64* __restrict__ list_e,
-                                                         uint32_t* __restrict__ list_j, u64* __restrict__ nlist) {
+                                                         uint32_t* __restrict__ list_j, uint4* __restrict__ list_f,
+                                                         u64* __restrict__ nlist) {
   __shared__ unsigned s_cnt[8];
   __shared__ u64 s_base;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -507,9 +527,11 @@ __global__ void __launch_bounds__(256) k_screen_classify(FwdArgs a, u64 wbeg, u6
     const u64 w0 = wb + (u64)warp * CW;
     unsigned unsure_bits = 0, total = 0;
     u64 js[CW];
+    uint4 fs[CW];
     for (int k = 0; k < CW; ++k) {
       const u64 w = w0 + k;
       js[k] = 0;
+      fs[k] = make_uint4(0, 0, 0, 0);
       if (w >= nwords) continue;  // warp-uniform
       const u64 e = (w << 5) + lane;
       const bool valid = e < a.x.nex;
@@ -522,6 +544,7 @@ __global__ void __launch_bounds__(256) k_screen_classify(FwdArgs a, u64 wbeg, u6
         f = example_feat(a.x, load_key<KT>(a.x.keys, j), a.x.cc[j], (unsigned)(e - a.x.goff[j]) + 1u, j);
       }
       js[k] = j;
+      fs[k] = pack_feat(f);
       const float lb = 10.f * (f.lc + f.lv);
       const bool gk = valid && lb >= a.lguard;
       const bool unsure = valid && !gk && lb >= a.lfloor;
@@ -568,6 +591,7 @@ __global__ void __launch_bounds__(256) k_screen_classify(FwdArgs a, u64 wbeg, u6
         const u64 q = pos + __popc(bu & lt);
         list_e[q] = (w << 5) + lane;
         list_j[q] = (uint32_t)js[k];
+        list_f[q] = fs[k];
       }
       pos += __popc(bu);
     }
@@ -698,8 +722,8 @@ __global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(FwdArgs a) {
       if (valid) {
         e = __ldg(a.list_e + idx);
         j = __ldg(a.list_j + idx);
+        f = unpack_feat(__ldg(a.list_f + idx));  // computed by the pre-pass
         const KT key = load_key<KT>(a.x.keys, j);
-        f = example_feat(a.x, key, a.x.cc[j], (unsigned)(e - a.x.goff[j]) + 1u, j);
         occ[0] = kword(key, 0) & nmask0;
         if (sizeof(KT) > 8) occ[1] = kword(key, 1) & nmask1;
       }
@@ -1277,14 +1301,15 @@ static int screen_infer(Ctx& c, Screen& s, const u64* keys, const double* amps, 
   if ((st = read_words(c, goff + n, sizeof(u64), &nex))) return st;
   const u64 nwords = (nex + 31) / 32;
   // the network's list is built and run in chunks of examples (whole keep words)
-  const u64 CHW = (1ull << 26) / 32;
+  const u64 CHW = (1ull << 25) / 32;
   const u64 chunk = std::min<u64>(nwords, CHW) * 32;
   uint32_t* keep = (uint32_t*)scratch_get(c, "sc_keep", (nwords + 1) * sizeof(uint32_t));
   u64* kt = (u64*)scratch_get(c, "sc_kterms", (2 * (n + 1) + 1) * sizeof(u64));
   u64* le = (u64*)scratch_get(c, "sc_le", (chunk + 1) * sizeof(u64));
   uint32_t* lj = (uint32_t*)scratch_get(c, "sc_lj", (chunk + 1) * sizeof(uint32_t));
+  uint4* lf = (uint4*)scratch_get(c, "sc_lf", (chunk + 1) * sizeof(uint4));
   u64* nl = (u64*)scratch_get(c, "sc_nl", sizeof(u64));
-  if (!keep || !kt || !le || !lj || !nl) return SFCI_ERR_NOMEM;
+  if (!keep || !kt || !le || !lj || !lf || !nl) return SFCI_ERR_NOMEM;
   u64* kg = kt + (n + 1);
   u64* allt = kg + (n + 1);
   SFCI_CUDA(cudaMemsetAsync(kt, 0, (2 * (n + 1) + 1) * sizeof(u64), c.stream));
@@ -1305,14 +1330,15 @@ static int screen_infer(Ctx& c, Screen& s, const u64* keys, const double* amps, 
   a.err = s.err;
   a.list_e = le;
   a.list_j = lj;
+  a.list_f = lf;
   for (u64 w0 = 0; w0 < nwords; w0 += CHW) {
     const u64 w1 = std::min<u64>(nwords, w0 + CHW);
     SFCI_CUDA(cudaMemsetAsync(nl, 0, sizeof(u64), c.stream));
     const unsigned cg = (unsigned)std::min<u64>((w1 - w0 + 8 * CW - 1) / (8 * CW), (u64)c.sm_count * 8);
     if (c.W == 1)
-      SFCI_LAUNCH(c, k_screen_classify<u64>, cg, 256, 0, a, w0, w1, le, lj, nl);
+      SFCI_LAUNCH(c, k_screen_classify<u64>, cg, 256, 0, a, w0, w1, le, lj, lf, nl);
     else
-      SFCI_LAUNCH(c, k_screen_classify<K128>, cg, 256, 0, a, w0, w1, le, lj, nl);
+      SFCI_LAUNCH(c, k_screen_classify<K128>, cg, 256, 0, a, w0, w1, le, lj, lf, nl);
     u64 nlist = 0;
     if ((st = read_words(c, nl, sizeof(u64), &nlist))) return st;
     if (!nlist) continue;

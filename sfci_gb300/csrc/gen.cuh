@@ -89,9 +89,10 @@ struct DetInfo {
   unsigned char occ[2][64];
   unsigned char vir[2][64];
   // single excitations of spin s, entry ii * nv[s] + aa (na * nv <= 32 * 32
-  // for 64 orbitals of a spin): descriptor of occ[s][ii] -> vir[s][aa], whose
-  // two orbitals are also the two key bits it flips
+  // for 64 orbitals of a spin): descriptor of occ[s][ii] -> vir[s][aa] and
+  // the two key bits it flips
   unsigned sd[2][1024];
+  KT kx[2][1024];
   unsigned char hx[1024];  // alpha-class change of each spin-0 single
 };
 
@@ -105,6 +106,10 @@ SFCI_HD void det_fill_singles(DetInfo<KT>& d, unsigned k0, unsigned step) {
       const int i = d.occ[s][ii], a = d.vir[s][aa];
       d.sd[s][k] = (unsigned)i | ((unsigned)a << 7) | ((unsigned)spatial_pair(i >> 1, a >> 1) << 14) |
                    ((unsigned)between_parity(d.h.key, i, a) << 26);
+      KT m = key_zero<KT>();
+      key_flip(m, i);
+      key_flip(m, a);
+      d.kx[s][k] = m;
       if (s == 0) d.hx[k] = (unsigned char)(alpha_class_of_orb(i) ^ alpha_class_of_orb(a));
     }
   }
@@ -261,25 +266,18 @@ SFCI_HD Exc decode(const DetHead<KT>& d, const unsigned short* pt, unsigned l) {
   return e;
 }
 
-// the key with the two orbitals of a single-excitation descriptor flipped
-template <class KT>
-SFCI_HD void key_move(KT& k, unsigned t) {
-  key_flip(k, (int)sd_i(t));
-  key_flip(k, (int)sd_a(t));
-}
-
 template <class KT>
 SFCI_HD KT target_key(const DetHead<KT>& h, const DetInfo<KT>& d, const Exc& e) {
   KT k = h.key;
   if (e.cls == 1) {
-    key_move(k, d.sd[e.s][e.x]);
+    key_xor(k, d.kx[e.s][e.x]);
   } else if (e.cls == 2) {
     const unsigned nv = e.s ? h.nv[1] : h.nv[0];
-    key_move(k, d.sd[e.s][e.x * nv + e.u]);
-    key_move(k, d.sd[e.s][e.y * nv + e.v]);
+    key_xor(k, d.kx[e.s][e.x * nv + e.u]);
+    key_xor(k, d.kx[e.s][e.y * nv + e.v]);
   } else if (e.cls == 3) {
-    key_move(k, d.sd[0][e.x]);
-    key_move(k, d.sd[1][e.y]);
+    key_xor(k, d.kx[0][e.x]);
+    key_xor(k, d.kx[1][e.y]);
   }
   return k;
 }
@@ -389,12 +387,10 @@ SFCI_HD double double_term(const DetHead<KT>& dh, const DetInfo<KT>& d, const un
   }
   const int r1 = opp ? 0 : s, r2 = opp ? 1 : s;
   const unsigned t1 = d.sd[r1][k1], t2 = d.sd[r2][k2];
-  const int i = (int)sd_i(t1), a = (int)sd_a(t1), j = (int)sd_i(t2), b = (int)sd_a(t2);
   key = dh.key;
-  key_flip(key, i);
-  key_flip(key, a);
-  key_flip(key, j);
-  key_flip(key, b);
+  key_xor(key, d.kx[r1][k1]);
+  key_xor(key, d.kx[r2][k2]);
+  const int i = (int)sd_i(t1), a = (int)sd_a(t1), j = (int)sd_i(t2), b = (int)sd_a(t2);
   // opposite spin: the entry of pair (min(i,j), max(i,j)); same spin: (a,i,b,j) - (b,i,a,j)
   const bool fwd = !opp || i < j;
   const int blk = opp ? (fwd ? 1 : 2) : 3 * s;

@@ -271,9 +271,6 @@ __host__ __device__ inline size_t gen_smem_bytes(int mode, unsigned nbp, unsigne
     s += al16(sizeof(uint32_t) * nbp) + 2 * al16(sizeof(u64) * nbp) + 3 * al16(sizeof(unsigned short) * GEN_ROUND);
   s += 2 * al16(sizeof(uint32_t) * kl_cap);
   if (cls) s += cls_smem_bytes();
-  // a screened or class-pass generation pass keeps each round's full term
-  // indices (two rounds' worth) so that its staged terms need no second remap
-  if (mode == M_SCATTER && kl_cap) s += 2 * al16(sizeof(uint32_t) * GEN_ROUND);
   return s;
 }
 
@@ -316,8 +313,6 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
   unsigned char* cbq = reinterpret_cast<unsigned char*>(cperm) + al16(sizeof(unsigned short) * CP_MAX);
   uint32_t* cbcnt = reinterpret_cast<uint32_t*>(cbq + al16(CP_MAX));  // bucket sizes
   uint32_t* cboff = cbcnt + al16(sizeof(uint32_t) * 257) / sizeof(uint32_t);  // bucket starts
-  if (g.cls_on) off += cls_smem_bytes();
-  uint32_t* slf = reinterpret_cast<uint32_t*>(smem + off);  // screened: [2][GEN_ROUND] full term indices
   __shared__ unsigned s_nk, s_n2;
   __shared__ u64 s_det;
   __shared__ unsigned s_nsq;
@@ -357,7 +352,6 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
   __syncthreads();
   double eacc = 0.0;
   unsigned pbad = 0;
-  unsigned rpar = 0;  // round parity: which half of slf a round writes
   const int shift1 = 64 - g.b1;
   u64 det = (t0 < t1) ? s_det : 0;
   while (t0 < t1) {
@@ -590,20 +584,18 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
     };
     const unsigned l0 = (unsigned)(t0 - dbeg);
     const unsigned l1 = (unsigned)((t1 < dend ? t1 : dend) - dbeg);
-    for (unsigned rb = l0; rb < l1; rb += GEN_ROUND, ++rpar) {
+    for (unsigned rb = l0; rb < l1; rb += GEN_ROUND) {
       if (MODE == M_SCATTER) {
         // (1) bin every term of the round by its hash alone and rank the ones
         // in this pass; (2) stage their round indices sorted by bin; (3) decode,
         // build the keys and amplitudes of the staged terms only, with full
         // warps, and write each bin's run contiguously
         unsigned br[GEN_IPT];  // (rank << 16) | local bin, or ~0u
-        uint32_t* rlf = slf + (rpar & 1u) * GEN_ROUND;  // this round's full indices (screened)
 #pragma unroll
         for (int it = 0; it < GEN_IPT; ++it) {
           unsigned l = rb + it * GEN_THREADS + tid;
           br[it] = ~0u;
           const unsigned lf = l < l1 ? remap(l) : 0u;
-          if (screened) rlf[it * GEN_THREADS + tid] = lf;
           if (l < l1 && in_pass(lf)) {
             const unsigned bin = (unsigned)(key_hash(target_key(dh, d, decode(dh, pt, lf))) >> shift1);
             if (bin >= g.bin_lo && bin < g.bin_hi) {
@@ -647,8 +639,7 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
         // Doubles (most terms) take one branch-free path whatever their kind.
         const bool with_singles = rb < dh.c[2];
         for (unsigned i = tid; i < tot; i += GEN_THREADS) {
-          // the full term index (the diagonal and the singles map to themselves)
-          const unsigned l = screened ? rlf[sx[i]] : rb + sx[i];
+          const unsigned l = rb + sx[i];
           if (with_singles && l != 0 && l < dh.c[2]) {
             sq[atomicAdd(&s_nsq, 1u)] = (unsigned short)i;
             continue;
@@ -660,7 +651,7 @@ __global__ void __launch_bounds__(GEN_THREADS, 2) k_gen(GenArgs<KT> g) {
             key = dh.key;
             amp = dh.dterm;
           } else {
-            amp = double_term(dh, d, pt, hv, l, key);
+            amp = double_term(dh, d, pt, hv, remap(l), key);
           }
           g.okeys[pos] = key;
           g.oamps[pos] = amp;

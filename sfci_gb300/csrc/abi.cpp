@@ -61,6 +61,20 @@ void scratch_free_all(Ctx& c) {
   c.scratch.clear();
 }
 
+void scratch_release(Ctx& c, const char* name) {
+  auto it = c.scratch.find(name);
+  if (it == c.scratch.end() || !it->second.p) return;
+  cudaStreamSynchronize(c.stream);
+  cudaFree(it->second.p);
+  c.scratch.erase(it);
+}
+
+void scratch_release_plan(Ctx& c) {
+  for (const char* nm : {"sp_l1k", "sp_l1a", "sp_l2k", "sp_l2a", "sp_sk", "sp_sa", "rs_keys", "rs_vals", "topk_k",
+                         "topk_a"})
+    scratch_release(c, nm);
+}
+
 u64* pinned_words(Ctx& c, size_t n) {
   if (c.h_pin_words >= n) return c.h_pin;
   if (c.h_pin) cudaFreeHost(c.h_pin);

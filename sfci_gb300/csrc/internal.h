@@ -100,6 +100,10 @@ void screen_orphan(struct Screen* s);
 // growable named device scratch (contents not preserved on growth)
 void* scratch_get(Ctx& c, const char* name, size_t bytes);
 void scratch_free_all(Ctx& c);
+// free one named buffer; free the SpMSpV plan's large buffers (its next call
+// re-plans from the memory that is then free)
+void scratch_release(Ctx& c, const char* name);
+void scratch_release_plan(Ctx& c);
 // pinned host words for readbacks
 u64* pinned_words(Ctx& c, size_t n);
 

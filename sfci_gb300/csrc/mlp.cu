@@ -1434,6 +1434,13 @@ int screen_select(Ctx& c, const void* keys, const double* amps, u64 n, ScreenLis
   if ((st = read_words(c, kts + n, sizeof(u64), &tk))) return st;
   uint32_t* ks = (uint32_t*)scratch_get(c, "sc_kstart", (nk + 1) * sizeof(uint32_t));
   uint32_t* kp = (uint32_t*)scratch_get(c, "sc_kpre", (nk + 1) * sizeof(uint32_t));
+  if (!ks || !kp) {
+    // the previous product's buffers still hold the device: let them go (this
+    // product plans after the lists are built) and try once more
+    scratch_release_plan(c);
+    ks = (uint32_t*)scratch_get(c, "sc_kstart", (nk + 1) * sizeof(uint32_t));
+    kp = (uint32_t*)scratch_get(c, "sc_kpre", (nk + 1) * sizeof(uint32_t));
+  }
   if (!ks || !kp) return SFCI_ERR_NOMEM;
   if (n) {
     const unsigned grid = (unsigned)std::min<u64>((n * 32 + 255) / 256, (u64)c.sm_count * 16);

@@ -5,15 +5,17 @@
 // reference; it screens the generator of OffDiagGen_bit (src/bitstr.cpp:162-302).
 //
 // Layer 1 has sparse inputs (the source's occupancy bits, one-hot p, q, r and
-// class, two scalars).  Inference (k_mlp_infer) runs its one-hot part on the
-// tensor cores, an MMA of the tile's 0/1 input rows with W1^T streamed in K
-// chunks by bulk copies, and adds the class row and the scalar rows in the
-// epilogue.  The training forward sums the about 25 rows of W1 on CUDA cores,
-// the occupancy part shared by the rows of a tile that come from one source.
-// Layer 2 (256 x 256) runs on the tensor cores in both: tiles of 128 groups,
-// tcgen05.mma with the BF16 weight image staged once per persistent CTA by a
-// bulk (TMA) copy, the FP32 accumulator in TMEM.  Layer 3 and the sigmoid are
-// the epilogue.
+// class, two scalars).  Inference runs in two kernels: a pre-pass
+// (k_screen_classify) that keeps the groups the guard keeps, skips those under
+// the floor and lists the rest with their features, and the network
+// (k_mlp_infer), which runs layer 1's 0/1 part on the tensor cores, an MMA of
+// the tile's input rows with W1^T streamed in K chunks by bulk copies, and
+// adds the class row and the scalar rows in the epilogue.  The training
+// forward sums the about 25 rows of W1 on CUDA cores, the occupancy part
+// shared by the rows of a tile that come from one source.  Layer 2 (256 x 256)
+// runs on the tensor cores in both: tiles of 128 groups, tcgen05.mma with the
+// BF16 weight chunks in shared memory, the FP32 accumulator in TMEM.  Layer 3
+// and the sigmoid are the epilogue.
 //
 // Training (hand-written, four kernels per step): a forward kernel that also
 // forms the output error and the layer-2 error Delta2; a backward kernel with
@@ -602,21 +604,23 @@ __global__ void __launch_bounds__(256) k_screen_classify(FwdArgs a, u64 wbeg, u6
 // ---------------------------------------------------------------------------
 // inference: both hidden layers on the tensor cores
 // ---------------------------------------------------------------------------
-// Warps 0-7 are row warps: warp w holds rows 32 (w % 4) .. + 31 of the tile
-// (the TMEM lane quarter it may read) and the column half w / 4 of every
-// 256-wide epilogue, so two warps share each row and each scheduler has two.
-// Warp 8 is a copy warp.  Every tile takes the same 20 B-operand chunks (256 x
-// 32, 16 KB): 12 of W1^T for the one-hot inputs p, q, r (W1 rows 128..511) and
-// 8 of W2, through a ring of 6 stages; the copy warp streams them ahead of use,
-// across tile boundaries and through the epilogues.  Layer 1: per W1 chunk the
-// row warps write the tile's 0/1 input chunk into the stage and one thread
-// issues its two MMAs into TMEM columns 0..255.  The layer-1 epilogue adds the
-// source's bias (b1 plus its occupancy rows, summed once per source), the class
-// row and the two scalar rows (kept in shared memory as FP32 copies of the BF16
-// weights), applies the ReLU and writes the BF16 layer-2 operand (64 KB); layer
-// 2 accumulates into TMEM columns 256..511; layer 3 and the sigmoid are the last
-// epilogue, its two column halves added through shared memory.  The same
-// function as the training forward (layer1_row), summed in another order.
+// The rows of a tile are entries of the pre-pass's list (example, source,
+// features), in any order.  Warps 0-7 are row warps: warp w holds rows
+// 32 (w % 4) .. + 31 of the tile (the TMEM lane quarter it may read) and the
+// column half w / 4 of every 256-wide epilogue, so two warps share each row
+// and each scheduler has two.  Warp 8 is a copy warp.  Every tile takes the
+// same 24 B-operand chunks (256 x 32, 16 KB): 16 of W1^T for the 0/1 inputs
+// (occupancy, p, q, r: W1 rows 0..511) and 8 of W2, through a ring of 6
+// stages; the copy warp streams them ahead of use, across tile boundaries and
+// through the epilogues.  Layer 1: per W1 chunk the row warps write the tile's
+// 0/1 input chunk (the source's occupancy bits or a one-hot index) into the
+// stage and one thread issues its two MMAs into TMEM columns 0..255.  The
+// layer-1 epilogue adds b1, the class row and the two scalar rows (kept in
+// shared memory as FP32 copies of the BF16 weights), applies the ReLU and
+// writes the BF16 layer-2 operand (64 KB); layer 2 accumulates into TMEM
+// columns 256..511; layer 3 and the sigmoid are the last epilogue, its two
+// column halves added through shared memory.  The same function as the
+// training forward (layer1_row), summed in another order.
 //
 // Barrier phases: chunk g of the CTA's sequence uses stage g % 6; its use
 // u = g / 6 completes `full` (copy landed) and, after the MMAs that read the

@@ -1,12 +1,15 @@
-// Test-only harness: the device excitation decoder (sfci_gb300/csrc/gen.cuh),
-// compiled for the host so that its enumeration, phases and matrix elements can
-// be checked on a CPU-only machine against the reference's emitted terms.
-// Built by tests/test_gen_host.py; not part of the library.
+// Test-only harness: the device excitation decoder (sfci_gb300/csrc/gen.cuh)
+// and the screen's term groups (sfci_gb300/csrc/screen.cuh), compiled for the
+// host so that their enumeration, phases and matrix elements can be checked on a
+// CPU-only machine against the reference's emitted terms.  Built by
+// tests/test_gen_host.py and tests/test_screen_host.py; not part of the library.
+#include <cmath>
 #include <cstring>
 #include <string>
 #include <vector>
 
 #include "gen.cuh"
+#include "screen.cuh"
 #include "internal.h"
 
 using namespace sfci;
@@ -164,6 +167,113 @@ extern "C" long gh_double_term_mismatches(const uint64_t* kw, int words) {
     DetInfo<K128> d;
     setup_host(d, K128{kw[0], kw[1]}, g_h.M, 0.37, 0.0);
     run(d);
+  }
+  return bad;
+}
+
+// The screen's term groups of one determinant.  Writes per group g >= 1 the row
+// (cls, p, q, r, start, size) into rows (6 ints a group, at most cap groups) and
+// per double-excitation term l in [c[2], c[5]) its target key words and
+// group_of_term(l) (at most tcap terms); returns the number of groups and sets
+// *bad to the number of failed checks: the groups tile [c[2], c[5]) in index
+// order, group_of_term maps each of their terms back to g, and each term's
+// excitation removes p and q and adds r (the larger added orbital of a
+// same-spin pair, the spin-0 one of an opposite-spin pair).
+template <class KT>
+static long groups_of(const KT& key, int N, int* rows, long cap, uint64_t* tk, unsigned* tg, long tcap,
+                      long* nterms, long* bad) {
+  static unsigned short pt[2016];
+  pair_table(pt);
+  DetInfo<KT> d;
+  setup_host(d, key, N / 2, 1.0, 0.0);
+  const GroupCounts gc = group_counts(d.h.na[0], d.h.nv[0], d.h.na[1], d.h.nv[1]);
+  const u64 ng = det_groups(d.h.na[0], d.h.nv[0], d.h.na[1], d.h.nv[1]);
+  const int W = (int)(sizeof(KT) / 8);
+  long nb = 0;
+  unsigned next = d.h.c[2];
+  for (unsigned g = 1; g < ng; ++g) {
+    const GroupDesc gd = group_desc(gc, d.h.c, g);
+    int p, q, r;
+    group_orbitals(key, N, gc, gd, p, q, r);
+    if ((long)g <= cap) {
+      int* o = rows + 6 * (g - 1);
+      o[0] = gd.cls, o[1] = p, o[2] = q, o[3] = r, o[4] = (int)gd.start, o[5] = (int)gd.size;
+    }
+    if (gd.start != next || gd.size == 0) ++nb;
+    next = gd.start + gd.size;
+    for (unsigned l = gd.start; l < gd.start + gd.size; ++l) {
+      if (group_of_term(gc, d.h.c, l) != g) ++nb;
+      const KT t = target_key(d.h, d, decode(d.h, pt, l));
+      int rem[4], add[4], nr = 0, na = 0;
+      for (int b = 0; b < N; ++b) {
+        const bool was = key_test(key, b), is = key_test(t, b);
+        if (was && !is && nr < 4) rem[nr++] = b;
+        if (is && !was && na < 4) add[na++] = b;
+      }
+      if (nr != 2 || na != 2) {
+        ++nb;
+        continue;
+      }
+      const bool pq = (rem[0] == p && rem[1] == q) || (rem[0] == q && rem[1] == p);
+      const int rr = gd.cls < 3 ? add[1] : ((add[0] & 1) ? add[1] : add[0]);
+      if (!pq || rr != r) ++nb;
+    }
+  }
+  if (next != d.h.c[5]) ++nb;
+  long nt = 0;
+  for (unsigned l = d.h.c[2]; l < d.h.c[5]; ++l, ++nt)
+    if (nt < tcap) {
+      const KT t = target_key(d.h, d, decode(d.h, pt, l));
+      for (int w = 0; w < W; ++w) tk[W * nt + w] = kword(t, w);
+      tg[nt] = group_of_term(gc, d.h.c, l);
+    }
+  *nterms = nt;
+  *bad = nb;
+  return (long)ng - 1;
+}
+
+extern "C" long gh_groups(const uint64_t* kw, int N, int* rows, long cap, uint64_t* tk, unsigned* tg, long tcap,
+                          long* nterms, long* bad) {
+  if (N <= 64) return groups_of<u64>(kw[0], N, rows, cap, tk, tg, tcap, nterms, bad);
+  return groups_of<K128>(K128{kw[0], kw[1]}, N, rows, cap, tk, tg, tcap, nterms, bad);
+}
+
+// unrank_pair for every k < n against the colex definition; select64 and
+// nth_orbital against a scan of the bits of random words.  Returns the failures.
+extern "C" long gh_screen_index_checks(unsigned n, uint64_t seed) {
+  long bad = 0;
+  for (unsigned k = 0; k < n; ++k) {
+    unsigned x, y;
+    unrank_pair(k, x, y);
+    if (!(x < y) || y * (y - 1) / 2 + x != k) ++bad;
+  }
+  uint64_t st = seed | 1;
+  auto rnd = [&]() {
+    st ^= st << 13;
+    st ^= st >> 7;
+    st ^= st << 17;
+    return st;
+  };
+  for (int it = 0; it < 20000; ++it) {
+    const u64 w = rnd() & rnd();
+    unsigned k = 0;
+    for (int b = 0; b < 64; ++b)
+      if ((w >> b) & 1ull) {
+        if (select64(w, k) != b) ++bad;
+        ++k;
+      }
+    if (select64(w, k) != -1) ++bad;
+    const K128 key{rnd(), rnd()};
+    for (int s = 0; s < 2; ++s)
+      for (int occ = 0; occ < 2; ++occ) {
+        unsigned kk = 0;
+        for (int b = s; b < 128; b += 2)
+          if (key_test(key, b) == (occ != 0)) {
+            if (nth_orbital(key, 128, s, occ != 0, kk) != b) ++bad;
+            ++kk;
+          }
+        if (nth_orbital(key, 128, s, occ != 0, kk) != -1) ++bad;
+      }
   }
   return bad;
 }

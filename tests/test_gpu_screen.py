@@ -70,7 +70,7 @@ def group_of_target(d, k, N):
     vir = [[b for b in range(s, N, 2) if not d >> b & 1] for s in (0, 1)]
     na = [len(o) for o in occ]
     nv = [len(v) for v in vir]
-    gss = [c2(na[s]) * (nv[s] - 1) for s in (0, 1)]
+    gss = [c2(na[s]) * (nv[s] - 1) if nv[s] else 0 for s in (0, 1)]
     if rb[0] % 2 == rb[1] % 2:  # same spin
         s = rb[0] % 2
         x, y = sorted(occ[s].index(b) for b in rb)

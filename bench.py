@@ -643,7 +643,7 @@ def run_screen(args):
 
 
 def run_lanczos(args):
-    """The whole truncated Lanczos ground-state solve of the configs' system
+    """The whole truncated Lanczos ground-state solve of the selected system
     (sparse_krylov_solve_eigenval as the sfci binary runs it, from |HF>):
     wall time, products, time per Krylov iteration and the energies."""
     import sfci_gb300 as sg

@@ -269,8 +269,8 @@ int sfci_autotune(sfci_ctx* ctx, const sfci_vec* in, sfci_vec* out, int* best4, 
  * generator of OffDiagGen_bit (src/bitstr.cpp:162-302) restricted to the kept
  * groups.  Threshold 0 keeps every group and gives the plain product exactly;
  * products with extra sources (sfci_spmspv_linear, sfci_res_norm) and
- * sfci_energy are never screened, so calc_energy stays the judge of a screened
- * run's energy. */
+ * sfci_energy are never screened, so calc_energy stays an unscreened check of a
+ * screened run's energy. */
 typedef struct sfci_screen sfci_screen;
 /* A screen lives on the context it is created on; destroying that context first
  * frees the screen's device memory and leaves a handle that only

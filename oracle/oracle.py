@@ -2,7 +2,8 @@
 
 Nothing in the product imports this module; only ``tests/``,
 ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg use it, and only
-as the checker / the timed CPU reference.
+as the oracle the GPU results are compared with, or as the timed CPU
+reference.
 
 Two CPU backends with one interface:
 

@@ -1,7 +1,7 @@
 // Oracle restatement of the SFCI hot path — TEST INFRASTRUCTURE ONLY.
 //
 // A C++/OpenMP restatement of the reference algorithm, used by the tests as the
-// checker and by bench.py as the timed CPU baseline ("port").  Nothing in the
+// oracle and by bench.py as the timed CPU baseline ("port").  Nothing in the
 // product links it.  It follows the reference function by function, with each
 // step citing the reference line it restates, and generalises the determinant
 // type to 128 bits so that it also covers systems beyond 64 spin orbitals

@@ -1,6 +1,6 @@
 """bench.py's multi-rank plumbing on CPU: two gloo ranks on 127.0.0.1, the
 max-over-ranks timing reduction and the barrier the timed region is bracketed by.
-On the GPU machine the same functions run over NCCL, one rank per GPU, each rank an
+On a GPU machine the same functions run over NCCL, one rank per GPU, each rank an
 independent replica of the product (no data-path collective)."""
 import multiprocessing as mp
 import os

@@ -30,7 +30,7 @@ CUT = 1e-5
 
 
 def test_lanczos_56_orbital_system_truncating(golden_in):
-    """configs[1]'s system at Nd = 2e4, Nl = 30: the energies of every restart and
+    """The 56-spin-orbital system at Nd = 2e4, Nl = 30: the energies of every restart and
     the final calc_energy against the reference driver.  The reference's signed
     convergence test (previousE - E < dE with previousE = 0, :535) ends a run
     with a positive energy after its first restart, and so does this one.  The
@@ -48,7 +48,7 @@ def test_lanczos_56_orbital_system_truncating(golden_in):
     en = en[~np.isnan(en)]
     ref, alt = g["L_energies"], g["P_energies"]
     spread = float(np.max(np.abs(ref - alt))) if len(alt) == len(ref) else float("nan")
-    print("configs[1] Lanczos at Nd=%d: GPU %s (final %.12f), reference %s (final %.12f), "
+    print("56-spin-orbital Lanczos at Nd=%d: GPU %s (final %.12f), reference %s (final %.12f), "
           "max |GPU - reference| %.3e, tie-breaking spread of the CPU runs %.3e"
           % (int(g["L_Nd"]), en, fe, ref, float(g["L_final_e"]), np.max(np.abs(en - ref)), spread))
     assert len(en) == len(ref)
@@ -84,7 +84,7 @@ def _sample_vector(rng, N, ne, n):
     return ints, amps / np.linalg.norm(amps)
 
 
-def test_configs2_system_products_lanczos_and_minres(sys128, port):
+def test_128_orbital_system_products_lanczos_and_minres(sys128, port):
     N, ne = 128, 20
     rng = np.random.default_rng(23)
     ints, amps = _sample_vector(rng, N, ne, 1000)

@@ -277,3 +277,10 @@ extern "C" long gh_screen_index_checks(unsigned n, uint64_t seed) {
   }
   return bad;
 }
+
+// The integer magnitude cut of the compactions (common.cuh: cut_key, above_cut)
+// for n values against one cut: out[i] = above_cut(x[i], cut_key(cut)).
+extern "C" void gh_above_cut(const double* x, long n, double cut, unsigned char* out) {
+  const long long ck = cut_key(cut);
+  for (long i = 0; i < n; ++i) out[i] = above_cut(x[i], ck) ? 1 : 0;
+}

@@ -37,6 +37,8 @@ def fx(tmp_path_factory):
     L.gh_fx_roundtrip.argtypes = [C.c_double, C.POINTER(C.c_int)]
     L.gh_fx32_sum.restype = C.c_double
     L.gh_fx32_sum.argtypes = [np.ctypeslib.ndpointer(np.float64), C.c_long, C.POINTER(C.c_int)]
+    L.gh_above_cut.argtypes = [np.ctypeslib.ndpointer(np.float64), C.c_long, C.c_double,
+                               np.ctypeslib.ndpointer(np.uint8)]
     return L
 
 
@@ -186,3 +188,23 @@ def test_digit_form_capacity_and_range(fx32):
         assert got == sign * float(Fraction(to_grid(big)) * n / (1 << FRAC))
     for x in (math.ldexp(1.0, 18), -3e5, float("inf"), float("nan")):
         assert f32sum(fx32, np.array([x]))[1] == 1
+
+
+def test_integer_magnitude_cut(fx):
+    """The prunes and compactions test |a| > cut as an integer compare of the bits of
+    |a| against those of the cut (cut_key / above_cut).  For every finite amplitude,
+    signed zeros, subnormals, infinities and values one ulp either side of the cut
+    included, it must agree with the floating-point compare; a negative cut keeps
+    everything."""
+    rng = np.random.default_rng(7)
+    for cut in (1e-5, 1e-8, 0.0, 5e-324, 1.0, 1e300, -1.0):
+        mags = 10.0 ** rng.uniform(-330, 308, 20000)
+        x = np.concatenate([mags * rng.choice([-1.0, 1.0], mags.size),
+                            [0.0, -0.0, 5e-324, -5e-324, np.inf, -np.inf, 2.2e-308, -1.1e-308]])
+        if cut >= 0:
+            near = [cut, np.nextafter(cut, np.inf), np.nextafter(cut, 0.0) if cut > 0 else 0.0]
+            x = np.concatenate([x, near, [-v for v in near]])
+        x = np.ascontiguousarray(x, np.float64)
+        out = np.zeros(x.size, np.uint8)
+        fx.gh_above_cut(x, x.size, cut, out)
+        np.testing.assert_array_equal(out.astype(bool), np.abs(x) > cut)

@@ -216,9 +216,16 @@ INST_SHIFT = 59  # instance tag: the top five bits of a batched context's two-wo
 
 
 def tag_keys(keys, inst: int):
-    """Two-word keys (n, 2) of batched instance `inst` (bits 123..127 of the key)."""
+    """Two-word keys (n, 2) of batched instance `inst` (bits 123..127 of the key).
+    ValueError for an instance outside 0..31 or a key that already sets one of
+    the tag bits."""
+    inst = int(inst)
+    if not 0 <= inst < 32:
+        raise ValueError("batched instance %d outside 0..31" % inst)
     k = np.array(keys, dtype=np.uint64, copy=True).reshape(-1, 2)
-    k[:, 1] |= np.uint64(int(inst) << INST_SHIFT)
+    if k.size and np.any(k[:, 1] >> np.uint64(INST_SHIFT)):
+        raise ValueError("keys already use the instance bits 123..127")
+    k[:, 1] |= np.uint64(inst << INST_SHIFT)
     return k
 
 

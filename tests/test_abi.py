@@ -93,6 +93,19 @@ def test_keys_roundtrip_helpers():
     assert sg.ints_from_keys(k) == ints
 
 
+def test_tag_keys_checks_instance_and_tag_bits():
+    k = sg.keys_from_ints([(1 << 119) | 7, 3], 2)
+    t = sg.tag_keys(k, 31)
+    assert sg.ints_from_keys(t) == [(31 << 123) | (1 << 119) | 7, (31 << 123) | 3]
+    assert sg.ints_from_keys(sg.tag_keys(k, 0)) == sg.ints_from_keys(k)
+    assert sg.tag_keys(np.zeros((0, 2), np.uint64), 5).shape == (0, 2)
+    for bad in (-1, 32):
+        with pytest.raises(ValueError):
+            sg.tag_keys(k, bad)
+    with pytest.raises(ValueError):
+        sg.tag_keys(t, 1)
+
+
 def test_solver_entry_points_reject_null_arguments():
     """Argument checks of the linear-solver and subspace entry points run before
     any device call."""

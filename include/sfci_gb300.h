@@ -94,7 +94,10 @@ int sfci_vec_destroy(sfci_vec* v);
 int sfci_vec_len(const sfci_vec* v, uint64_t* len);
 int sfci_vec_cap(const sfci_vec* v, uint64_t* cap);
 /* Host -> device: keys (len * key_words words) and amplitudes.  The vector is
- * sorted by key on the device if it is not already (dynVec keeps key order). */
+ * sorted by key on the device if it is not already (dynVec keeps key order).
+ * In a batched context every key must carry the tag of one of its instances
+ * and no bit at or above that instance's num_orb, else SFCI_ERR_ARG before any
+ * copy. */
 int sfci_vec_upload(sfci_vec* v, const uint64_t* keys, const double* amps, uint64_t len);
 /* Device -> host: copies min(len, cap) entries, reports len. */
 int sfci_vec_download(const sfci_vec* v, uint64_t* keys, double* amps, uint64_t cap,

@@ -589,6 +589,13 @@ int sfci_vec_upload(sfci_vec* v, const uint64_t* keys, const double* amps, uint6
   if (len && (!keys || !amps)) return set_error(SFCI_ERR_ARG, "null host buffers");
   if (len > v->v.cap) return set_error(SFCI_ERR_CAPACITY, "upload longer than vector capacity");
   Ctx& c = *v->v.ctx;
+  if (len && c.ninst) {
+    const u64 bad = first_bad_batched_key((const u64*)keys, len, c.inst_N.data(), c.ninst);
+    if (bad < len)
+      return set_error(SFCI_ERR_ARG, "key " + std::to_string(bad) +
+                                         " names no instance of the batch or sets a bit beyond its instance's "
+                                         "spin orbitals");
+  }
   if (len) {
     SFCI_CUDA(cudaMemcpyAsync(v->v.keys, keys, len * c.W * sizeof(u64), cudaMemcpyHostToDevice, c.stream));
     SFCI_CUDA(cudaMemcpyAsync(v->v.amps, amps, len * sizeof(double), cudaMemcpyHostToDevice, c.stream));

@@ -52,6 +52,23 @@ SFCI_HD HamView ham_for(const HamView& h, const KT& k) {
   return h.inst ? h.inst[inst_of(k)] : h;
 }
 
+// Host check of two-word keys (lo, hi word pairs) entering a batched context,
+// whose kernels index the per-instance tables by the tag: the index of the
+// first key whose tag names no instance (tag >= ninst) or that sets a bit at
+// or above its instance's spin-orbital count inst_N[tag]; n when all are valid.
+inline u64 first_bad_batched_key(const u64* kw, u64 n, const int* inst_N, int ninst) {
+  const u64 body = (1ull << INST_SHIFT) - 1ull;
+  for (u64 i = 0; i < n; ++i) {
+    const u64 lo = kw[2 * i], hi = kw[2 * i + 1];
+    const u64 t = hi >> INST_SHIFT;
+    if (t >= (u64)ninst) return i;
+    const int N = inst_N[t];
+    const bool over = N >= 64 ? ((hi & body) >> (N - 64)) != 0ull : ((hi & body) != 0ull || (lo >> N) != 0ull);
+    if (over) return i;
+  }
+  return n;
+}
+
 // Single-excitation descriptor of spin orbitals i (occupied) -> a (empty):
 // i | a << 7 | spatial_pair(i>>1, a>>1) << 14 | phase << 26, where the phase
 // bit is the parity of the occupied orbitals strictly between i and a.

@@ -284,3 +284,9 @@ extern "C" void gh_above_cut(const double* x, long n, double cut, unsigned char*
   const long long ck = cut_key(cut);
   for (long i = 0; i < n; ++i) out[i] = above_cut(x[i], ck) ? 1 : 0;
 }
+
+// The batched-key check of uploads (gen.cuh: first_bad_batched_key).
+extern "C" unsigned long long gh_first_bad_batched_key(const uint64_t* kw, unsigned long long n, const int* inst_N,
+                                                       int ninst) {
+  return first_bad_batched_key((const u64*)kw, n, inst_N, ninst);
+}

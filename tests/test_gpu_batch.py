@@ -80,6 +80,25 @@ def test_batched_product_equals_unbatched_products(curve):
         assert np.array_equal(aa[sel].view(np.uint64), want[k][1].view(np.uint64)), k
 
 
+def test_upload_rejects_keys_outside_the_batch(curve):
+    """Uploads check keys on the host before any copy: a tag naming no instance,
+    or a bit at or above its instance's spin orbitals, is SFCI_ERR_ARG and the
+    vector keeps its contents."""
+    orbs = [2 * M for M, _, _, _ in INSTANCES]
+    nes = [ne for _, ne, _, _ in INSTANCES]
+    bc = sg.Context.batch(curve, orbs, nes, Nd=10 ** 4)
+    v = bc.vec(4)
+    good = hf_tagged(nes[0], 0)
+    v.upload(good, np.array([1.0]))
+    bad_tag = np.array([[1, np.uint64(len(INSTANCES)) << np.uint64(sg.INST_SHIFT)]], np.uint64)
+    bad_bit = sg.tag_keys(sg.keys_from_ints([1 << orbs[1]], 2), 1)
+    for bad in (bad_tag, bad_bit):
+        with pytest.raises(sg.SfciError) as e:
+            v.upload(np.concatenate([good, bad]), np.array([1.0, 1.0]))
+        assert e.value.status == "SFCI_ERR_ARG"
+        assert len(v) == 1
+
+
 @pytest.mark.parametrize("cap", [2000000, 3000])
 def test_batched_lanczos_matches_unbatched_runs(curve, cap):
     """cap is every instance's hpsi_cap; at 3000 it cuts each instance's

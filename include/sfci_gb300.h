@@ -132,7 +132,8 @@ int sfci_vec_clear(sfci_vec* v);                                   /* setZeroVec
  * SFCI_ERR_UNSUPPORTED. */
 int sfci_spmspv(sfci_ctx* ctx, const sfci_vec* in, sfci_vec* out, double lambda, double coeff,
                 double* diag);
-/* DiagCal_bit (src/bitstr.cpp:433-476) for `n` host keys. */
+/* DiagCal_bit (src/bitstr.cpp:433-476) for `n` host keys (checked like
+ * sfci_vec_upload's in a batched context). */
 int sfci_diag_elements(sfci_ctx* ctx, const uint64_t* keys, uint64_t n, double* out);
 /* calc_energy (src/functions.cpp:1272-1313): <psi|H|psi> on psi's support. */
 int sfci_energy(sfci_ctx* ctx, const sfci_vec* psi, double* energy);
@@ -198,7 +199,8 @@ int sfci_shift_invert(sfci_ctx* ctx, sfci_vec* b, double target_energy, int num_
  * (capacity >= *block_size, which is set before the capacity check); evals
  * [0..n_evals) the lowest eigenvalues ascending (the reference prints 10);
  * *resid (nullable) the norm of H x - E x.  The eigenvector sign is fixed so that
- * its largest component is positive. */
+ * its largest component is positive.  Ordinary contexts only (a batched context
+ * is SFCI_ERR_UNSUPPORTED), as for sfci_fci. */
 int sfci_cisd(sfci_ctx* ctx, const uint64_t* ref_key, int state_idx, int n_evals, double* evals,
               sfci_vec* out, double* resid, uint64_t* block_size);
 /* fci (src/dense_algo.cpp:77-124) over generateBasis (:55-74): lowest eigenvalues

@@ -644,6 +644,13 @@ int sfci_diag_elements(sfci_ctx* x, const uint64_t* keys, uint64_t n, double* ou
   if (!x || (n && (!keys || !out))) return set_error(SFCI_ERR_ARG, "null argument");
   if (!n) return SFCI_OK;
   Ctx& c = x->c;
+  if (c.ninst) {
+    const u64 bad = first_bad_batched_key((const u64*)keys, n, c.inst_N.data(), c.ninst);
+    if (bad < n)
+      return set_error(SFCI_ERR_ARG, "key " + std::to_string(bad) +
+                                         " names no instance of the batch or sets a bit beyond its instance's "
+                                         "spin orbitals");
+  }
   void* dk = scratch_get(c, "de_keys", n * c.W * sizeof(u64));
   if (!dk) return SFCI_ERR_NOMEM;
   SFCI_CUDA(cudaMemcpyAsync(dk, keys, n * c.W * sizeof(u64), cudaMemcpyHostToDevice, c.stream));
@@ -686,6 +693,7 @@ int sfci_cisd(sfci_ctx* x, const uint64_t* ref_key, int state_idx, int n_evals, 
     return set_error(SFCI_ERR_ARG, "bad cisd arguments");
   if (out->v.ctx != &x->c) return set_error(SFCI_ERR_ARG, "output vector belongs to another context");
   Ctx& c = x->c;
+  if (c.ninst) return set_error(SFCI_ERR_UNSUPPORTED, "cisd takes an ordinary (single-Hamiltonian) context");
   return SFCI_W(c, cisd_impl, c, (const u64*)ref_key, state_idx, n_evals, evals, out->v, resid, (u64*)block_size);
 }
 
@@ -694,6 +702,7 @@ int sfci_fci(sfci_ctx* x, int n_evals, double* evals, sfci_vec* ground, double* 
   if (ground && (vec_check(ground) || ground->v.ctx != &x->c))
     return set_error(SFCI_ERR_ARG, "ground vector belongs to another context");
   Ctx& c = x->c;
+  if (c.ninst) return set_error(SFCI_ERR_UNSUPPORTED, "fci takes an ordinary (single-Hamiltonian) context");
   return SFCI_W(c, fci_impl, c, n_evals, evals, ground ? &ground->v : nullptr, resid, (u64*)dim);
 }
 

@@ -9,6 +9,8 @@ product over all of them per Krylov step.
   energies within 1e-10 Eh of an unbatched run of the same instance.
 * The autotuner times product plans and keeps one; every plan gives the same
   product bit for bit.
+* Host keys whose tag names no instance, or that set a bit beyond their
+  instance's spin orbitals, are rejected before they reach the device.
 """
 import numpy as np
 import pytest
@@ -81,9 +83,9 @@ def test_batched_product_equals_unbatched_products(curve):
 
 
 def test_upload_rejects_keys_outside_the_batch(curve):
-    """Uploads check keys on the host before any copy: a tag naming no instance,
-    or a bit at or above its instance's spin orbitals, is SFCI_ERR_ARG and the
-    vector keeps its contents."""
+    """Uploads (and DiagCal_bit's host keys) are checked on the host before any
+    copy: a tag naming no instance, or a bit at or above its instance's spin
+    orbitals, is SFCI_ERR_ARG and the vector keeps its contents."""
     orbs = [2 * M for M, _, _, _ in INSTANCES]
     nes = [ne for _, ne, _, _ in INSTANCES]
     bc = sg.Context.batch(curve, orbs, nes, Nd=10 ** 4)
@@ -97,6 +99,9 @@ def test_upload_rejects_keys_outside_the_batch(curve):
             v.upload(np.concatenate([good, bad]), np.array([1.0, 1.0]))
         assert e.value.status == "SFCI_ERR_ARG"
         assert len(v) == 1
+        with pytest.raises(sg.SfciError) as e:
+            bc.DiagCal_bit(np.concatenate([good, bad]))
+        assert e.value.status == "SFCI_ERR_ARG"
 
 
 @pytest.mark.parametrize("cap", [2000000, 3000])

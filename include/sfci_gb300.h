@@ -15,7 +15,11 @@
  *
  * Every call returns SFCI_OK (0) or a negative status; sfci_last_error()
  * returns a message for the calling thread's last failure.  A context is used
- * from one host thread at a time.
+ * from one host thread at a time.  Vectors passed to a call together with a
+ * context must have been created on it (SFCI_ERR_ARG otherwise: another
+ * context's keys may have another width); sfci_vec_copy needs both vectors on
+ * one context.  The screen's label log alone takes vectors of another context
+ * over the same number of orbitals.
  */
 #ifndef SFCI_GB300_H
 #define SFCI_GB300_H

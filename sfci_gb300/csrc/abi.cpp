@@ -385,6 +385,7 @@ int sfci_ctx_get_tuning(const sfci_ctx* x, int* t4) {
 
 int sfci_autotune(sfci_ctx* x, const sfci_vec* in, sfci_vec* out, int* best4, double* best_ms) {
   if (!x || !in || !out) return set_error(SFCI_ERR_ARG, "null argument");
+  if (vec_of(x, in) || vec_of(x, out)) return SFCI_ERR_ARG;
   Ctx& c = x->c;
   // candidates: level-1 bins, partition digit width, leaf size, generation occupancy
   static const int cand[][4] = {{9, 9, 120, 2}, {9, 8, 120, 2}, {8, 9, 120, 2}, {9, 9, 80, 2},
@@ -623,6 +624,7 @@ int sfci_vec_download(const sfci_vec* v, uint64_t* keys, double* amps, uint64_t 
 
 int sfci_vec_copy(sfci_vec* dst, const sfci_vec* src) {
   if (vec_check(dst) || vec_check(src)) return SFCI_ERR_ARG;
+  if (dst->v.ctx != src->v.ctx) return set_error(SFCI_ERR_ARG, "copy between vectors of different contexts");
   return op_copy(*dst->v.ctx, dst->v, src->v);
 }
 
@@ -635,7 +637,8 @@ int sfci_vec_clear(sfci_vec* v) {
 // ---- hot path -----------------------------------------------------------------
 
 int sfci_spmspv(sfci_ctx* x, const sfci_vec* in, sfci_vec* out, double lambda, double coeff, double* diag) {
-  if (!x || vec_check(in) || vec_check(out) || !diag) return set_error(SFCI_ERR_ARG, "null argument");
+  if (!x || !diag) return set_error(SFCI_ERR_ARG, "null argument");
+  if (vec_of(x, in) || vec_of(x, out)) return SFCI_ERR_ARG;
   if (in == out) return set_error(SFCI_ERR_ARG, "spmspv input and output must differ");
   return op_spmspv(x->c, in->v, out->v, lambda, coeff, diag);
 }
@@ -658,7 +661,8 @@ int sfci_diag_elements(sfci_ctx* x, const uint64_t* keys, uint64_t n, double* ou
 }
 
 int sfci_energy(sfci_ctx* x, const sfci_vec* psi, double* E) {
-  if (!x || vec_check(psi) || !E) return set_error(SFCI_ERR_ARG, "null argument");
+  if (!x || !E) return set_error(SFCI_ERR_ARG, "null argument");
+  if (vec_of(x, psi)) return SFCI_ERR_ARG;
   return op_energy(x->c, psi->v, E);
 }
 
@@ -666,12 +670,12 @@ int sfci_energy(sfci_ctx* x, const sfci_vec* psi, double* E) {
 
 int sfci_spmspv_linear(sfci_ctx* x, const sfci_vec* in, sfci_vec* out, double lambda, const sfci_vec* const* basis,
                        int nbasis, double* hij) {
-  if (!x || vec_check(in) || vec_check(out) || !basis || nbasis < 1 || nbasis > 64 || !hij)
-    return set_error(SFCI_ERR_ARG, "bad spmspv_linear arguments");
+  if (!x || !basis || nbasis < 1 || nbasis > 64 || !hij) return set_error(SFCI_ERR_ARG, "bad spmspv_linear arguments");
+  if (vec_of(x, in) || vec_of(x, out)) return SFCI_ERR_ARG;
   if (in == out) return set_error(SFCI_ERR_ARG, "spmspv_linear input and output must differ");
   std::vector<const Vec*> bp(nbasis);
   for (int j = 0; j < nbasis; ++j) {
-    if (vec_check(basis[j])) return SFCI_ERR_ARG;
+    if (vec_of(x, basis[j])) return SFCI_ERR_ARG;
     if (basis[j] == out) return set_error(SFCI_ERR_ARG, "spmspv_linear output is one of the basis vectors");
     bp[j] = &basis[j]->v;
   }
@@ -679,8 +683,8 @@ int sfci_spmspv_linear(sfci_ctx* x, const sfci_vec* in, sfci_vec* out, double la
 }
 
 int sfci_res_norm(sfci_ctx* x, const sfci_vec* xv, sfci_vec* r, const sfci_vec* b, double lambda, double* res) {
-  if (!x || vec_check(xv) || vec_check(r) || vec_check(b) || !res)
-    return set_error(SFCI_ERR_ARG, "bad res_norm arguments");
+  if (!x || !res) return set_error(SFCI_ERR_ARG, "bad res_norm arguments");
+  if (vec_of(x, xv) || vec_of(x, r) || vec_of(x, b)) return SFCI_ERR_ARG;
   if (r == xv || r == b) return set_error(SFCI_ERR_ARG, "res_norm output must differ from its inputs");
   return op_res_norm(x->c, xv->v, r->v, b->v, lambda, res);
 }
@@ -707,22 +711,26 @@ int sfci_fci(sfci_ctx* x, int n_evals, double* evals, sfci_vec* ground, double* 
 }
 
 int sfci_dot(sfci_ctx* x, const sfci_vec* a, const sfci_vec* b, double* out) {
-  if (!x || vec_check(a) || vec_check(b) || !out) return set_error(SFCI_ERR_ARG, "null argument");
+  if (!x || !out) return set_error(SFCI_ERR_ARG, "null argument");
+  if (vec_of(x, a) || vec_of(x, b)) return SFCI_ERR_ARG;
   return op_dot(x->c, a->v, b->v, out);
 }
 
 int sfci_norm(sfci_ctx* x, const sfci_vec* v, double* out) {
-  if (!x || vec_check(v) || !out) return set_error(SFCI_ERR_ARG, "null argument");
+  if (!x || !out) return set_error(SFCI_ERR_ARG, "null argument");
+  if (vec_of(x, v)) return SFCI_ERR_ARG;
   return norm_impl(x->c, v->v, out);
 }
 
 int sfci_scale(sfci_ctx* x, sfci_vec* v, double a) {
-  if (!x || vec_check(v)) return set_error(SFCI_ERR_ARG, "null argument");
+  if (!x) return set_error(SFCI_ERR_ARG, "null argument");
+  if (vec_of(x, v)) return SFCI_ERR_ARG;
   return scale_impl(x->c, v->v, a);
 }
 
 int sfci_normalize(sfci_ctx* x, sfci_vec* v) {
-  if (!x || vec_check(v)) return set_error(SFCI_ERR_ARG, "null argument");
+  if (!x) return set_error(SFCI_ERR_ARG, "null argument");
+  if (vec_of(x, v)) return SFCI_ERR_ARG;
   double n = 0;
   int st = norm_impl(x->c, v->v, &n);
   if (st) return st;
@@ -730,28 +738,31 @@ int sfci_normalize(sfci_ctx* x, sfci_vec* v) {
 }
 
 int sfci_add_two(sfci_ctx* x, sfci_vec* v, const sfci_vec* w, double a) {
-  if (!x || vec_check(v) || vec_check(w)) return set_error(SFCI_ERR_ARG, "null argument");
+  if (!x) return set_error(SFCI_ERR_ARG, "null argument");
+  if (vec_of(x, v) || vec_of(x, w)) return SFCI_ERR_ARG;
   return op_add_two(x->c, v->v, w->v, a);
 }
 
 int sfci_add_three(sfci_ctx* x, sfci_vec* v, const sfci_vec* a, const sfci_vec* b, const sfci_vec* cc, double ca,
                    double cb, double c3) {
-  if (!x || vec_check(v) || vec_check(a) || vec_check(b) || vec_check(cc))
-    return set_error(SFCI_ERR_ARG, "null argument");
+  if (!x) return set_error(SFCI_ERR_ARG, "null argument");
+  if (vec_of(x, v) || vec_of(x, a) || vec_of(x, b) || vec_of(x, cc)) return SFCI_ERR_ARG;
   return op_add_three(x->c, v->v, a->v, b->v, cc->v, ca, cb, c3);
 }
 
 int sfci_shrink_from(sfci_ctx* x, sfci_vec* dst, const sfci_vec* src) {
-  if (!x || vec_check(dst) || vec_check(src)) return set_error(SFCI_ERR_ARG, "null argument");
+  if (!x) return set_error(SFCI_ERR_ARG, "null argument");
+  if (vec_of(x, dst) || vec_of(x, src)) return SFCI_ERR_ARG;
   if (dst == src) return set_error(SFCI_ERR_ARG, "shrink_from needs distinct vectors");
   return op_shrink(x->c, dst->v, src->v);
 }
 
 int sfci_combine(sfci_ctx* x, sfci_vec* dst, const sfci_vec* const* vs, const double* coef, int n) {
-  if (!x || vec_check(dst) || n < 0 || (n && (!vs || !coef))) return set_error(SFCI_ERR_ARG, "null argument");
+  if (!x || n < 0 || (n && (!vs || !coef))) return set_error(SFCI_ERR_ARG, "null argument");
+  if (vec_of(x, dst)) return SFCI_ERR_ARG;
   std::vector<const Vec*> p(n);
   for (int i = 0; i < n; ++i) {
-    if (vec_check(vs[i])) return SFCI_ERR_ARG;
+    if (vec_of(x, vs[i])) return SFCI_ERR_ARG;
     p[i] = &vs[i]->v;
   }
   return op_combine(x->c, dst->v, p.data(), coef, n);

@@ -125,6 +125,15 @@ struct sfci_vec {
   sfci::Vec v;
 };
 
+// A vector passed to an entry point with a context must belong to that
+// context: another context's vectors may hold keys of another width or tags of
+// another batch.  SFCI_OK, or SFCI_ERR_ARG with the error text set.
+inline int vec_of(const sfci_ctx* x, const sfci_vec* v) {
+  if (!v || !v->v.ctx) return sfci::set_error(SFCI_ERR_ARG, "null vector");
+  if (v->v.ctx != &x->c) return sfci::set_error(SFCI_ERR_ARG, "vector belongs to another context");
+  return SFCI_OK;
+}
+
 #define SFCI_CUDA(call)                                         \
   do {                                                          \
     cudaError_t e_ = (call);                                    \

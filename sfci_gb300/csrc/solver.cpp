@@ -416,6 +416,7 @@ int sfci_gsaes(int n, const double* K, const double* S, double* evals, double* e
 int sfci_lanczos_ground(sfci_ctx* x, sfci_vec* v, int Nl, int restarts, double* energies, double* final_e) {
   if (!x || !v || !energies || !final_e || Nl < 1 || restarts < 1)
     return set_error(SFCI_ERR_ARG, "bad lanczos arguments");
+  if (vec_of(x, v)) return SFCI_ERR_ARG;
   if (v->v.len == 0) return set_error(SFCI_ERR_ARG, "lanczos start vector is empty");
   return lanczos_ground(x->c, v->v, Nl, restarts, energies, final_e);
 }
@@ -424,6 +425,7 @@ int sfci_krylov_linear(sfci_ctx* x, const sfci_vec* b, sfci_vec* result, double 
                        int num_restart, double* residues) {
   if (!x || !b || !result || num_iter < 1 || num_iter > 63 || num_restart < 1 || b == result)
     return set_error(SFCI_ERR_ARG, "bad krylov_linear arguments");
+  if (vec_of(x, b) || vec_of(x, result)) return SFCI_ERR_ARG;
   if (b->v.len == 0) return set_error(SFCI_ERR_ARG, "krylov_linear right-hand side is empty");
   return krylov_linear(x->c, b->v, result->v, target_energy, num_iter, num_restart, residues);
 }
@@ -431,6 +433,7 @@ int sfci_krylov_linear(sfci_ctx* x, const sfci_vec* b, sfci_vec* result, double 
 int sfci_shift_invert(sfci_ctx* x, sfci_vec* b, double target_energy, int num_iter, int num_restart, double* energy) {
   if (!x || !b || !energy || num_iter < 1 || num_iter > 63 || num_restart < 1)
     return set_error(SFCI_ERR_ARG, "bad shift_invert arguments");
+  if (vec_of(x, b)) return SFCI_ERR_ARG;
   if (b->v.len == 0) return set_error(SFCI_ERR_ARG, "shift_invert start vector is empty");
   return shift_invert(x->c, b->v, target_energy, num_iter, num_restart, energy);
 }
@@ -438,6 +441,7 @@ int sfci_shift_invert(sfci_ctx* x, sfci_vec* b, double target_energy, int num_it
 int sfci_minres(sfci_ctx* x, const sfci_vec* rhs, const sfci_vec* guess, sfci_vec* result, int iters, double tol,
                 double lambda, int* iters_done) {
   if (!x || !rhs || !guess || !result || iters < 0) return set_error(SFCI_ERR_ARG, "bad minres arguments");
+  if (vec_of(x, rhs) || vec_of(x, guess) || vec_of(x, result)) return SFCI_ERR_ARG;
   return minres(x->c, rhs->v, guess->v, result->v, iters, tol, lambda, iters_done);
 }
 

@@ -126,6 +126,23 @@ def test_minres_matches_oracle(golden_in, port):
     compare_vectors(xk, xa, k, a, capped=len(xa) == Nd, rtol=1e-9, atol=1e-12)
 
 
+def test_vectors_of_another_context_are_rejected(golden_in):
+    """Entry points taking a context check that its vectors belong to it (another
+    context's keys may have another width) before any device work."""
+    g, path, c = ctx_for(golden_in, "c1")
+    c2 = sg.Context(path, 2 * int(g["M"]), int(g["ne"]), Nd=1000)
+    v = c.vec_from(np.array([g["hf"]], np.uint64), np.array([1.0]))
+    w = c2.vec_from(np.array([g["hf"]], np.uint64), np.array([1.0]))
+    out2 = c2.vec(10)
+    for call in (lambda: c2.SpMVMtply_bucket(v, out2, 0.0, 1.0), lambda: v.dot(w), lambda: v.addTwo(w, 1.0),
+                 lambda: w.naiveCopy(v), lambda: c2.calc_energy(v)):
+        with pytest.raises(sg.SfciError) as e:
+            call()
+        assert e.value.status == "SFCI_ERR_ARG"
+    assert v.len == 1 and w.len == 1 and out2.len == 0
+    assert close(v.dot(v), 1.0)
+
+
 def test_empty_input_leaves_diag_untouched(golden_in):
     g, path, c = ctx_for(golden_in, "c1")
     vin = c.vec(10)

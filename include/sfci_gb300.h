@@ -93,6 +93,7 @@ int sfci_ctx_profile_reset(sfci_ctx* ctx);
 int sfci_ctx_last_stats(const sfci_ctx* ctx, uint64_t stats[8]);
 
 /* ---- sparse vectors (dynVec, src/all.h:150-625) ------------------------------ */
+/* A device vector of capacity cap (at most 2^40 entries, else SFCI_ERR_ARG). */
 int sfci_vec_create(sfci_ctx* ctx, uint64_t cap, sfci_vec** out);
 int sfci_vec_destroy(sfci_vec* v);
 int sfci_vec_len(const sfci_vec* v, uint64_t* len);

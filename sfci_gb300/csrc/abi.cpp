@@ -545,6 +545,8 @@ int sfci_ctx_last_stats(const sfci_ctx* x, uint64_t stats[8]) {
 int sfci_vec_create(sfci_ctx* x, uint64_t cap, sfci_vec** out) {
   if (!x || !out) return set_error(SFCI_ERR_ARG, "null argument");
   *out = nullptr;
+  // bounds the byte sizes below far from overflow (2^40 entries: 26 TB)
+  if (cap > (1ull << 40)) return set_error(SFCI_ERR_ARG, "vector capacity beyond 2^40 entries");
   sfci_vec* v = new sfci_vec();
   v->v.ctx = &x->c;
   v->v.cap = cap;

@@ -123,6 +123,16 @@ def test_solver_entry_points_reject_null_arguments():
     assert name(L.sfci_ctx_set_screen_floor(None, 1e-8)) == "SFCI_ERR_ARG"
 
 
+def test_vec_create_rejects_oversized_capacity_without_a_device_call():
+    """A capacity beyond 2^40 entries is SFCI_ERR_ARG before the context is read
+    (the placeholder context address is never dereferenced)."""
+    L = sg.load_library()
+    h = C.c_void_p()
+    st = L.sfci_vec_create(C.c_void_p(16), (1 << 40) + 1, C.byref(h))
+    assert L.sfci_status_name(st).decode() == "SFCI_ERR_ARG" and not h.value
+    assert L.sfci_status_name(L.sfci_vec_create(None, 1, C.byref(h))).decode() == "SFCI_ERR_ARG"
+
+
 def test_dot_noalloc_rejects_bad_arguments_without_a_device_call():
     """sfci_dot_noalloc checks its arguments before any CUDA call: null pointers,
     a key width other than 1 or 2 words, and sizes beyond the fixed scratch

@@ -648,6 +648,7 @@ int sfci_spmspv(sfci_ctx* x, const sfci_vec* in, sfci_vec* out, double lambda, d
 int sfci_diag_elements(sfci_ctx* x, const uint64_t* keys, uint64_t n, double* out) {
   if (!x || (n && (!keys || !out))) return set_error(SFCI_ERR_ARG, "null argument");
   if (!n) return SFCI_OK;
+  if (n > (1ull << 40)) return set_error(SFCI_ERR_ARG, "more than 2^40 keys");
   Ctx& c = x->c;
   if (c.ninst) {
     const u64 bad = first_bad_batched_key((const u64*)keys, n, c.inst_N.data(), c.ninst);

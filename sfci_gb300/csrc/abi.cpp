@@ -346,11 +346,24 @@ int sfci_batch_create(int n, const char* const* in_paths, const int* num_orb, co
 int sfci_batch_lanczos(sfci_ctx* x, sfci_vec* const* v, int n, int Nl, int restarts, double* energies,
                        double* final_e) {
   if (!x || !v || !energies || !final_e) return set_error(SFCI_ERR_ARG, "null argument");
-  std::vector<Vec*> vs(n > 0 ? n : 0);
+  if (!x->c.ninst || x->c.W != 2) return set_error(SFCI_ERR_ARG, "batched Lanczos needs a batched context");
+  if (n != x->c.ninst) return set_error(SFCI_ERR_ARG, "batched Lanczos: one vector per instance");
+  std::vector<Vec*> vs(n);
   for (int i = 0; i < n; ++i) {
     if (!v[i] || v[i]->v.ctx != &x->c) return set_error(SFCI_ERR_ARG, "batched Lanczos: vector of another context");
     if (v[i]->v.len == 0) return set_error(SFCI_ERR_ARG, "batched Lanczos: an empty start vector");
     vs[i] = &v[i]->v;
+  }
+  // vector i must hold instance i's keys only: vectors are sorted by key and the
+  // tag is the key's top field, so the first and last keys carry every key's tag
+  for (int i = 0; i < n; ++i) {
+    const Vec& w = v[i]->v;
+    u64 hi[2] = {0ull, 0ull};
+    SFCI_CUDA(cudaMemcpyAsync(&hi[0], w.keys + 1, sizeof(u64), cudaMemcpyDeviceToHost, x->c.stream));
+    SFCI_CUDA(cudaMemcpyAsync(&hi[1], w.keys + 2 * (w.len - 1) + 1, sizeof(u64), cudaMemcpyDeviceToHost, x->c.stream));
+    SFCI_CUDA(cudaStreamSynchronize(x->c.stream));
+    if ((hi[0] >> INST_SHIFT) != (u64)i || (hi[1] >> INST_SHIFT) != (u64)i)
+      return set_error(SFCI_ERR_ARG, "batched Lanczos: vector " + std::to_string(i) + " holds keys of another instance");
   }
   return lanczos_batched(x->c, vs.data(), n, Nl, restarts, energies, final_e);
 }

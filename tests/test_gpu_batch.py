@@ -85,7 +85,8 @@ def test_batched_product_equals_unbatched_products(curve):
 def test_upload_rejects_keys_outside_the_batch(curve):
     """Uploads (and DiagCal_bit's host keys) are checked on the host before any
     copy: a tag naming no instance, or a bit at or above its instance's spin
-    orbitals, is SFCI_ERR_ARG and the vector keeps its contents."""
+    orbitals, is SFCI_ERR_ARG and the vector keeps its contents.  The batched
+    driver rejects vectors passed out of instance order."""
     orbs = [2 * M for M, _, _, _ in INSTANCES]
     nes = [ne for _, ne, _, _ in INSTANCES]
     bc = sg.Context.batch(curve, orbs, nes, Nd=10 ** 4)
@@ -102,6 +103,15 @@ def test_upload_rejects_keys_outside_the_batch(curve):
         with pytest.raises(sg.SfciError) as e:
             bc.DiagCal_bit(np.concatenate([good, bad]))
         assert e.value.status == "SFCI_ERR_ARG"
+    # the batched driver takes instance k's vector in place k
+    vs = []
+    for k, (M, ne, t, nd) in enumerate(INSTANCES):
+        w = bc.vec(nd)
+        w.upload(hf_tagged(ne, k), np.array([1.0]))
+        vs.append(w)
+    with pytest.raises(sg.SfciError) as e:
+        bc.batch_lanczos(vs[::-1], 4, 1)
+    assert e.value.status == "SFCI_ERR_ARG"
 
 
 @pytest.mark.parametrize("cap", [2000000, 3000])

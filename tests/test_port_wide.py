@@ -5,9 +5,11 @@ The reference stops at 64 spin orbitals (src/main.cpp:84-85), so the
 restatement's 128-bit path is the only checker for the 128-spin-orbital system.
 Here it runs the golden systems (at most 64 spin orbitals) with every key
 widened to two words, high word zero, and must reproduce the reference's
-diagonal elements, emitted terms, SpMSpV products, energies and vector algebra
-to the same tolerances as the one-word path (tests/test_port.py): the key
-width changes the representation, not the arithmetic."""
+diagonal elements, emitted terms, SpMSpV products, energies, vector algebra and
+Lanczos energies to the same tolerances as the one-word path
+(tests/test_port.py): the key width changes the representation, not the
+arithmetic.  The Lanczos runs take the two smaller systems, which keep the CPU
+suite short."""
 import numpy as np
 import pytest
 
@@ -88,3 +90,17 @@ def test_vector_algebra_and_energy_wide(port, golden_in, name):
     compare_vectors(g["add3_keys"], g["add3_amps"], narrow(k), a, capped=len(g["add3_amps"]) == int(g["add3_Nd"]))
     k, a = be.shrink_from(kB, aB, int(g["shrink_cap"]))
     compare_vectors(g["shrink_keys"], g["shrink_amps"], narrow(k), a, capped=True)
+
+
+@pytest.mark.parametrize("name", ["u8", "r16"])
+def test_lanczos_energies_wide(port, golden_in, name):
+    g, path = golden_in(name)
+    if "L_energies" not in g:
+        pytest.skip("no Lanczos case")
+    be = _setup(port, path, g, int(g["L_Nd"]))
+    en, fe, _ = port.lanczos(be, wide([g["hf"]]), np.array([1.0]), int(g["L_Nl"]), int(g["L_restarts"]),
+                             int(g["L_Nd"]), hpsi_cap=int(g["L_hpsi_cap"]))
+    ref = g["L_energies"]
+    assert len(en) == len(ref)
+    assert np.max(np.abs(en - ref)) < 1e-8
+    assert abs(fe - float(g["L_final_e"])) < 1e-8

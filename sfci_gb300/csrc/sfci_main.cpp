@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <exception>
 #include <fstream>
 #include <string>
 #include <vector>
@@ -18,11 +19,14 @@ struct Params {
   int Nl = 0, num_restart = 0, num_orb = 0, num_e = 0, num_thread = 0;
   unsigned long long bucket_unit = 60000;
   std::string filename, task, init_hf_text;
+  bool init_hf_ok = false;
   double coeff_cut = 1e-5, target_E = 0.0;
 };
 
-// decimal string -> 128-bit value
+// decimal string -> 128-bit value; false for other characters, no digits or
+// a value beyond 128 bits
 static bool parse_u128(const std::string& s, unsigned long long& lo, unsigned long long& hi) {
+  const unsigned __int128 top = ~(unsigned __int128)0;
   unsigned __int128 v = 0;
   bool any = false;
   for (char ch : s) {
@@ -30,12 +34,21 @@ static bool parse_u128(const std::string& s, unsigned long long& lo, unsigned lo
       if (ch == ' ' || ch == '\r' || ch == '\t') continue;
       return false;
     }
-    v = v * 10 + (unsigned)(ch - '0');
+    const unsigned d = (unsigned)(ch - '0');
+    if (v > (top - d) / 10) return false;
+    v = v * 10 + d;
     any = true;
   }
   lo = (unsigned long long)v;
   hi = (unsigned long long)(v >> 64);
   return any;
+}
+
+// the determinant has no bit at or above num_orb
+static bool fits_orbitals(unsigned long long lo, unsigned long long hi, int num_orb) {
+  if (num_orb >= 128) return true;
+  if (num_orb >= 64) return (hi >> (num_orb - 64)) == 0;
+  return hi == 0 && (lo >> num_orb) == 0;
 }
 
 static void parse(Params& p, const std::string& key, const std::string& val) {
@@ -50,7 +63,7 @@ static void parse(Params& p, const std::string& key, const std::string& val) {
   else if (key == "filename") { p.filename = val; echo(val); }
   else if (key == "coeff_cut") { p.coeff_cut = std::stod(val); echo(val); }
   else if (key == "bucket_unit") { p.bucket_unit = std::stoull(val); echo(val); }
-  else if (key == "init_hf") { p.init_hf_text = val; parse_u128(val, p.init_hf_lo, p.init_hf_hi); echo(val); }
+  else if (key == "init_hf") { p.init_hf_text = val; p.init_hf_ok = parse_u128(val, p.init_hf_lo, p.init_hf_hi); echo(val); }
   else if (key == "task") { p.task = val; echo(val); }
   else if (key == "target_E") { p.target_E = std::stod(val); echo(val); }
 }
@@ -64,7 +77,25 @@ int main(int argc, char** argv) {
     while (std::getline(f, raw)) {
       auto pos = raw.find('=');
       if (pos == std::string::npos) continue;  // the reference would misparse; skip instead
-      parse(p, raw.substr(0, pos), raw.substr(pos + 1));
+      const std::string key = raw.substr(0, pos), val = raw.substr(pos + 1);
+      try {
+        parse(p, key, val);
+      } catch (const std::exception&) {  // std::stoi and friends: not a number, or out of range
+        fprintf(stderr, "sfci: bad value for %s: %s\n", key.c_str(), val.c_str());
+        return 1;
+      }
+    }
+  }
+  if (p.task == "ground") {
+    if (!p.init_hf_ok) {
+      fprintf(stderr, "sfci: init_hf must be a decimal integer below 2^128: %s\n", p.init_hf_text.c_str());
+      return 1;
+    }
+    // (a num_orb outside [1, 128] is reported by the context set-up)
+    if (p.num_orb > 0 && p.num_orb <= 128 && !fits_orbitals(p.init_hf_lo, p.init_hf_hi, p.num_orb)) {
+      fprintf(stderr, "sfci: init_hf %s sets a spin orbital at or above num_orb=%d\n", p.init_hf_text.c_str(),
+              p.num_orb);
+      return 1;
     }
   }
   sfci_opts o{};

@@ -43,3 +43,27 @@ def test_sfci_binary_reports_a_missing_integral_file(tmp_path):
     r = subprocess.run([b.EXE], cwd=str(tmp_path), capture_output=True, text=True, timeout=120)
     assert r.returncode == 1
     assert "sfci:" in r.stderr
+
+
+@pytest.mark.parametrize("lines,msg", [
+    ("Nd=abc\n", "bad value for Nd"),
+    ("num_orb=twenty\n", "bad value for num_orb"),
+    ("Nl=99999999999999999999\n", "bad value for Nl"),
+    ("init_hf=10x23\n", "init_hf must be a decimal integer"),
+    ("init_hf=340282366920938463463374607431768211456\n", "init_hf must be a decimal integer"),  # 2^128
+    ("init_hf=1048576\n", "at or above num_orb=20"),  # bit 20 of a 20-spin-orbital system
+])
+def test_sfci_binary_rejects_bad_input_values(tmp_path, lines, msg):
+    """Runs without a GPU: sfci.input is parsed and checked before any device call.
+    A malformed number or an init_hf that does not fit num_orb spin orbitals is an
+    error message and exit status 1, not an abort."""
+    from sfci_gb300 import build as b
+    b.build()
+    base = {"task": "ground", "Nd": "100", "Nl": "5", "num_restart": "1", "num_orb": "20", "num_e": "10",
+            "init_hf": "1023", "filename": "missing_IN"}
+    k = lines.split("=", 1)[0]
+    base[k] = lines.split("=", 1)[1].strip()
+    (tmp_path / "sfci.input").write_text("".join("%s=%s\n" % kv for kv in base.items()))
+    r = subprocess.run([b.EXE], cwd=str(tmp_path), capture_output=True, text=True, timeout=120)
+    assert r.returncode == 1, (r.returncode, r.stderr)
+    assert msg in r.stderr, r.stderr
